@@ -1,0 +1,470 @@
+#!/usr/bin/env python3
+"""Benchmark of the ray-query hot path on one GB300 (or N replicas).
+
+Workload (one step): rebuild the LBVH of a 998,000-triangle fBm heightfield
+(1001 x 500 grid over [-1,1]^2, 5 octaves, amplitude 0.3), then trace
+1920 x 1080 x 4 jittered primary rays closest-hit, one cosine-weighted
+secondary ray per primary hit closest-hit, and one shadow ray per primary
+hit any-hit.  Geometry and rays are seeded synthetic data resident in HBM
+when the timed region starts; rays (265 MB per pass) exceed the 129 MB L2
+and L2 is additionally flushed (256 MB write) before every timed step.
+
+  value  = rays traced per second over the whole step (build included), Grays/s
+  e2e    = the same through the C ABI with pinned host buffers: mesh upload,
+           rebuild, ray upload and hit/bit download inside the timed region
+  roofline: the step's dominant kernel against measured HBM bandwidth, with
+           algorithmic bytes from the engine's traversal counters
+  cpu_baseline: the CPU oracle (the reference's algorithms: median BVH build,
+           collect-all division-slab traversal, Moller-Trumbore) on a bounded
+           sample of the same rays, all host threads
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "raytracer-data-structures_gb300"))
+
+METRIC = "closest-hit Grays/s & LBVH build Mtri/s; served p50/p99 latency vs plain"
+UNIT = "Grays/s"
+WORKLOAD = ("LBVH build + incoherent traversal: 998,000-triangle fBm heightfield (1001x500), "
+            "1920x1080x4 jittered primary closest-hit + cosine secondary closest-hit + shadow any-hit")
+SEED = 20261203
+EYE, TARGET, FOV = (0.0, -1.9, 1.9), (0.0, 0.15, 0.0), 40.0
+LIGHT = (1.5, -1.0, 3.0)
+RAY_BYTES, HIT_BYTES, NODE_BYTES, TRI_BYTES = 32, 16, 64, 48
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_inputs():
+    import scenes
+    verts, idx = scenes.heightfield(1001, 500, amplitude=0.3, octaves=5, seed=SEED % 1000)
+    primary = scenes.pinhole_rays(1920, 1080, 4, eye=EYE, target=TARGET, fov_deg=FOV, seed=SEED + 1)
+    return verts, idx, primary
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "trace_lbvh_heightfield.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith(f"dram_bytes_per_launch[{kernel_key}]:"):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import torch
+    import rq
+    import scenes
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    verts, idx, primary = make_inputs()
+    n_tri = len(idx)
+    eng = rq.Engine(local)
+    eng.set_stream(stream.cuda_stream)
+    d_verts = torch.from_numpy(verts).to(dev)
+    d_idx = torch.from_numpy(idx.view(np.int32)).to(dev)
+    scene = eng.scene_triangles(d_verts, d_idx)
+    acc = eng.build(scene, rq.LBVH)
+
+    def dev_rays(r):
+        return torch.from_numpy(np.ascontiguousarray(r).view(np.uint8)).to(dev)
+
+    d_prim = dev_rays(primary)
+    n_p = len(primary)
+    d_hits_p = torch.empty(n_p * HIT_BYTES, dtype=torch.uint8, device=dev)
+    eng.trace_closest(acc, d_prim, d_hits_p)
+    eng.synchronize()
+    hits_p = d_hits_p.cpu().numpy().view(rq.HIT_DTYPE)
+    secondary = scenes.cosine_rays(verts, idx, primary, hits_p, seed=SEED + 2)
+    shadow = scenes.shadow_rays(verts, idx, primary, hits_p, LIGHT)
+    n_s, n_sh = len(secondary), len(shadow)
+    d_sec, d_sh = dev_rays(secondary), dev_rays(shadow)
+    d_hits_s = torch.empty(n_s * HIT_BYTES, dtype=torch.uint8, device=dev)
+    d_bits = torch.empty(((n_sh + 31) // 32) * 4, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    total_rays = n_p + n_s + n_sh
+    log(f"[bench] tris={n_tri} primary={n_p} secondary={n_s} shadow={n_sh}")
+
+    # Traversal work of each query on these exact rays (the byte model's inputs).
+    counts = {}
+    for name, rays, anyhit in (("primary", primary, False), ("secondary", secondary, False), ("shadow", shadow, True)):
+        _, cnt = eng.trace_counters(acc, rays, any_hit=anyhit)
+        counts[name] = (int(cnt[0]), int(cnt[1]))
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def step(marks=None):
+        if marks: marks[0].record(stream)
+        acc.rebuild()
+        if marks: marks[1].record(stream)
+        eng.trace_closest(acc, d_prim, d_hits_p)
+        if marks: marks[2].record(stream)
+        eng.trace_closest(acc, d_sec, d_hits_s)
+        if marks: marks[3].record(stream)
+        eng.trace_any(acc, d_sh, d_bits)
+        if marks: marks[4].record(stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    eng.synchronize()
+
+    launches0 = rq.kernel_launch_count()
+    phase = np.zeros((args.steps, 4))
+    step_ms = np.zeros(args.steps)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            marks = [ev() for _ in range(5)]
+            step(marks)
+            torch.cuda.synchronize(dev)
+            step_ms[k] = marks[0].elapsed_time(marks[4])
+            phase[k] = [marks[i].elapsed_time(marks[i + 1]) for i in range(4)]
+    eng.synchronize()
+    launches = rq.kernel_launch_count() - launches0
+    mean_ms = float(step_ms.mean())
+    if ws > 1:
+        t = torch.tensor([mean_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        mean_ms = float(t.item())
+    value = ws * total_rays / (mean_ms * 1e-3) / 1e9
+    ph = phase.mean(0)
+    build_ms, prim_ms, sec_ms, sh_ms = ph
+
+    # Roofline of the dominant kernel (largest share of the step).
+    kern = {"build": build_ms, "trace_primary": prim_ms, "trace_secondary": sec_ms, "trace_shadow": sh_ms}
+    dom = max(kern, key=kern.get)
+    peak, peak_kind = measured_peaks()
+
+    def trace_bytes(name, n, closest=True):
+        v, t = counts[name]
+        return n * RAY_BYTES + (n * HIT_BYTES if closest else ((n + 31) // 32) * 4) + v * NODE_BYTES + t * TRI_BYTES
+
+    build_bytes = build_bytes_per_tri() * n_tri
+    alg = {"build": build_bytes, "trace_primary": trace_bytes("primary", n_p),
+           "trace_secondary": trace_bytes("secondary", n_s), "trace_shadow": trace_bytes("shadow", n_sh, False)}
+    achieved = alg[dom] / (kern[dom] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": profile_traffic(dom), "algorithmic_bytes": int(alg[dom]),
+                "compulsory_frac": round((((n_p if dom == "trace_primary" else n_s if dom == "trace_secondary" else n_sh)
+                                           * (RAY_BYTES + HIT_BYTES)) / (kern[dom] * 1e-3) / 1e9) / peak, 4)
+                if dom != "build" else None}
+
+    e2e = None
+    if rank == 0 and not args.skip_e2e:
+        e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(verts, idx, primary, secondary, shadow, budget_s=args.cpu_budget)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "dataStructure": "LBVH", "triangles": n_tri, "primary_rays": n_p,
+                       "secondary_rays": n_s, "shadow_rays": n_sh, "seed": SEED,
+                       "l2": "flushed before every timed step (256 MB write); rays exceed L2",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "lbvh_build_mtri_s": round(n_tri / (build_ms * 1e-3) / 1e6, 2),
+            "closest_grays_s": round((n_p + n_s) / ((prim_ms + sec_ms) * 1e-3) / 1e9, 4),
+            "any_grays_s": round(n_sh / (sh_ms * 1e-3) / 1e9, 4),
+            "phase_ms": {"build": round(build_ms, 4), "trace_primary": round(prim_ms, 4),
+                         "trace_secondary": round(sec_ms, 4), "trace_shadow": round(sh_ms, 4)},
+            "traversal_work": {k: {"nodes_per_ray": round(v[0] / max(1, {"primary": n_p, "secondary": n_s, "shadow": n_sh}[k]), 3),
+                                   "tris_per_ray": round(v[1] / max(1, {"primary": n_p, "secondary": n_s, "shadow": n_sh}[k]), 3)}
+                               for k, v in counts.items()},
+            "roofline": roofline,
+            "build_roofline": {"achieved": round(build_bytes / (build_ms * 1e-3) / 1e9, 1), "peak": peak,
+                               "unit": "GB/s", "bytes_per_tri": build_bytes_per_tri(),
+                               "frac": round(build_bytes / (build_ms * 1e-3) / 1e9 / peak, 4)},
+            "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),
+        }
+        print(json.dumps(out), flush=True)
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def build_bytes_per_tri():
+    """Compulsory bytes per triangle of the LBVH build kernels:
+    bounds 6 (12 B per vertex, 0.5 vertex per triangle) + Morton 26 (12 B indices,
+    6 B vertices, 8 B code/index write) + 4 sort passes x 16 + Karras 28 (code
+    read 4, links 16, parents 8) + refit 150 (order 4, indices 12, vertices 6,
+    48 B payload write, 24 B child box write, 48 B sibling reread per internal
+    node, 4 B parent link, 4 B flag)."""
+    return 6 + 26 + 64 + 28 + 150
+
+
+def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args):
+    import torch
+    import rq
+
+    def pinned(a):
+        a = np.ascontiguousarray(a)
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        v = t.numpy().view(a.dtype).reshape(a.shape)
+        v[...] = a
+        return t, v
+
+    keep = []
+    tv, hv = pinned(verts); keep.append(tv)
+    ti, hi = pinned(idx); keep.append(ti)
+    tp, hp = pinned(primary); keep.append(tp)
+    ts, hs = pinned(secondary); keep.append(ts)
+    tsh, hsh = pinned(shadow); keep.append(tsh)
+    th1, out_p = pinned(np.zeros(len(primary), rq.HIT_DTYPE)); keep.append(th1)
+    th2, out_s = pinned(np.zeros(len(secondary), rq.HIT_DTYPE)); keep.append(th2)
+    tb, out_b = pinned(np.zeros((len(shadow) + 31) // 32, np.uint32)); keep.append(tb)
+
+    def step():
+        scene.update(hv, hi)
+        acc.rebuild()
+        eng.trace_closest(acc, hp, out_p)
+        eng.trace_closest(acc, hs, out_s)
+        eng.trace_any(acc, hsh, out_b)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    eng.synchronize()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    eng.synchronize()
+    t = float(np.mean(times))
+    rays = len(primary) + len(secondary) + len(shadow)
+    h2d = hv.nbytes + hi.nbytes + hp.nbytes + hs.nbytes + hsh.nbytes
+    d2h = out_p.nbytes + out_s.nbytes + out_b.nbytes
+    return {"value": round(rays / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3)}
+
+
+# -------------------------------------------------------------- CPU baseline
+
+class CpuBaseline:
+    """The reference's algorithms on the host cores (the oracle port): median
+    BVH build (constructBVHNew's partition + nth_element, one thread as the
+    reference runs it), collect-all division-slab traversal (boxIntersect)
+    with Moller-Trumbore closest hit and any hit for shadow rays, on all host
+    threads.  A bounded, seeded sample of each ray class is traced; the
+    whole-job time is the build time plus the measured per-ray cost times the
+    full ray counts."""
+
+    def __init__(self, verts, idx, samples, counts, budget_s=20.0):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
+        self.O = O
+        self.cores = os.cpu_count() or 1
+        self.prims, aabb, cen = O.tri_prims(verts, idx)
+        t0 = time.perf_counter()
+        self.bvh = O.build_median(aabb, cen, compat=True)
+        self.build_s = time.perf_counter() - t0
+        self.n_tri = len(idx)
+        self.counts = counts
+        self.pool = samples  # name -> (rays, query)
+        rng = np.random.default_rng(SEED + 9)
+        self.sample = 256
+        while True:
+            self.sel = {k: rng.choice(len(r), size=min(self.sample, len(r)), replace=False)
+                        for k, (r, q) in self.pool.items()}
+            per = self.measure()
+            spent = sum(per[k] * len(self.sel[k]) for k in per)
+            if spent > budget_s / 10 or self.sample >= 1 << 15:
+                break
+            self.sample *= 4
+
+    def measure(self):
+        O = self.O
+        per = {}
+        for k, (rays, q) in self.pool.items():
+            r = rays[self.sel[k]]
+            t1 = time.perf_counter()
+            O.trace_bvh2(O.TRIANGLES, O.REFERENCE, q, self.bvh, self.prims, r, nthreads=self.cores)
+            per[k] = (time.perf_counter() - t1) / len(r)
+        return per
+
+    def record(self, per):
+        trace_s = sum(per[k] * self.counts[k] for k in per)
+        value = sum(self.counts.values()) / (self.build_s + trace_s) / 1e9
+        return {"value": value, "unit": UNIT, "cores": self.cores, "kind": "port",
+                "sample": (f"median-BVH build of all {self.n_tri} triangles (1 thread, {self.build_s:.2f} s) + "
+                           f"{self.sample} seeded rays per class (primary/secondary/shadow) traced with the "
+                           f"reference's collect-all traversal on {self.cores} threads; whole job = build + "
+                           f"per-ray cost x full ray counts"),
+                "build_s": round(self.build_s, 3), "per_ray_us": {k: round(v * 1e6, 3) for k, v in per.items()}}
+
+
+def cpu_baseline(verts, idx, primary, secondary, shadow, budget_s=20.0):
+    O_any, O_closest = 1, 0
+    cb = CpuBaseline(verts, idx, {"primary": (primary, O_closest), "secondary": (secondary, O_closest),
+                                  "shadow": (shadow, O_any)},
+                     {"primary": len(primary), "secondary": len(secondary), "shadow": len(shadow)}, budget_s)
+    return cb.record(cb.measure())
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    verts, idx, primary = make_inputs()
+    import scenes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as O
+    # Secondary and shadow rays start at primary hits: find the hits of a
+    # seeded subset of primary rays with the oracle, and scale the counts by
+    # the subset's hit fraction.
+    prims, aabb, cen = O.tri_prims(verts, idx)
+    bvh = O.build_median(aabb, cen)
+    rng = np.random.default_rng(SEED + 7)
+    sub = primary[rng.choice(len(primary), size=min(100_000, len(primary)), replace=False)]
+    h = O.trace_bvh2(O.TRIANGLES, O.FAST, O.CLOSEST, bvh, prims, sub)
+    secondary = scenes.cosine_rays(verts, idx, sub, h, seed=SEED + 2)
+    shadow = scenes.shadow_rays(verts, idx, sub, h, LIGHT)
+    n_hit = int(round(len(primary) * len(secondary) / len(sub)))
+    counts = {"primary": len(primary), "secondary": n_hit, "shadow": n_hit}
+    cb = CpuBaseline(verts, idx, {"primary": (sub, O.CLOSEST), "secondary": (secondary, O.CLOSEST),
+                                  "shadow": (shadow, O.ANY)}, counts, budget_s=args.cpu_budget)
+    vals, rec = [], None
+    for k in range(args.warmup + args.steps):
+        rec = cb.record(cb.measure())
+        if k >= args.warmup:
+            vals.append(rec["value"])
+    v = float(np.mean(vals))
+    rec["value"] = v
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": WORKLOAD, "dataStructure": "BVH (the reference's median builder)",
+                      "triangles": len(idx), "primary_rays": counts["primary"],
+                      "secondary_rays": counts["secondary"], "shadow_rays": counts["shadow"], "seed": SEED},
+           "cpu_baseline": rec,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("[bench] warm-up raised to 3 steps")
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,251 @@
+/*
+ * rq.h — C ABI of the GB300 ray-query engine (acceleration-structure build +
+ * ray traversal for sm_103a, one GPU).
+ *
+ * The engine replaces the hot path of the reference CPU ray tracer
+ * (Alhajras/Raytracer-Data-structures, project/raytracer/): the builders
+ * behind the Settings::dataStructure switch and the queries castRay makes
+ * through them.  Every entry point below names the reference interface it
+ * replaces.  Plain C types only: opaque handles, pointers and sizes.
+ *
+ * Conventions
+ *  - Every call returns rq_status_t; no exception crosses the ABI.
+ *    rq_last_error(ctx) describes the last failure on that context.
+ *  - Device memory of scenes and acceleration structures is owned by the
+ *    engine.  Caller buffers are host memory unless RQ_DEVICE_POINTERS is set
+ *    in `flags`, in which case they are device pointers on the context's
+ *    device.
+ *  - Host-pointer calls are synchronous.  Device-pointer calls are enqueued
+ *    on the context's stream (rq_set_stream) and return at once; device-side
+ *    errors (traversal stack overflow, a bounded wait that gave up) are then
+ *    reported by rq_synchronize.
+ *  - A context is used by one host thread at a time; distinct contexts may be
+ *    used concurrently.
+ */
+#ifndef RQ_H
+#define RQ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RQ_ABI_VERSION 1
+
+typedef enum rq_status_t {
+  RQ_SUCCESS = 0,
+  RQ_ERROR_INVALID_ARGUMENT = 1, /* null handle/pointer, size out of range, NaN input, bad index */
+  RQ_ERROR_UNSUPPORTED = 2,      /* e.g. UNIFORM_GRID, declared but never built by the reference */
+  RQ_ERROR_OUT_OF_MEMORY = 3,
+  RQ_ERROR_CUDA = 4,             /* a CUDA runtime call failed; see rq_last_error */
+  RQ_ERROR_STACK_OVERFLOW = 5,   /* a traversal stack would have overflowed; the ray was abandoned */
+  RQ_ERROR_TIMEOUT = 6,          /* a bounded device-side wait gave up */
+  RQ_ERROR_EMPTY_SCENE = 7,      /* zero primitives (undefined behaviour in the reference) */
+  RQ_ERROR_NO_DEVICE = 8
+} rq_status_t;
+
+/* AccType, accelerators.h:21 — same names and values. */
+typedef enum rq_acc_type_t {
+  RQ_BVH = 0,          /* median/midpoint BVH, constructBVHNew accelerators.h:246 */
+  RQ_KDTREE = 1,       /* SAH KD-tree, constructKDTreeNew accelerators.h:951 */
+  RQ_UNIFORM_GRID = 2, /* declared by the reference, never implemented: RQ_ERROR_UNSUPPORTED */
+  RQ_LBVH = 3,         /* Morton + radix sort + Karras + refit (cited at accelerators.h:371,568) */
+  RQ_NONE = 4          /* brute force, castRay default branch main.cpp:373-387 */
+} rq_acc_type_t;
+
+/* SceneModel, settings.h:4 — same names and values. */
+typedef enum rq_scene_model_t {
+  RQ_IGEA = 0, RQ_ARMADILLO = 1, RQ_BUNNY = 2, RQ_BUNNIES = 3,
+  RQ_TEST = 4, RQ_GRASS = 5, RQ_BUDDHA = 6, RQ_CITY = 7
+} rq_scene_model_t;
+
+/* Settings, settings.h:7-17: the reference's fields in the reference's order
+ * with the reference's defaults (rq_settings_default), followed by engine
+ * fields. */
+typedef struct rq_settings_t {
+  uint32_t width;             /* 640 */
+  uint32_t height;            /* 480 */
+  float fov;                  /* 90; the reference's render() ignores it and uses 30 (main.cpp:545) */
+  float backgroundColor[3];   /* (1, 1, 1) */
+  float bias;                 /* 1e-4 */
+  uint32_t aa_samples;        /* 1 */
+  int32_t dataStructure;      /* rq_acc_type_t, RQ_BVH */
+  int32_t sceneModel;         /* rq_scene_model_t, RQ_BUNNY */
+  /* ---- engine fields ---- */
+  int32_t traversal;          /* rq_traversal_t, RQ_TRAVERSAL_FAST */
+  int32_t morton;             /* rq_morton_t, RQ_MORTON_SCENE_BOUNDS */
+  int32_t kd_max_depth;       /* <= 0: round(8 + 1.3 log2 N) as the reference (accelerators.h:958) */
+  int32_t reserved[5];
+} rq_settings_t;
+
+/* How rays meet boxes and primitives. */
+typedef enum rq_traversal_t {
+  /* Reciprocal-direction slab test clipped to [tmin, closest hit], widened by
+   * 1 + 2*gamma(3) so no box is lost to rounding; near child first; hits
+   * limited to (tmin, tmax). */
+  RQ_TRAVERSAL_FAST = 0,
+  /* The reference's semantics: division slab test with no clipping
+   * (accelerators.h:588-626), boxIntersect's pre-order candidate walk
+   * (accelerators.h:668-690), castRay's closest selection (t0 < 0 -> t1,
+   * strict <, main.cpp:343-358), kdtreeIntersect's any-hit
+   * (accelerators.h:997-1086).  Reproduces the reference's pixels. */
+  RQ_TRAVERSAL_REFERENCE = 1
+} rq_traversal_t;
+
+/* Centroid normalisation before morton3D. */
+typedef enum rq_morton_t {
+  RQ_MORTON_SCENE_BOUNDS = 0, /* (c - lo) / (hi - lo); lo/hi = vertex box (triangles) or centre box (spheres) */
+  RQ_MORTON_REFERENCE = 1     /* (c + 30) / 1000, accelerators.h:577 */
+} rq_morton_t;
+
+/* Flags for calls that take caller buffers. */
+#define RQ_DEVICE_POINTERS 0x1u
+
+/* Ray, 32 bytes: the origin/direction pair castRay receives (main.cpp:291-298)
+ * plus the query interval. */
+typedef struct rq_ray_t {
+  float org[3];
+  float tmin;
+  float dir[3];
+  float tmax;
+} rq_ray_t;
+
+/* Closest hit, 16 bytes.  prim = RQ_MISS and t = tmax when nothing is hit.
+ * u, v: barycentrics for triangles, 0 for spheres. */
+typedef struct rq_hit_t {
+  float t;
+  uint32_t prim;
+  float u;
+  float v;
+} rq_hit_t;
+
+#define RQ_MISS 0xFFFFFFFFu
+
+typedef struct rq_context* rq_ctx_t;
+typedef struct rq_scene* rq_scene_t;
+typedef struct rq_accel* rq_accel_t;
+
+/* Description of a built structure, for the caller and for parity checks. */
+typedef struct rq_accel_info_t {
+  int32_t type;            /* rq_acc_type_t */
+  int32_t prim_kind;       /* 0 triangles, 1 spheres */
+  uint32_t n_prims;
+  uint32_t n_nodes;        /* BVH2: internal nodes; KD: nodes */
+  uint32_t n_slots;        /* BVH2: leaf slots; KD: primitive-index entries */
+  uint32_t max_depth;      /* KD: depth limit used */
+  float root_bounds[6];    /* min xyz, max xyz */
+  uint64_t device_bytes;   /* device memory held by the structure */
+} rq_accel_info_t;
+
+/* ------------------------------------------------------------ lifecycle */
+
+/* Defaults of settings.h:7-17 plus engine defaults. */
+void rq_settings_default(rq_settings_t* s);
+
+/* Replaces the implicit global state of main() (main.cpp:723-760).  Binds
+ * `device` (a CUDA ordinal); settings may be NULL for defaults. */
+rq_status_t rq_create(const rq_settings_t* settings, int device, rq_ctx_t* out);
+rq_status_t rq_destroy(rq_ctx_t ctx);
+rq_status_t rq_get_settings(rq_ctx_t ctx, rq_settings_t* out);
+rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* settings);
+/* cudaStream_t passed as void*; NULL selects the engine's own stream. */
+rq_status_t rq_set_stream(rq_ctx_t ctx, void* cuda_stream);
+rq_status_t rq_synchronize(rq_ctx_t ctx);
+const char* rq_last_error(rq_ctx_t ctx);
+const char* rq_status_string(rq_status_t status);
+
+/* ----------------------------------------------------------------- scenes */
+
+/* Triangle mesh: verts = nv * 3 floats, idx = nt * 3 uint32 (the OBJ `v`/`f`
+ * content the reference's loader, main.cpp:599-721, reads only as points).
+ * Validated: finite vertices, indices < nv, nt > 0. */
+rq_status_t rq_scene_create_triangles(rq_ctx_t ctx, const float* verts, uint32_t nv,
+                                      const uint32_t* idx, uint32_t nt, uint32_t flags,
+                                      rq_scene_t* out);
+/* Spheres: n * (cx, cy, cz, r), the SceneObject list createScene_new builds
+ * (main.cpp:677-692, 702-717); primitive id = position. */
+rq_status_t rq_scene_create_spheres(rq_ctx_t ctx, const float* center_radius, uint32_t n,
+                                    uint32_t flags, rq_scene_t* out);
+/* Overwrite a scene's geometry with the same counts (dynamic scenes; follow
+ * with rq_accel_rebuild): data = vertices (triangles) or spheres; idx = new
+ * triangle indices, or NULL to keep them. */
+rq_status_t rq_scene_update(rq_ctx_t ctx, rq_scene_t scene, const float* data, const uint32_t* idx,
+                            uint32_t flags);
+rq_status_t rq_scene_destroy(rq_scene_t scene);
+
+/* ----------------------------------------------------------------- builds */
+
+/* The dataStructure switch of main() (main.cpp:791-843):
+ *   RQ_BVH    -> constructBVHNew (accelerators.h:246)
+ *   RQ_KDTREE -> constructKDTreeNew (accelerators.h:951)
+ *   RQ_LBVH   -> constructLBVHTree (accelerators.h:570), as a Karras LBVH
+ *   RQ_NONE   -> no structure; queries test every primitive
+ * Uses the context's settings (morton normalisation, kd_max_depth). */
+rq_status_t rq_build(rq_ctx_t ctx, rq_scene_t scene, int32_t acc_type, rq_accel_t* out);
+/* Rebuild in place from the (possibly updated) scene, reusing device memory. */
+rq_status_t rq_accel_rebuild(rq_ctx_t ctx, rq_accel_t accel);
+rq_status_t rq_accel_destroy(rq_accel_t accel);
+rq_status_t rq_accel_get_info(rq_accel_t accel, rq_accel_info_t* info);
+
+/* Host copies of a built structure (layouts in the engine documentation):
+ * BVH2 (RQ_BVH, RQ_LBVH): nodes = n_nodes * 16 words, order = n_slots ids,
+ * sorted_codes = n_prims Morton codes in slot order (RQ_LBVH only; may be
+ * NULL).  KD: nodes = n_nodes * 3 words in the reference's KdAccelNode
+ * encoding (accelerators.h:715-742), prim_idx = n_slots ids. */
+rq_status_t rq_accel_export_bvh2(rq_ctx_t ctx, rq_accel_t accel, float* nodes, uint32_t* order,
+                                 uint32_t* sorted_codes);
+rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t accel, int32_t* nodes, int32_t* prim_idx);
+
+/* ---------------------------------------------------------------- queries */
+
+/* Closest hit per ray: replaces boxIntersect + castRay's candidate loop
+ * (accelerators.h:668-690, main.cpp:330-388). */
+rq_status_t rq_trace_closest(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n,
+                             rq_hit_t* hits, uint32_t flags);
+/* Any hit within (tmin, tmax) per ray, one bit per ray (bit r%32 of word
+ * r/32): replaces kdtreeIntersect (accelerators.h:997) and the shadow query
+ * trace_more (main.cpp:235-245, a stub returning false). */
+rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n,
+                         uint32_t* occluded_bits, uint32_t flags);
+
+/* The FAST closest/any query of rq_trace_closest / rq_trace_any that also
+ * sums, over all rays, the internal nodes visited (counters[0]) and the
+ * primitives tested (counters[1]): the inputs of the traversal byte model.
+ * BVH2 structures (RQ_BVH, RQ_LBVH).  Synchronous; results go to `out`
+ * (hits or occlusion bits) as in the plain calls. */
+rq_status_t rq_trace_counters(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n,
+                              int32_t any, void* out, uint64_t* counters, uint32_t flags);
+
+/* Kernel launches the engine has made in this process, over all contexts. */
+uint64_t rq_kernel_launch_count(void);
+
+/* --------------------------------------------------- component kernels */
+
+/* morton3D over centroids (accelerators.h:374-394, 575-580): codes for the
+ * scene's primitives with the context's normalisation, in primitive order. */
+rq_status_t rq_morton_codes(rq_ctx_t ctx, rq_scene_t scene, uint32_t* codes, uint32_t flags);
+/* Stable LSD radix sort of (key, value) pairs on the low `key_bits` bits:
+ * what radixSort (accelerators.h:348-369) intends (it sorts a by-value copy
+ * and so has no effect).  In place. */
+rq_status_t rq_sort_pairs(rq_ctx_t ctx, uint32_t* keys, uint32_t* values, uint32_t n,
+                          uint32_t key_bits, uint32_t flags);
+
+/* ------------------------------------------------------------ render step */
+
+/* render() (main.cpp:541-566) with castRay's shading (main.cpp:390-497) for
+ * a sphere scene: pinhole camera at the origin looking down -z, fov 30,
+ * aa_samples jittered samples per pixel, one point light at (0, 3, 30).
+ * jitter: 2 doubles per sample in (y, x, sample) order; NULL draws the
+ * reference's default-seeded mt19937 sequence.  surface_rgb: 3 floats per
+ * sphere.  pixels: width*height*3 bytes of the P6 payload (main.cpp:516-528).
+ * rgb_sum (may be NULL): per-pixel colour sums before quantisation. */
+rq_status_t rq_render_reference(rq_ctx_t ctx, rq_accel_t accel, const rq_settings_t* settings,
+                                const double* jitter, const float* surface_rgb, uint8_t* pixels,
+                                float* rgb_sum);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RQ_H */

@@ -1,0 +1,172 @@
+// Build orchestration: the dataStructure switch of main() (main.cpp:791-843)
+// over the engine's kernels, the LBVH pipeline, query dispatch and
+// device-side input validation.
+#include <atomic>
+
+#include "rq_build.hpp"
+#include "rq_device.cuh"
+
+namespace rq {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+uint64_t launch_total() { return g_launches.load(std::memory_order_relaxed); }
+
+namespace {
+
+constexpr int kSortPasses = 4;  // 30-bit Morton codes, 8-bit digits
+
+#define RQ_B(call, what)                                           \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return BuildResult::cuda_error(e_, what); \
+  } while (0)
+
+__global__ void k_validate(const float* __restrict__ verts, uint32_t nv, const uint32_t* __restrict__ idx,
+                           uint32_t nt, const float4* __restrict__ sph, uint32_t n, uint32_t* err) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool bad = false;
+  if (i < nv * 3ull) bad |= !isfinite(verts[i]);
+  if (i < nt * 3ull) bad |= idx[i] >= nv;
+  if (i < n) {
+    float4 s = sph[i];
+    bad |= !(isfinite(s.x) && isfinite(s.y) && isfinite(s.z) && isfinite(s.w) && s.w >= 0.f);
+  }
+  if (bad) atomicOr(err, kErrBadInput);
+}
+
+}  // namespace
+
+void launch_validate(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                     const float4* sph, uint32_t n, uint32_t* err, cudaStream_t st) {
+  uint64_t m = (uint64_t)nv * 3;
+  if ((uint64_t)nt * 3 > m) m = (uint64_t)nt * 3;
+  if (n > m) m = n;
+  if (m == 0) return;
+  count_launch();
+  k_validate<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(verts, nv, idx, nt, sph, n, err);
+}
+
+// Zero region layout: [hist 1024][counters 16][status words][refit flags]
+static size_t zero_words(uint32_t n, int passes) {
+  return 1024 + 16 + sort_status_words(n, passes) + (n > 1 ? n - 1 : 0);
+}
+
+BuildResult sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, bool compute_hist,
+                       BuildScratch& sc, uint32_t* err, cudaStream_t st) {
+  if (n <= 1) return {};
+  RQ_B(sc.keys_alt.ensure((size_t)n * 4), "sort scratch");
+  RQ_B(sc.vals_alt.ensure((size_t)n * 4), "sort scratch");
+  if (compute_hist) {
+    RQ_B(sc.zero.ensure(zero_words(n, passes) * 4), "sort scratch");
+    RQ_B(cudaMemsetAsync(sc.zero.p, 0, (1024 + 16 + sort_status_words(n, passes)) * 4, st), "memset");
+    launch_histogram(keys, n, passes, sc.zero.as<uint32_t>(), st);
+  }
+  uint32_t* z = sc.zero.as<uint32_t>();
+  SortScratch s{sc.keys_alt.as<uint32_t>(), sc.vals_alt.as<uint32_t>(), z, z + 1040, z + 1024};
+  launch_onesweep(keys, vals, n, passes, s, err, st);
+  RQ_B(cudaGetLastError(), "radix sort launch");
+  return {};
+}
+
+BuildResult morton_codes(const SceneView& s, int mode, uint32_t* codes, uint32_t* vals,
+                         uint32_t* hist, BuildScratch& sc, cudaStream_t st) {
+  RQ_B(sc.lohi.ensure(64), "scratch");
+  int32_t* lohi = sc.lohi.as<int32_t>();
+  if (s.kind == kTriangles) {
+    launch_init_bounds(lohi, st);
+    launch_point_bounds(s.verts, s.nv, 3, lohi, st);
+    launch_morton_tris(s.verts, s.idx, s.n, lohi, codes, vals, hist, st);
+  } else {
+    if (mode == RQ_MORTON_SCENE_BOUNDS) {
+      launch_init_bounds(lohi, st);
+      launch_point_bounds(reinterpret_cast<const float*>(s.sph), s.n, 4, lohi, st);
+    }
+    launch_morton_spheres(s.sph, s.n, mode, lohi, codes, vals, hist, st);
+  }
+  RQ_B(cudaGetLastError(), "morton launch");
+  return {};
+}
+
+static BuildResult build_lbvh(const SceneView& s, const rq_settings_t& cfg, AccelBuffers& a,
+                              BuildScratch& sc, uint32_t* err, cudaStream_t st) {
+  const uint32_t n = s.n;
+  const size_t payload = s.kind == kTriangles ? 48 : 16;
+  RQ_B(a.nodes.ensure((size_t)(n > 1 ? n - 1 : 1) * 64), "LBVH nodes");
+  RQ_B(a.prims.ensure((size_t)n * payload), "LBVH payload");
+  RQ_B(a.order.ensure((size_t)n * 4), "LBVH order");
+  RQ_B(a.codes.ensure((size_t)n * 4), "LBVH codes");
+  RQ_B(a.root.ensure(32), "LBVH root");
+  RQ_B(sc.keys_alt.ensure((size_t)n * 4), "sort scratch");
+  RQ_B(sc.vals_alt.ensure((size_t)n * 4), "sort scratch");
+  RQ_B(sc.zero.ensure(zero_words(n, kSortPasses) * 4), "build scratch");
+  RQ_B(sc.parent.ensure((size_t)(2 * (uint64_t)n) * 4), "parent links");
+  uint32_t* z = sc.zero.as<uint32_t>();
+  RQ_B(cudaMemsetAsync(z, 0, zero_words(n, kSortPasses) * 4, st), "memset");
+  uint32_t* codes = a.codes.as<uint32_t>();
+  uint32_t* order = a.order.as<uint32_t>();
+  BuildResult r = morton_codes(s, cfg.morton, codes, order, z, sc, st);
+  if (!r.ok()) return r;
+  r = sort_pairs(codes, order, n, kSortPasses, false, sc, err, st);
+  if (!r.ok()) return r;
+  launch_karras(codes, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(), st);
+  uint32_t* flags = z + 1040 + sort_status_words(n, kSortPasses);
+  launch_refit(s.kind, s.verts, s.idx, s.sph, order, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(),
+               flags, a.prims.as<float4>(), a.root.as<float>(), err, st);
+  RQ_B(cudaGetLastError(), "LBVH launch");
+  a.n_nodes = n > 1 ? n - 1 : 0;
+  a.n_slots = n;
+  a.max_depth = 0;
+  return {};
+}
+
+static BuildResult build_none(const SceneView& s, AccelBuffers& a, cudaStream_t st) {
+  const size_t payload = s.kind == kTriangles ? 48 : 16;
+  RQ_B(a.prims.ensure((size_t)s.n * payload), "payload");
+  launch_prims_by_id(s.kind, s.verts, s.idx, s.sph, s.n, a.prims.as<float4>(), nullptr, st);
+  RQ_B(cudaGetLastError(), "payload launch");
+  a.n_nodes = 0;
+  a.n_slots = 0;
+  return {};
+}
+
+BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, AccelBuffers& a,
+                        BuildScratch& sc, uint32_t* err, cudaStream_t st) {
+  if (s.n == 0) return BuildResult::error(RQ_ERROR_EMPTY_SCENE, "empty scene");
+  switch (type) {
+    case RQ_LBVH: return build_lbvh(s, cfg, a, sc, err, st);
+    case RQ_BVH: return build_median_bvh(s, a, sc, err, st);
+    case RQ_KDTREE: return build_kd_tree(s, cfg.kd_max_depth, a, sc, err, st);
+    case RQ_NONE: return build_none(s, a, st);
+    default: return BuildResult::error(RQ_ERROR_UNSUPPORTED, "unsupported dataStructure");
+  }
+}
+
+void launch_query(int type, const SceneView& s, const AccelBuffers& a, int traversal, bool any,
+                  const QueryTarget& q, uint32_t* err, cudaStream_t st) {
+  if (type == RQ_NONE) {
+    launch_trace_brute(s.kind, traversal, any, a.prims.as<const float4>(), s.n, q.rays, q.n, q.hits,
+                       q.occ, st);
+  } else if (type == RQ_KDTREE) {
+    KdView v{a.kd_nodes.as<const int4>(), a.kd_idx.as<const int32_t>(), a.prims.as<const float4>(),
+             a.root.as<const float>()};
+    launch_trace_kd(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
+  } else {
+    Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+               a.root.as<const float>(), a.n_nodes, a.n_slots};
+    launch_trace_bvh2(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
+  }
+}
+
+BuildResult trace_counted(int type, const SceneView& s, const AccelBuffers& a, bool any, const QueryTarget& q,
+                          unsigned long long* counters, uint32_t* err, cudaStream_t st) {
+  if (type != RQ_LBVH && type != RQ_BVH)
+    return BuildResult::error(RQ_ERROR_UNSUPPORTED, "traversal counters exist for BVH2 structures");
+  Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+             a.root.as<const float>(), a.n_nodes, a.n_slots};
+  launch_trace_bvh2_counted(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, counters, st);
+  RQ_B(cudaGetLastError(), "counted trace launch");
+  return {};
+}
+
+}  // namespace rq

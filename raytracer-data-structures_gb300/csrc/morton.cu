@@ -1,0 +1,182 @@
+// Morton codes over primitive centroids (accelerators.h:374-394, 575-580),
+// fused with the radix sort's digit histogram so the codes are read once.
+#include "rq_device.cuh"
+#include "rq_internal.hpp"
+
+namespace rq {
+namespace {
+
+constexpr int kThreads = 256;
+
+__global__ void k_init_bounds(int32_t* lohi) {
+  int t = threadIdx.x;
+  if (t < 3) lohi[t] = ordered_pos_inf();
+  else if (t < 6) lohi[t] = ordered_neg_inf();
+}
+
+// Box of n points with `stride` floats between consecutive points.
+__global__ void __launch_bounds__(kThreads) k_point_bounds(const float* __restrict__ pts, uint32_t n,
+                                                           uint32_t stride, int32_t* lohi) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* p = pts + (size_t)i * stride;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float v = __ldg(p + k);
+      lo[k] = fminf(lo[k], v);
+      hi[k] = fmaxf(hi[k], v);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+      hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+    }
+  __shared__ float s[kThreads / 32][6];
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+    for (int k = 0; k < 3; ++k) { s[w][k] = lo[k]; s[w][3 + k] = hi[k]; }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    int k = threadIdx.x;
+    float v = s[0][k];
+    for (int q = 1; q < kThreads / 32; ++q) v = k < 3 ? fminf(v, s[q][k]) : fmaxf(v, s[q][k]);
+    if (k < 3) atomicMin(&lohi[k], float_to_ordered(v));
+    else atomicMax(&lohi[k], float_to_ordered(v));
+  }
+}
+
+__device__ __forceinline__ void bounds_from(const int32_t* lohi, float* lo, float* ext) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = ordered_to_float(lohi[k]);
+    float hi = ordered_to_float(lohi[3 + k]);
+    ext[k] = __fsub_rn(hi, lo[k]);
+  }
+}
+
+// (c - lo) / ext per axis, 0 where the extent is 0.
+__device__ __forceinline__ uint32_t code_scene(F3 c, const float* lo, const float* ext) {
+  float q0 = ext[0] > 0.f ? __fdiv_rn(__fsub_rn(c.x, lo[0]), ext[0]) : 0.f;
+  float q1 = ext[1] > 0.f ? __fdiv_rn(__fsub_rn(c.y, lo[1]), ext[1]) : 0.f;
+  float q2 = ext[2] > 0.f ? __fdiv_rn(__fsub_rn(c.z, lo[2]), ext[2]) : 0.f;
+  return morton3d(q0, q1, q2);
+}
+
+struct SharedHist {
+  uint32_t h[4][256];
+};
+
+__device__ __forceinline__ void hist_zero(SharedHist& sh) {
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) (&sh.h[0][0])[i] = 0;
+}
+__device__ __forceinline__ void hist_add(SharedHist& sh, uint32_t code) {
+#pragma unroll
+  for (int p = 0; p < 4; ++p) atomicAdd(&sh.h[p][(code >> (8 * p)) & 255u], 1u);
+}
+__device__ __forceinline__ void hist_flush(SharedHist& sh, uint32_t* hist) {
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+    uint32_t v = (&sh.h[0][0])[i];
+    if (v) atomicAdd(&hist[i], v);
+  }
+}
+
+// Centroid ((v0 + v1) + v2) / 3 per axis, then scene-box normalisation.
+__global__ void __launch_bounds__(kThreads) k_morton_tris(const float* __restrict__ verts,
+                                                          const uint32_t* __restrict__ idx,
+                                                          uint32_t nt, const int32_t* __restrict__ lohi,
+                                                          uint32_t* __restrict__ keys,
+                                                          uint32_t* __restrict__ vals,
+                                                          uint32_t* __restrict__ hist) {
+  __shared__ SharedHist sh;
+  __shared__ float s_lo[3], s_ext[3];
+  if (hist) hist_zero(sh);
+  if (threadIdx.x == 0) bounds_from(lohi, s_lo, s_ext);
+  __syncthreads();
+  float lo[3] = {s_lo[0], s_lo[1], s_lo[2]}, ext[3] = {s_ext[0], s_ext[1], s_ext[2]};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+    uint32_t i0 = __ldg(idx + 3 * (size_t)i), i1 = __ldg(idx + 3 * (size_t)i + 1),
+             i2 = __ldg(idx + 3 * (size_t)i + 2);
+    const float* a = verts + 3 * (size_t)i0;
+    const float* b = verts + 3 * (size_t)i1;
+    const float* c = verts + 3 * (size_t)i2;
+    F3 cen;
+    cen.x = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a), __ldg(b)), __ldg(c)), 3.0f);
+    cen.y = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a + 1), __ldg(b + 1)), __ldg(c + 1)), 3.0f);
+    cen.z = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a + 2), __ldg(b + 2)), __ldg(c + 2)), 3.0f);
+    uint32_t code = code_scene(cen, lo, ext);
+    keys[i] = code;
+    vals[i] = i;
+    if (hist) hist_add(sh, code);
+  }
+  if (hist) {
+    __syncthreads();
+    hist_flush(sh, hist);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_morton_spheres(const float4* __restrict__ sph, uint32_t n,
+                                                             int mode, const int32_t* __restrict__ lohi,
+                                                             uint32_t* __restrict__ keys,
+                                                             uint32_t* __restrict__ vals,
+                                                             uint32_t* __restrict__ hist) {
+  __shared__ SharedHist sh;
+  __shared__ float s_lo[3], s_ext[3];
+  if (hist) hist_zero(sh);
+  if (threadIdx.x == 0 && mode == RQ_MORTON_SCENE_BOUNDS) bounds_from(lohi, s_lo, s_ext);
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 s = __ldg(sph + i);
+    uint32_t code;
+    if (mode == RQ_MORTON_REFERENCE) {
+      // (center + 30) / 1000, accelerators.h:577
+      code = morton3d(__fdiv_rn(__fadd_rn(s.x, 30.f), 1000.f), __fdiv_rn(__fadd_rn(s.y, 30.f), 1000.f),
+                      __fdiv_rn(__fadd_rn(s.z, 30.f), 1000.f));
+    } else {
+      code = code_scene({s.x, s.y, s.z}, s_lo, s_ext);
+    }
+    keys[i] = code;
+    vals[i] = i;
+    if (hist) hist_add(sh, code);
+  }
+  if (hist) {
+    __syncthreads();
+    hist_flush(sh, hist);
+  }
+}
+
+int grid_for(uint32_t n) {
+  uint32_t g = (n + kThreads - 1) / kThreads;
+  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+}  // namespace
+
+void launch_init_bounds(int32_t* lohi, cudaStream_t s) {
+  count_launch();
+  k_init_bounds<<<1, 32, 0, s>>>(lohi);
+}
+
+void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t* lohi,
+                         cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  k_point_bounds<<<grid_for(n) > 1024 ? 1024 : grid_for(n), kThreads, 0, s>>>(pts, n, stride, lohi);
+}
+
+void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, const int32_t* lohi,
+                        uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s) {
+  if (nt == 0) return;
+  count_launch();
+  k_morton_tris<<<grid_for(nt), kThreads, 0, s>>>(verts, idx, nt, lohi, keys, vals, hist);
+}
+
+void launch_morton_spheres(const float4* sph, uint32_t n, int mode, const int32_t* lohi,
+                           uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  k_morton_spheres<<<grid_for(n), kThreads, 0, s>>>(sph, n, mode, lohi, keys, vals, hist);
+}
+
+}  // namespace rq

@@ -1,0 +1,166 @@
+// The render step around the ray queries: render()'s camera rays
+// (main.cpp:541-566) and castRay's shading (main.cpp:390-497), reproducing
+// the reference's arithmetic (mixed double/float, explicit rounding, no
+// fused multiply-adds) so that its pixels come out the same.
+#include <vector>
+
+#include "rq_build.hpp"
+#include "rq_device.cuh"
+
+namespace rq {
+namespace {
+
+constexpr int kThreads = 128;
+
+// geometry.h normalize(): factor = float(1.0 / sqrt(double(x*x + y*y + z*z))).
+__device__ __forceinline__ F3 normalize_ref(F3 v) {
+  float n = __fadd_rn(__fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)), __fmul_rn(v.z, v.z));
+  if (n > 0.f) {
+    float f = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn((double)n)));
+    v.x = __fmul_rn(v.x, f);
+    v.y = __fmul_rn(v.y, f);
+    v.z = __fmul_rn(v.z, f);
+  }
+  return v;
+}
+
+// xx = (2 * ((x + jx) * invWidth) - 1) * angle * aspectratio, in double,
+// stored to float; yy = (1 - 2 * ((y + jy) * invHeight)) * angle.
+__global__ void __launch_bounds__(kThreads) k_camera_rays(uint32_t width, uint32_t height, uint32_t aa,
+                                                          float invWidth, float invHeight, float angle,
+                                                          float aspect, const double2* __restrict__ jitter,
+                                                          float4* __restrict__ rays, uint64_t nray) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nray) return;
+  uint64_t pix = k / aa;
+  uint32_t x = (uint32_t)(pix % width), y = (uint32_t)(pix / width);
+  double2 j = jitter[k];
+  double tx = __dmul_rn(__dsub_rn(__dmul_rn(2.0, __dmul_rn(__dadd_rn((double)x, j.x), (double)invWidth)), 1.0),
+                        (double)angle);
+  float xx = __double2float_rn(__dmul_rn(tx, (double)aspect));
+  double ty = __dmul_rn(__dsub_rn(1.0, __dmul_rn(2.0, __dmul_rn(__dadd_rn((double)y, j.y), (double)invHeight))),
+                        (double)angle);
+  float yy = __double2float_rn(ty);
+  F3 d = normalize_ref({xx, yy, -1.f});
+  rays[2 * k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  rays[2 * k + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7F800000));
+}
+
+// castRay's DIFFUSE_AND_GLOSSY branch with one light at (0, 3, 30), emission
+// (1, 1, 1); trace_more is a stub returning false, so nothing is shadowed.
+__device__ __forceinline__ F3 shade_one(const float4* __restrict__ sph, const float* __restrict__ surf,
+                                        const float4& r0, const float4& r1, const float4& h) {
+  uint32_t prim = __float_as_uint(h.y);
+  float4 s = __ldg(sph + prim);
+  F3 o = {r0.x, r0.y, r0.z}, d = {r1.x, r1.y, r1.z};
+  float tn = h.x;
+  F3 hp = {__fadd_rn(o.x, __fmul_rn(d.x, tn)), __fadd_rn(o.y, __fmul_rn(d.y, tn)),
+           __fadd_rn(o.z, __fmul_rn(d.z, tn))};
+  F3 N = normalize_ref(sub_rn(hp, {s.x, s.y, s.z}));
+  if (dot_rn(d, N) > 0.f) N = {-N.x, -N.y, -N.z};
+  F3 L = normalize_ref(sub_rn({0.f, 3.f, 30.f}, hp));
+  float ldn = dot_rn(L, N);
+  float LdotN = 0.f < ldn ? ldn : 0.f;
+  float amt = __fadd_rn(0.f, __fmul_rn(1.0f, LdotN));
+  F3 I = {-L.x, -L.y, -L.z};
+  float k2 = __fmul_rn(2.f, dot_rn(I, N));
+  F3 R = {__fsub_rn(I.x, __fmul_rn(N.x, k2)), __fsub_rn(I.y, __fmul_rn(N.y, k2)),
+          __fsub_rn(I.z, __fmul_rn(N.z, k2))};
+  float rd = -dot_rn(R, d);
+  float sp = powf(0.f < rd ? rd : 0.f, 25.f);
+  float spec = __fadd_rn(0.f, __fmul_rn(1.0f, sp));
+  const float dd[3] = {__fmul_rn(0.815f, 0.8f), __fmul_rn(0.235f, 0.8f), __fmul_rn(0.031f, 0.8f)};
+  const float* sc = surf + 3 * (size_t)prim;
+  F3 c;
+  c.x = __fadd_rn(__fadd_rn(0.f, __fadd_rn(__fdiv_rn(__fmul_rn(amt, dd[0]), 2.f), __fmul_rn(spec, 0.5f))), __ldg(sc));
+  c.y = __fadd_rn(__fadd_rn(0.f, __fadd_rn(__fdiv_rn(__fmul_rn(amt, dd[1]), 2.f), __fmul_rn(spec, 0.5f))), __ldg(sc + 1));
+  c.z = __fadd_rn(__fadd_rn(0.f, __fadd_rn(__fdiv_rn(__fmul_rn(amt, dd[2]), 2.f), __fmul_rn(spec, 0.5f))), __ldg(sc + 2));
+  return c;
+}
+
+__global__ void __launch_bounds__(kThreads) k_shade(const float4* __restrict__ sph, const float* __restrict__ surf,
+                                                    const float4* __restrict__ rays,
+                                                    const float4* __restrict__ hits,
+                                                    const uint32_t* __restrict__ kd_bits, uint32_t npix,
+                                                    uint32_t aa, float* __restrict__ rgb_sum,
+                                                    uint8_t* __restrict__ pixels) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  const F3 bg = {0.6f, 0.8f, 1.0f};
+  F3 sum = {0.f, 0.f, 0.f};
+  for (uint32_t s = 0; s < aa; ++s) {
+    uint64_t r = (uint64_t)p * aa + s;
+    F3 c;
+    if (kd_bits) {
+      bool hit = (__ldg(kd_bits + (r >> 5)) >> (r & 31)) & 1u;
+      c = hit ? F3{0.f, 0.f, 0.f} : bg;
+    } else {
+      float4 h = __ldg(hits + r);
+      c = __float_as_uint(h.y) == kMiss ? bg
+                                         : shade_one(sph, surf, __ldg(rays + 2 * r), __ldg(rays + 2 * r + 1), h);
+    }
+    sum = {__fadd_rn(sum.x, c.x), __fadd_rn(sum.y, c.y), __fadd_rn(sum.z, c.z)};
+  }
+  if (rgb_sum) {
+    rgb_sum[3 * (size_t)p] = sum.x;
+    rgb_sum[3 * (size_t)p + 1] = sum.y;
+    rgb_sum[3 * (size_t)p + 2] = sum.z;
+  }
+  // write_into_file: (unsigned char)(min(1, c / aa) * 255)
+  float faa = (float)aa;
+  float v[3] = {__fdiv_rn(sum.x, faa), __fdiv_rn(sum.y, faa), __fdiv_rn(sum.z, faa)};
+  for (int k = 0; k < 3; ++k) {
+    float m = v[k] < 1.f ? v[k] : 1.f;
+    pixels[3 * (size_t)p + k] = (uint8_t)__float2uint_rz(__fmul_rn(m, 255.f));
+  }
+}
+
+}  // namespace
+
+cudaError_t render_reference(int type, const SceneView& s, const AccelBuffers& a,
+                             const rq_settings_t& cfg, float angle, float aspect,
+                             const double* jitter_host, const float* surface_rgb_host,
+                             DevBuf& stage_a, DevBuf& stage_b, DevBuf& stage_c,
+                             uint8_t* pixels_host, float* rgb_sum_host, uint32_t* err,
+                             cudaStream_t st) {
+  const uint64_t npix = (uint64_t)cfg.width * cfg.height;
+  const uint64_t nray = npix * cfg.aa_samples;
+  const size_t jit_bytes = nray * 16, ray_bytes = nray * 32;
+  const size_t res_bytes = type == RQ_KDTREE ? ((nray + 31) / 32) * 4 : nray * 16;
+  const size_t surf_bytes = (size_t)s.n * 12;
+  const size_t out_bytes = npix * 3 + npix * 12 + 256;
+  cudaError_t e;
+  if ((e = stage_a.ensure(ray_bytes)) != cudaSuccess) return e;
+  if ((e = stage_b.ensure(res_bytes > jit_bytes ? res_bytes : jit_bytes)) != cudaSuccess) return e;
+  if ((e = stage_c.ensure(surf_bytes + out_bytes)) != cudaSuccess) return e;
+  float4* rays = stage_a.as<float4>();
+  char* cbase = stage_c.as<char>();
+  float* surf = reinterpret_cast<float*>(cbase);
+  uint8_t* pix = reinterpret_cast<uint8_t*>(cbase + surf_bytes);
+  float* sums = reinterpret_cast<float*>(cbase + ((surf_bytes + npix * 3 + 15) & ~size_t(15)));
+  // jitter shares stage_b with the query results: rays are generated first
+  if ((e = cudaMemcpyAsync(stage_b.p, jitter_host, jit_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(surf, surface_rgb_host, surf_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  float invW = 1 / float(cfg.width), invH = 1 / float(cfg.height);
+  count_launch(2);  // camera rays + shading
+  k_camera_rays<<<(unsigned)((nray + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+      cfg.width, cfg.height, cfg.aa_samples, invW, invH, angle, aspect, stage_b.as<const double2>(), rays, nray);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  QueryTarget q;
+  q.rays = rays;
+  q.n = (uint32_t)nray;
+  if (type == RQ_KDTREE) q.occ = stage_b.as<uint32_t>();
+  else q.hits = stage_b.as<float4>();
+  launch_query(type, s, a, RQ_TRAVERSAL_REFERENCE, type == RQ_KDTREE, q, err, st);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  k_shade<<<(unsigned)((npix + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+      s.sph, surf, rays, q.hits, q.occ, (uint32_t)npix, cfg.aa_samples, sums, pix);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(pixels_host, pix, npix * 3, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if (rgb_sum_host &&
+      (e = cudaMemcpyAsync(rgb_sum_host, sums, npix * 12, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  return cudaStreamSynchronize(st);
+}
+
+}  // namespace rq

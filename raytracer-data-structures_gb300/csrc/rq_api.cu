@@ -1,0 +1,632 @@
+// The C ABI (include/rq.h): contexts, scenes, the dataStructure build switch
+// and the ray queries, over the kernels of the other translation units.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "rq_device.cuh"
+#include "rq_internal.hpp"
+#include "rq_build.hpp"
+
+using namespace rq;
+
+struct rq_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  rq_settings_t settings{};
+  std::string last_error;
+  uint32_t* d_err = nullptr;
+  int sm_count = 0;
+  DevBuf stage_in, stage_out, stage_aux;
+  BuildScratch scratch;
+};
+
+struct rq_scene {
+  rq_ctx_t ctx = nullptr;
+  int kind = kTriangles;
+  uint32_t n = 0;   // primitives
+  uint32_t nv = 0;  // vertices (triangles)
+  DevBuf verts, idx, sph;
+};
+
+struct rq_accel {
+  rq_ctx_t ctx = nullptr;
+  rq_scene_t scene = nullptr;
+  int type = RQ_NONE;
+  AccelBuffers buf;
+};
+
+namespace {
+
+rq_status_t fail(rq_ctx_t ctx, rq_status_t st, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return st;
+}
+
+rq_status_t cuda_fail(rq_ctx_t ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();  // clear a sticky launch error where possible
+  return fail(ctx, e == cudaErrorMemoryAllocation ? RQ_ERROR_OUT_OF_MEMORY : RQ_ERROR_CUDA, m);
+}
+
+#define RQ_TRY_CUDA(ctx, call)                                   \
+  do {                                                           \
+    cudaError_t e_ = (call);                                     \
+    if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);   \
+  } while (0)
+
+#define RQ_TRY(call)                  \
+  do {                                \
+    rq_status_t s_ = (call);          \
+    if (s_ != RQ_SUCCESS) return s_;  \
+  } while (0)
+
+rq_status_t bind(rq_ctx_t ctx) {
+  if (!ctx) return RQ_ERROR_INVALID_ARGUMENT;
+  RQ_TRY_CUDA(ctx, cudaSetDevice(ctx->device));
+  return RQ_SUCCESS;
+}
+
+// Read and clear the device error word; map it to a status.
+rq_status_t collect_device_errors(rq_ctx_t ctx) {
+  uint32_t e = 0;
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(&e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (e) {
+    RQ_TRY_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream));
+    if (e & kErrStackOverflow)
+      return fail(ctx, RQ_ERROR_STACK_OVERFLOW, "traversal stack overflow (tree deeper than 64)");
+    if (e & kErrTimeout) return fail(ctx, RQ_ERROR_TIMEOUT, "a bounded device-side wait gave up");
+    if (e & kErrBadInput) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "invalid scene data (NaN/Inf or index out of range)");
+    if (e & kErrCorrupt) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed acceleration structure (walk bound exceeded)");
+  }
+  return RQ_SUCCESS;
+}
+
+rq_status_t check_launch(rq_ctx_t ctx, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+  return RQ_SUCCESS;
+}
+
+// Copy a caller buffer to the device (or pass a device pointer through).
+template <typename T>
+rq_status_t to_device(rq_ctx_t ctx, DevBuf& stage, const T* src, size_t bytes, uint32_t flags,
+                      const T** out) {
+  if (flags & RQ_DEVICE_POINTERS) {
+    *out = src;
+    return RQ_SUCCESS;
+  }
+  RQ_TRY_CUDA(ctx, stage.ensure(bytes));
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(stage.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  *out = stage.as<const T>();
+  return RQ_SUCCESS;
+}
+
+bool finite3(const float* p, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rq_settings_default(rq_settings_t* s) {
+  if (!s) return;
+  std::memset(s, 0, sizeof(*s));
+  s->width = 640;
+  s->height = 480;
+  s->fov = 90;
+  s->backgroundColor[0] = s->backgroundColor[1] = s->backgroundColor[2] = 1.f;
+  s->bias = 0.0001f;
+  s->aa_samples = 1;
+  s->dataStructure = RQ_BVH;
+  s->sceneModel = RQ_BUNNY;
+  s->traversal = RQ_TRAVERSAL_FAST;
+  s->morton = RQ_MORTON_SCENE_BOUNDS;
+  s->kd_max_depth = -1;
+}
+
+const char* rq_status_string(rq_status_t st) {
+  switch (st) {
+    case RQ_SUCCESS: return "success";
+    case RQ_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case RQ_ERROR_UNSUPPORTED: return "unsupported";
+    case RQ_ERROR_OUT_OF_MEMORY: return "out of device memory";
+    case RQ_ERROR_CUDA: return "CUDA error";
+    case RQ_ERROR_STACK_OVERFLOW: return "traversal stack overflow";
+    case RQ_ERROR_TIMEOUT: return "device wait timed out";
+    case RQ_ERROR_EMPTY_SCENE: return "empty scene";
+    case RQ_ERROR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+rq_status_t rq_create(const rq_settings_t* settings, int device, rq_ctx_t* out) {
+  if (!out) return RQ_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return RQ_ERROR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return RQ_ERROR_INVALID_ARGUMENT;
+  rq_context* ctx = new (std::nothrow) rq_context();
+  if (!ctx) return RQ_ERROR_OUT_OF_MEMORY;
+  ctx->device = device;
+  if (settings) ctx->settings = *settings;
+  else rq_settings_default(&ctx->settings);
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 4);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 4);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    rq_status_t st = e == cudaErrorMemoryAllocation ? RQ_ERROR_OUT_OF_MEMORY : RQ_ERROR_CUDA;
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    delete ctx;
+    cudaGetLastError();
+    return st;
+  }
+  ctx->stream = ctx->own_stream;
+  *out = ctx;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_destroy(rq_ctx_t ctx) {
+  if (!ctx) return RQ_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->stage_in.release();
+  ctx->stage_out.release();
+  ctx->stage_aux.release();
+  ctx->scratch.release();
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_get_settings(rq_ctx_t ctx, rq_settings_t* out) {
+  if (!ctx || !out) return RQ_ERROR_INVALID_ARGUMENT;
+  *out = ctx->settings;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
+  if (!ctx || !s) return RQ_ERROR_INVALID_ARGUMENT;
+  if (s->traversal != RQ_TRAVERSAL_FAST && s->traversal != RQ_TRAVERSAL_REFERENCE)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.traversal must be FAST or REFERENCE");
+  if (s->morton != RQ_MORTON_SCENE_BOUNDS && s->morton != RQ_MORTON_REFERENCE)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.morton must be SCENE_BOUNDS or REFERENCE");
+  ctx->settings = *s;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_set_stream(rq_ctx_t ctx, void* stream) {
+  if (!ctx) return RQ_ERROR_INVALID_ARGUMENT;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_synchronize(rq_ctx_t ctx) {
+  RQ_TRY(bind(ctx));
+  return collect_device_errors(ctx);
+}
+
+const char* rq_last_error(rq_ctx_t ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+// ------------------------------------------------------------------ scenes
+
+rq_status_t rq_scene_create_triangles(rq_ctx_t ctx, const float* verts, uint32_t nv,
+                                      const uint32_t* idx, uint32_t nt, uint32_t flags,
+                                      rq_scene_t* out) {
+  if (!out) return RQ_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  RQ_TRY(bind(ctx));
+  if (nt == 0) return fail(ctx, RQ_ERROR_EMPTY_SCENE, "scene has no triangles");
+  if (!verts || !idx || nv == 0) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null vertex or index buffer");
+  if (nt >= (1u << 30)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "2^30 or more triangles");
+  if (!(flags & RQ_DEVICE_POINTERS)) {
+    if (!finite3(verts, (size_t)nv * 3)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "non-finite vertex");
+    for (size_t i = 0; i < (size_t)nt * 3; ++i)
+      if (idx[i] >= nv) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "triangle index out of range");
+  }
+  rq_scene* s = new (std::nothrow) rq_scene();
+  if (!s) return RQ_ERROR_OUT_OF_MEMORY;
+  s->ctx = ctx;
+  s->kind = kTriangles;
+  s->n = nt;
+  s->nv = nv;
+  cudaMemcpyKind k = (flags & RQ_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  cudaError_t e = s->verts.ensure((size_t)nv * 12);
+  if (e == cudaSuccess) e = s->idx.ensure((size_t)nt * 12);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(s->verts.p, verts, (size_t)nv * 12, k, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(s->idx.p, idx, (size_t)nt * 12, k, ctx->stream);
+  if (e == cudaSuccess && (flags & RQ_DEVICE_POINTERS)) {
+    launch_validate(s->verts.as<float>(), nv, s->idx.as<uint32_t>(), nt, nullptr, 0, ctx->d_err, ctx->stream);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    s->verts.release();
+    s->idx.release();
+    delete s;
+    return cuda_fail(ctx, e, "scene upload");
+  }
+  rq_status_t st = collect_device_errors(ctx);
+  if (st != RQ_SUCCESS) {
+    s->verts.release();
+    s->idx.release();
+    delete s;
+    return st;
+  }
+  *out = s;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_scene_create_spheres(rq_ctx_t ctx, const float* sph, uint32_t n, uint32_t flags,
+                                    rq_scene_t* out) {
+  if (!out) return RQ_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  RQ_TRY(bind(ctx));
+  if (n == 0) return fail(ctx, RQ_ERROR_EMPTY_SCENE, "scene has no spheres");
+  if (!sph) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null sphere buffer");
+  if (n >= (1u << 30)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "2^30 or more spheres");
+  if (!(flags & RQ_DEVICE_POINTERS)) {
+    if (!finite3(sph, (size_t)n * 4)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "non-finite sphere");
+    for (size_t i = 0; i < n; ++i)
+      if (sph[4 * i + 3] < 0.f) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "negative sphere radius");
+  }
+  rq_scene* s = new (std::nothrow) rq_scene();
+  if (!s) return RQ_ERROR_OUT_OF_MEMORY;
+  s->ctx = ctx;
+  s->kind = kSpheres;
+  s->n = n;
+  cudaMemcpyKind k = (flags & RQ_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  cudaError_t e = s->sph.ensure((size_t)n * 16);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(s->sph.p, sph, (size_t)n * 16, k, ctx->stream);
+  if (e == cudaSuccess && (flags & RQ_DEVICE_POINTERS)) {
+    launch_validate(nullptr, 0, nullptr, 0, s->sph.as<float4>(), n, ctx->d_err, ctx->stream);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    s->sph.release();
+    delete s;
+    return cuda_fail(ctx, e, "scene upload");
+  }
+  rq_status_t st = collect_device_errors(ctx);
+  if (st != RQ_SUCCESS) {
+    s->sph.release();
+    delete s;
+    return st;
+  }
+  *out = s;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_scene_update(rq_ctx_t ctx, rq_scene_t s, const float* data, const uint32_t* idx,
+                            uint32_t flags) {
+  if (!s || !data) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null scene or data");
+  RQ_TRY(bind(ctx));
+  const bool dev = flags & RQ_DEVICE_POINTERS;
+  size_t bytes = s->kind == kTriangles ? (size_t)s->nv * 12 : (size_t)s->n * 16;
+  if (!dev && !finite3(data, bytes / 4)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "non-finite coordinate");
+  if (idx && s->kind == kTriangles && !dev)
+    for (size_t i = 0; i < (size_t)s->n * 3; ++i)
+      if (idx[i] >= s->nv) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "triangle index out of range");
+  void* dst = s->kind == kTriangles ? s->verts.p : s->sph.p;
+  cudaMemcpyKind k = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dst, data, bytes, k, ctx->stream));
+  if (idx && s->kind == kTriangles)
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(s->idx.p, idx, (size_t)s->n * 12, k, ctx->stream));
+  if (dev) {
+    launch_validate(s->kind == kTriangles ? s->verts.as<float>() : nullptr, s->kind == kTriangles ? s->nv : 0,
+                    (idx && s->kind == kTriangles) ? s->idx.as<uint32_t>() : nullptr,
+                    (idx && s->kind == kTriangles) ? s->n : 0, s->kind == kSpheres ? s->sph.as<float4>() : nullptr,
+                    s->kind == kSpheres ? s->n : 0, ctx->d_err, ctx->stream);
+    RQ_TRY(check_launch(ctx, "validate launch"));
+    return RQ_SUCCESS;  // device-side validation result arrives with rq_synchronize
+  }
+  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_scene_destroy(rq_scene_t s) {
+  if (!s) return RQ_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
+  s->verts.release();
+  s->idx.release();
+  s->sph.release();
+  delete s;
+  return RQ_SUCCESS;
+}
+
+// ------------------------------------------------------------------ builds
+
+static SceneView scene_view(rq_scene_t s) {
+  SceneView v;
+  v.kind = s->kind;
+  v.n = s->n;
+  v.nv = s->nv;
+  v.verts = s->verts.as<const float>();
+  v.idx = s->idx.as<const uint32_t>();
+  v.sph = s->sph.as<const float4>();
+  return v;
+}
+
+static rq_status_t do_build(rq_ctx_t ctx, rq_accel_t a) {
+  SceneView sv = scene_view(a->scene);
+  BuildResult r = build_accel(a->type, sv, ctx->settings, a->buf, ctx->scratch, ctx->d_err, ctx->stream);
+  if (r.cuda != cudaSuccess) return cuda_fail(ctx, r.cuda, r.what ? r.what : "build");
+  if (r.status != RQ_SUCCESS) return fail(ctx, r.status, r.what ? r.what : "build failed");
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_build(rq_ctx_t ctx, rq_scene_t scene, int32_t acc_type, rq_accel_t* out) {
+  if (!out) return RQ_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  RQ_TRY(bind(ctx));
+  if (!scene) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null scene");
+  if (acc_type == RQ_UNIFORM_GRID)
+    return fail(ctx, RQ_ERROR_UNSUPPORTED, "UNIFORM_GRID is declared by the reference but never implemented");
+  if (acc_type != RQ_BVH && acc_type != RQ_KDTREE && acc_type != RQ_LBVH && acc_type != RQ_NONE)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "unknown dataStructure");
+  rq_accel* a = new (std::nothrow) rq_accel();
+  if (!a) return RQ_ERROR_OUT_OF_MEMORY;
+  a->ctx = ctx;
+  a->scene = scene;
+  a->type = acc_type;
+  rq_status_t st = do_build(ctx, a);
+  if (st == RQ_SUCCESS) st = collect_device_errors(ctx);
+  if (st != RQ_SUCCESS) {
+    a->buf.release();
+    delete a;
+    return st;
+  }
+  *out = a;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_accel_rebuild(rq_ctx_t ctx, rq_accel_t a) {
+  if (!a) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel");
+  RQ_TRY(bind(ctx));
+  return do_build(ctx, a);
+}
+
+rq_status_t rq_accel_destroy(rq_accel_t a) {
+  if (!a) return RQ_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(a->ctx->device);
+  cudaStreamSynchronize(a->ctx->stream);
+  a->buf.release();
+  delete a;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_accel_get_info(rq_accel_t a, rq_accel_info_t* info) {
+  if (!a || !info) return RQ_ERROR_INVALID_ARGUMENT;
+  rq_ctx_t ctx = a->ctx;
+  RQ_TRY(bind(ctx));
+  std::memset(info, 0, sizeof(*info));
+  info->type = a->type;
+  info->prim_kind = a->scene->kind;
+  info->n_prims = a->scene->n;
+  info->n_nodes = a->buf.n_nodes;
+  info->n_slots = a->buf.n_slots;
+  info->max_depth = a->buf.max_depth;
+  info->device_bytes = a->buf.device_bytes();
+  if (a->buf.root.p) {
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(info->root_bounds, a->buf.root.p, 24, cudaMemcpyDeviceToHost, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_accel_export_bvh2(rq_ctx_t ctx, rq_accel_t a, float* nodes, uint32_t* order,
+                                 uint32_t* sorted_codes) {
+  if (!a) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel");
+  RQ_TRY(bind(ctx));
+  if (a->type != RQ_BVH && a->type != RQ_LBVH)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "not a BVH2 structure");
+  if (nodes && a->buf.n_nodes)
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(nodes, a->buf.nodes.p, (size_t)a->buf.n_nodes * 64, cudaMemcpyDeviceToHost, ctx->stream));
+  if (order)
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(order, a->buf.order.p, (size_t)a->buf.n_slots * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (sorted_codes && a->type == RQ_LBVH)
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(sorted_codes, a->buf.codes.p, (size_t)a->scene->n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t a, int32_t* nodes, int32_t* prim_idx) {
+  if (!a) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel");
+  RQ_TRY(bind(ctx));
+  if (a->type != RQ_KDTREE) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "not a KD tree");
+  if (nodes && a->buf.n_nodes) {
+    std::vector<int4> tmp(a->buf.n_nodes);
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(tmp.data(), a->buf.kd_nodes.p, tmp.size() * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < tmp.size(); ++i) {
+      nodes[3 * i] = tmp[i].x;
+      nodes[3 * i + 1] = tmp[i].y;
+      nodes[3 * i + 2] = tmp[i].z;
+    }
+  }
+  if (prim_idx && a->buf.n_slots)
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(prim_idx, a->buf.kd_idx.p, (size_t)a->buf.n_slots * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RQ_SUCCESS;
+}
+
+// ----------------------------------------------------------------- queries
+
+static rq_status_t trace(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, void* out,
+                         uint32_t flags, bool any) {
+  RQ_TRY(bind(ctx));
+  if (!a) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel");
+  if (n == 0) return RQ_SUCCESS;
+  if (!rays || !out) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
+  const bool dev = flags & RQ_DEVICE_POINTERS;
+  const float4* d_rays = nullptr;
+  RQ_TRY(to_device(ctx, ctx->stage_in, reinterpret_cast<const float4*>(rays), (size_t)n * 32, flags, &d_rays));
+  const size_t out_bytes = any ? (size_t)((n + 31) / 32) * 4 : (size_t)n * 16;
+  void* d_out = out;
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, ctx->stage_out.ensure(out_bytes));
+    d_out = ctx->stage_out.p;
+  }
+  QueryTarget q;
+  q.rays = d_rays;
+  q.n = n;
+  q.hits = any ? nullptr : static_cast<float4*>(d_out);
+  q.occ = any ? static_cast<uint32_t*>(d_out) : nullptr;
+  launch_query(a->type, scene_view(a->scene), a->buf, ctx->settings.traversal, any, q, ctx->d_err, ctx->stream);
+  RQ_TRY(check_launch(ctx, "trace launch"));
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return collect_device_errors(ctx);
+  }
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_trace_closest(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n,
+                             rq_hit_t* hits, uint32_t flags) {
+  return trace(ctx, a, rays, n, hits, flags, false);
+}
+
+rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n,
+                         uint32_t* occluded_bits, uint32_t flags) {
+  return trace(ctx, a, rays, n, occluded_bits, flags, true);
+}
+
+rq_status_t rq_trace_counters(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, int32_t any,
+                              void* out, uint64_t* counters, uint32_t flags) {
+  RQ_TRY(bind(ctx));
+  if (!a || !counters) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel or counters");
+  counters[0] = counters[1] = 0;
+  if (n == 0) return RQ_SUCCESS;
+  if (!rays || !out) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
+  const bool dev = flags & RQ_DEVICE_POINTERS;
+  const float4* d_rays = nullptr;
+  RQ_TRY(to_device(ctx, ctx->stage_in, reinterpret_cast<const float4*>(rays), (size_t)n * 32, flags, &d_rays));
+  const size_t out_bytes = any ? (size_t)((n + 31) / 32) * 4 : (size_t)n * 16;
+  void* d_out = out;
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, ctx->stage_out.ensure(out_bytes));
+    d_out = ctx->stage_out.p;
+  }
+  RQ_TRY_CUDA(ctx, ctx->stage_aux.ensure(64));
+  unsigned long long* d_cnt = ctx->stage_aux.as<unsigned long long>();
+  RQ_TRY_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 16, ctx->stream));
+  QueryTarget q;
+  q.rays = d_rays;
+  q.n = n;
+  q.hits = any ? nullptr : static_cast<float4*>(d_out);
+  q.occ = any ? static_cast<uint32_t*>(d_out) : nullptr;
+  BuildResult r = trace_counted(a->type, scene_view(a->scene), a->buf, any != 0, q, d_cnt, ctx->d_err, ctx->stream);
+  if (r.cuda != cudaSuccess) return cuda_fail(ctx, r.cuda, r.what);
+  if (r.status != RQ_SUCCESS) return fail(ctx, r.status, r.what);
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(counters, d_cnt, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dev) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return collect_device_errors(ctx);
+}
+
+uint64_t rq_kernel_launch_count(void) { return launch_total(); }
+
+// -------------------------------------------------------- component kernels
+
+rq_status_t rq_morton_codes(rq_ctx_t ctx, rq_scene_t s, uint32_t* codes, uint32_t flags) {
+  RQ_TRY(bind(ctx));
+  if (!s || !codes) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null scene or output");
+  uint32_t* d_codes = codes;
+  if (!(flags & RQ_DEVICE_POINTERS)) {
+    RQ_TRY_CUDA(ctx, ctx->stage_out.ensure((size_t)s->n * 4));
+    d_codes = ctx->stage_out.as<uint32_t>();
+  }
+  RQ_TRY_CUDA(ctx, ctx->stage_aux.ensure((size_t)s->n * 4 + 64));
+  uint32_t* d_vals = ctx->stage_aux.as<uint32_t>();
+  BuildResult r = morton_codes(scene_view(s), ctx->settings.morton, d_codes, d_vals, nullptr, ctx->scratch, ctx->stream);
+  if (r.cuda != cudaSuccess) return cuda_fail(ctx, r.cuda, r.what);
+  RQ_TRY(check_launch(ctx, "morton launch"));
+  if (!(flags & RQ_DEVICE_POINTERS)) {
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(codes, d_codes, (size_t)s->n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_sort_pairs(rq_ctx_t ctx, uint32_t* keys, uint32_t* values, uint32_t n,
+                          uint32_t key_bits, uint32_t flags) {
+  RQ_TRY(bind(ctx));
+  if (n == 0) return RQ_SUCCESS;
+  if (!keys || !values) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null keys or values");
+  if (key_bits == 0 || key_bits > 32) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "key_bits must be 1..32");
+  if (n > (1u << 30) - 1) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "more than 2^30-1 pairs");
+  const bool dev = flags & RQ_DEVICE_POINTERS;
+  uint32_t* dk = keys;
+  uint32_t* dv = values;
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, ctx->stage_in.ensure((size_t)n * 4));
+    RQ_TRY_CUDA(ctx, ctx->stage_out.ensure((size_t)n * 4));
+    dk = ctx->stage_in.as<uint32_t>();
+    dv = ctx->stage_out.as<uint32_t>();
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dk, keys, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dv, values, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  BuildResult r = sort_pairs(dk, dv, n, (int)((key_bits + 7) / 8), true, ctx->scratch, ctx->d_err, ctx->stream);
+  if (r.cuda != cudaSuccess) return cuda_fail(ctx, r.cuda, r.what);
+  RQ_TRY(check_launch(ctx, "sort launch"));
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(keys, dk, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(values, dv, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    return collect_device_errors(ctx);
+  }
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_render_reference(rq_ctx_t ctx, rq_accel_t a, const rq_settings_t* settings,
+                                const double* jitter, const float* surface_rgb, uint8_t* pixels,
+                                float* rgb_sum) {
+  RQ_TRY(bind(ctx));
+  if (!a || !pixels || !surface_rgb) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel, colours or pixels");
+  if (a->scene->kind != kSpheres) return fail(ctx, RQ_ERROR_UNSUPPORTED, "the reference render shades spheres");
+  rq_settings_t s = settings ? *settings : ctx->settings;
+  if (s.width == 0 || s.height == 0 || s.aa_samples == 0) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "empty image");
+  const uint64_t npix = (uint64_t)s.width * s.height;
+  const uint64_t nray = npix * s.aa_samples;
+  if (nray > (1ull << 31)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "image too large");
+  // Jitter: the caller's, or the reference's default-seeded mt19937 draws
+  // (random_double, main.cpp:503-508) in render()'s call order.
+  std::vector<double> own;
+  if (!jitter) {
+    own.resize(2 * nray);
+    std::mt19937 gen;
+    std::uniform_real_distribution<double> dist(0.0, 1.0);
+    for (auto& v : own) v = dist(gen);
+    jitter = own.data();
+  }
+  // render() camera constants (main.cpp:544-546), computed on the host with
+  // the same double-precision tan the reference calls.
+  float fov = 30, aspect = s.width / float(s.height);
+  float angle = (float)std::tan(3.141592653589793 * 0.5 * fov / 180.);
+  RenderBuffers rb;
+  cudaError_t e = render_reference(a->type, scene_view(a->scene), a->buf, s, angle, aspect, jitter,
+                                   surface_rgb, ctx->stage_in, ctx->stage_out, ctx->stage_aux,
+                                   pixels, rgb_sum, ctx->d_err, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
+  return collect_device_errors(ctx);
+}
+
+}  // extern "C"

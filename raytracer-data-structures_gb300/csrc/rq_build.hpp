@@ -1,0 +1,114 @@
+// Build orchestration shared by the C ABI: device buffers of a structure,
+// reusable build scratch, and the per-type build / query entry points.
+#pragma once
+#include "rq_internal.hpp"
+
+namespace rq {
+
+struct SceneView {
+  int kind = kTriangles;
+  uint32_t n = 0;   // primitives
+  uint32_t nv = 0;  // vertices
+  const float* verts = nullptr;
+  const uint32_t* idx = nullptr;
+  const float4* sph = nullptr;
+};
+
+// Device memory held by one acceleration structure.
+struct AccelBuffers {
+  DevBuf nodes;        // BVH2 nodes, 64 B each
+  DevBuf prims;        // BVH2: payload in slot order; KD / NONE: payload in id order
+  DevBuf order;        // BVH2: slot -> primitive id
+  DevBuf codes;        // LBVH: sorted Morton codes
+  DevBuf root;         // 8 floats: root box (min xyz, max xyz)
+  DevBuf kd_nodes;     // KD: int4 per node
+  DevBuf kd_idx;       // KD: primitive indices
+  uint32_t n_nodes = 0;
+  uint32_t n_slots = 0;
+  uint32_t max_depth = 0;
+  void release() {
+    nodes.release(); prims.release(); order.release(); codes.release(); root.release();
+    kd_nodes.release(); kd_idx.release();
+    n_nodes = n_slots = max_depth = 0;
+  }
+  size_t device_bytes() const {
+    return nodes.cap + prims.cap + order.cap + codes.cap + root.cap + kd_nodes.cap + kd_idx.cap;
+  }
+};
+
+// Scratch reused across builds of one context (grow-only).
+struct BuildScratch {
+  DevBuf keys_alt, vals_alt;  // radix sort ping-pong
+  DevBuf zero;                // [hist 1024][counters 16][look-back status][refit flags]: zeroed per build
+  DevBuf parent;              // Karras parent links
+  DevBuf lohi;                // ordered-int scene box
+  DevBuf keys, vals;          // generic sort input
+  DevBuf m0, m1, m2, m3, m4, m5, m6, m7;  // median / KD working arrays
+  DevBuf host_pinned_dummy;
+  void release() {
+    keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); lohi.release();
+    keys.release(); vals.release();
+    m0.release(); m1.release(); m2.release(); m3.release(); m4.release(); m5.release(); m6.release(); m7.release();
+  }
+};
+
+struct BuildResult {
+  rq_status_t status = RQ_SUCCESS;
+  cudaError_t cuda = cudaSuccess;
+  const char* what = nullptr;
+  static BuildResult cuda_error(cudaError_t e, const char* w) {
+    BuildResult r;
+    r.cuda = e;
+    r.what = w;
+    return r;
+  }
+  static BuildResult error(rq_status_t s, const char* w) {
+    BuildResult r;
+    r.status = s;
+    r.what = w;
+    return r;
+  }
+  bool ok() const { return status == RQ_SUCCESS && cuda == cudaSuccess; }
+};
+
+BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& settings, AccelBuffers& a,
+                        BuildScratch& sc, uint32_t* err, cudaStream_t st);
+// Morton codes in primitive order (vals = identity); hist optional.
+BuildResult morton_codes(const SceneView& s, int mode, uint32_t* codes, uint32_t* vals,
+                         uint32_t* hist, BuildScratch& sc, cudaStream_t st);
+// In-place stable sort; compute_hist = false when sc.zero's histogram was
+// already filled (fused Morton kernel) and zeroed state is in place.
+BuildResult sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, bool compute_hist,
+                       BuildScratch& sc, uint32_t* err, cudaStream_t st);
+
+// Builders living in their own translation units.
+BuildResult build_median_bvh(const SceneView& s, AccelBuffers& a, BuildScratch& sc, uint32_t* err,
+                             cudaStream_t st);
+BuildResult build_kd_tree(const SceneView& s, int max_depth, AccelBuffers& a, BuildScratch& sc,
+                          uint32_t* err, cudaStream_t st);
+
+struct QueryTarget {
+  const float4* rays = nullptr;
+  uint32_t n = 0;
+  float4* hits = nullptr;
+  uint32_t* occ = nullptr;
+};
+void launch_query(int type, const SceneView& s, const AccelBuffers& a, int traversal, bool any,
+                  const QueryTarget& q, uint32_t* err, cudaStream_t st);
+
+uint64_t launch_total();
+BuildResult trace_counted(int type, const SceneView& s, const AccelBuffers& a, bool any, const QueryTarget& q,
+                          unsigned long long* counters, uint32_t* err, cudaStream_t st);
+
+void launch_validate(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                     const float4* sph, uint32_t n, uint32_t* err, cudaStream_t st);
+
+struct RenderBuffers {};
+cudaError_t render_reference(int type, const SceneView& s, const AccelBuffers& a,
+                             const rq_settings_t& settings, float angle, float aspect,
+                             const double* jitter_host, const float* surface_rgb_host,
+                             DevBuf& stage_a, DevBuf& stage_b, DevBuf& stage_c,
+                             uint8_t* pixels_host, float* rgb_sum_host, uint32_t* err,
+                             cudaStream_t st);
+
+}  // namespace rq

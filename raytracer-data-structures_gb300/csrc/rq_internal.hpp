@@ -1,0 +1,121 @@
+// Host-side internals shared by the engine's translation units: handle
+// structures, device buffers and the kernel launchers each .cu file exports.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "rq.h"
+
+namespace rq {
+
+// Grow-only device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+enum PrimKind { kTriangles = 0, kSpheres = 1 };
+
+// Process-wide count of kernel launches made by the engine (rq_kernel_launch_count).
+void count_launch(uint64_t k = 1);
+
+// ----------------------------------------------------------- radix sort
+struct SortScratch {
+  uint32_t* keys_alt;
+  uint32_t* vals_alt;
+  uint32_t* hist;      // 4 * 256 digit counts
+  uint32_t* status;    // passes * tiles * 256 look-back words
+  uint32_t* counters;  // one tile counter per pass
+};
+uint32_t sort_tiles(uint32_t n);
+size_t sort_status_words(uint32_t n, int passes);
+// hist must hold the digit histogram of `keys` for every pass (as produced by
+// launch_histogram or the fused Morton kernels).  status/counters must be
+// zero.  Result lands in keys/vals.
+void launch_histogram(const uint32_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
+void launch_onesweep(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
+                     uint32_t* err, cudaStream_t s);
+
+// --------------------------------------------------------- Morton codes
+void launch_init_bounds(int32_t* lohi, cudaStream_t s);
+void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t* lohi,
+                         cudaStream_t s);
+// mode: RQ_MORTON_SCENE_BOUNDS (uses lohi) or RQ_MORTON_REFERENCE.  hist may
+// be null; otherwise the 4-pass digit histogram is accumulated into it.
+void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, const int32_t* lohi,
+                        uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s);
+void launch_morton_spheres(const float4* sph, uint32_t n, int mode, const int32_t* lohi,
+                           uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s);
+
+// ---------------------------------------------------------------- LBVH
+void launch_karras(const uint32_t* sorted_codes, uint32_t n, float4* nodes, uint32_t* parent,
+                   cudaStream_t s);
+// Gathers each slot's primitive into the slot-ordered payload, writes leaf
+// boxes into the parents and climbs to the root; root_out gets 6 floats.
+void launch_refit(int kind, const float* verts, const uint32_t* idx, const float4* sph,
+                  const uint32_t* order, uint32_t n, float4* nodes, const uint32_t* parent,
+                  uint32_t* flags, float4* prims, float* root_out, uint32_t* err, cudaStream_t s);
+// Payload in primitive-id order (KD and brute force) plus per-primitive boxes.
+void launch_prims_by_id(int kind, const float* verts, const uint32_t* idx, const float4* sph,
+                        uint32_t n, float4* prims, float* aabb6, cudaStream_t s);
+
+// ------------------------------------------------------------ traversal
+struct Bvh2View {
+  const float4* nodes;
+  const float4* prims;    // slot order: 3 float4 per triangle, 1 per sphere
+  const uint32_t* order;  // slot -> primitive id
+  const float* root;      // 6 floats
+  uint32_t n_internal;
+  uint32_t n_slots;
+};
+void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
+                       uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s);
+// FAST traversal that also sums internal-node visits and primitive tests
+// into counters[0..1] (the inputs of the traversal byte model).
+void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n,
+                               float4* hits, uint32_t* occ, uint32_t* err, unsigned long long* counters,
+                               cudaStream_t s);
+void launch_trace_brute(int kind, int traversal, bool any, const float4* prims, uint32_t n_prims,
+                        const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
+                        cudaStream_t s);
+
+struct KdView {
+  const int4* nodes;      // {word0, word1, word2, 0}
+  const int32_t* prim_idx;
+  const float4* prims;    // primitive-id order
+  const float* root;      // 6 floats
+};
+void launch_trace_kd(int kind, int traversal, bool any, const KdView& v, const float4* rays,
+                     uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s);
+
+// --------------------------------------------------------- median BVH
+struct MedianScratch;
+// --------------------------------------------------------------- render
+void launch_camera_rays_ref(uint32_t width, uint32_t height, uint32_t aa, float angle,
+                            float aspect, const double* jitter, float4* rays, cudaStream_t s);
+void launch_shade_ref(const float4* sph, const float* surface_rgb, const float4* rays,
+                      const float4* hits, const uint32_t* kd_bits, uint32_t n, uint32_t aa,
+                      float* rgb_sum, uint8_t* pixels, uint32_t npix, cudaStream_t s);
+
+}  // namespace rq

@@ -1,0 +1,339 @@
+// Ray traversal of BVH2 structures (LBVH and median BVH) and the brute-force
+// NONE path.
+//
+// FAST (the engine's semantics): near child first, far child pushed on a
+// per-thread stack of 64 entries, child boxes clipped to [tmin, closest hit]
+// with a rounding-safe far bound, primitives accepted in (tmin, closest).
+// Replaces boxIntersect + castRay's candidate loop (accelerators.h:668-690,
+// main.cpp:330-358) with a pruned closest-hit walk.
+//
+// REFERENCE: the reference's own semantics, reproduced exactly: the root box
+// and each child box pass the division slab test of accelerators.h:588-626
+// with no clipping, candidates are visited in boxIntersect's pre-order (left
+// subtree before right) and castRay's strict-< selection keeps the first
+// closest.
+//
+// Any-hit queries stop at the first accepted primitive and write one bit per
+// ray (warp ballot).
+#include "rq_device.cuh"
+#include "rq_internal.hpp"
+
+namespace rq {
+namespace {
+
+constexpr int kThreads = 128;
+
+struct Ray {
+  F3 o, d;
+  float tmin, tmax;
+};
+
+__device__ __forceinline__ Ray load_ray(const float4* __restrict__ rays, uint32_t r) {
+  float4 a = __ldg(rays + 2 * (size_t)r), b = __ldg(rays + 2 * (size_t)r + 1);
+  return {{a.x, a.y, a.z}, {b.x, b.y, b.z}, a.w, b.w};
+}
+
+struct Closest {
+  float t;
+  uint32_t prim;
+  float u, v;
+};
+
+// Test the primitives of one leaf.  Returns true when an any-hit query is done.
+template <int KIND, bool ANY, bool REF>
+__device__ __forceinline__ bool test_leaf(const float4* __restrict__ prims,
+                                          const uint32_t* __restrict__ order, uint32_t first,
+                                          int count, const Ray& ray, Closest& c) {
+  for (int k = 0; k < count; ++k) {
+    uint32_t slot = first + (uint32_t)k;
+    if (KIND == kTriangles) {
+      float4 p0 = __ldg(prims + 3 * (size_t)slot), p1 = __ldg(prims + 3 * (size_t)slot + 1),
+             p2 = __ldg(prims + 3 * (size_t)slot + 2);
+      float t, u, v;
+      if (tri_mt(p0, p1, p2, ray.o, ray.d, ray.tmin, ANY ? ray.tmax : c.t, t, u, v)) {
+        if (ANY) return true;
+        c = {t, __float_as_uint(p0.w), u, v};
+      }
+    } else {
+      float4 s = __ldg(prims + slot);
+      if (ANY) {
+        float t0, t1, t;
+        if (REF ? sphere_ref(s, ray.o, ray.d, t0, t1)
+                : sphere_closest(s, ray.o, ray.d, ray.tmin, ray.tmax, false, t))
+          return true;
+      } else {
+        float t;
+        if (sphere_closest(s, ray.o, ray.d, ray.tmin, c.t, REF, t)) c = {t, __ldg(order + slot), 0.f, 0.f};
+      }
+    }
+  }
+  return false;
+}
+
+// Primitive tests one leaf visit performs: every primitive for closest hit;
+// up to and including the first accepted one for any hit (the oracle's count).
+template <int KIND, bool ANY>
+__device__ __forceinline__ uint32_t test_count(const float4* __restrict__ prims, uint32_t first, int count,
+                                               const Ray& ray) {
+  if (!ANY) return (uint32_t)count;
+  Closest dummy = {ray.tmax, kMiss, 0.f, 0.f};
+  for (int k = 0; k < count; ++k)
+    if (test_leaf<KIND, true, false>(prims, nullptr, first + (uint32_t)k, 1, ray, dummy)) return (uint32_t)k + 1;
+  return (uint32_t)count;
+}
+
+template <int KIND, bool ANY, bool COUNT = false>
+__global__ void __launch_bounds__(kThreads) k_trace_fast(Bvh2View bvh, const float4* __restrict__ rays,
+                                                         uint32_t n, float4* __restrict__ hits,
+                                                         uint32_t* __restrict__ occ, uint32_t* err,
+                                                         unsigned long long* counters = nullptr) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  bool occluded = false;
+  uint32_t visits = 0, tests = 0;
+  if (r < n) {
+    Ray ray = load_ray(rays, r);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    F3 inv = {__frcp_rn(ray.d.x), __frcp_rn(ray.d.y), __frcp_rn(ray.d.z)};
+    float tn;
+    const float* rb = bvh.root;
+    if (slab_fast(ray.o, inv, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
+      int2 stack[kStackSize];
+      int sp = 0;
+      int cur = bvh.n_internal ? 0 : -1;
+      int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
+      // A valid walk visits every node at most once.
+      const uint32_t max_steps = 2u * (bvh.n_internal + bvh.n_slots) + 8u;
+      uint32_t steps = 0;
+      for (;;) {
+        if (++steps > max_steps) { atomicOr(err, kErrCorrupt); break; }
+        if (cur >= 0) {
+          const float4* nd = bvh.nodes + 4 * (size_t)cur;
+          float4 a = __ldg(nd), b = __ldg(nd + 1), z = __ldg(nd + 2);
+          int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+          if (COUNT) ++visits;
+          const float tfar = ANY ? ray.tmax : c.t;
+          float tl, tr;
+          bool hl = slab_fast(ray.o, inv, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+          bool hr = slab_fast(ray.o, inv, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+          if (hl && hr) {
+            int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
+            if (tr < tl) { int2 s = nearE; nearE = farE; farE = s; }
+            if (sp >= kStackSize) { atomicOr(err, kErrStackOverflow); break; }
+            stack[sp++] = farE;
+            cur = nearE.x;
+            cnt = nearE.y;
+            continue;
+          }
+          if (hl) { cur = l.x; cnt = l.z; continue; }
+          if (hr) { cur = l.y; cnt = l.w; continue; }
+        } else {
+          if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, (uint32_t)(~cur), cnt, ray);
+          if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) {
+            occluded = true;
+            break;
+          }
+        }
+        if (sp == 0) break;
+        int2 e = stack[--sp];
+        cur = e.x;
+        cnt = e.y;
+      }
+    }
+    if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  }
+  if (ANY) {
+    uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+    uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+  }
+  if (COUNT) {
+    unsigned long long v = visits, t = tests;
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_down_sync(0xffffffffu, v, o);
+      t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(counters, v);
+      atomicAdd(counters + 1, t);
+    }
+  }
+}
+
+// Reference semantics: pre-order, unclipped division slab tests.
+template <int KIND, bool ANY>
+__global__ void __launch_bounds__(kThreads) k_trace_ref(Bvh2View bvh, const float4* __restrict__ rays,
+                                                        uint32_t n, float4* __restrict__ hits,
+                                                        uint32_t* __restrict__ occ, uint32_t* err) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  bool occluded = false;
+  if (r < n) {
+    Ray ray = load_ray(rays, r);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    float a0, a1;
+    const float* rb = bvh.root;
+    if (box_ref(ray.o, ray.d, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], a0, a1)) {
+      int2 stack[kStackSize];
+      int sp = 0;
+      int cur = bvh.n_internal ? 0 : -1;
+      int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
+      // A valid walk visits every node at most once.
+      const uint32_t max_steps = 2u * (bvh.n_internal + bvh.n_slots) + 8u;
+      uint32_t steps = 0;
+      for (;;) {
+        if (++steps > max_steps) { atomicOr(err, kErrCorrupt); break; }
+        if (cur >= 0) {
+          const float4* nd = bvh.nodes + 4 * (size_t)cur;
+          float4 a = __ldg(nd), b = __ldg(nd + 1), z = __ldg(nd + 2);
+          int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+          bool hl = box_ref(ray.o, ray.d, a.x, a.y, a.z, a.w, z.x, z.y, a0, a1);
+          bool hr = box_ref(ray.o, ray.d, b.x, b.y, b.z, b.w, z.z, z.w, a0, a1);
+          if (hr) {
+            if (sp >= kStackSize) { atomicOr(err, kErrStackOverflow); break; }
+            stack[sp++] = make_int2(l.y, l.w);
+          }
+          if (hl) { cur = l.x; cnt = l.z; continue; }
+        } else {
+          if (test_leaf<KIND, ANY, true>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) {
+            occluded = true;
+            break;
+          }
+        }
+        if (sp == 0) break;
+        int2 e = stack[--sp];
+        cur = e.x;
+        cnt = e.y;
+      }
+    }
+    if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  }
+  if (ANY) {
+    uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+    uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+  }
+}
+
+// NONE: every primitive in id order (main.cpp:373-387), staged through
+// shared memory in tiles shared by the block's rays.
+constexpr int kBruteTile = 256;
+
+template <int KIND, bool ANY, bool REF>
+__global__ void __launch_bounds__(kThreads) k_brute(const float4* __restrict__ prims, uint32_t n_prims,
+                                                    const float4* __restrict__ rays, uint32_t n,
+                                                    float4* __restrict__ hits, uint32_t* __restrict__ occ) {
+  constexpr int W = KIND == kTriangles ? 3 : 1;
+  __shared__ float4 tile[kBruteTile * W];
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = r < n;
+  Ray ray = active ? load_ray(rays, r) : Ray{{0, 0, 0}, {0, 0, 1}, 0.f, 0.f};
+  Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+  bool done = !active;
+  for (uint32_t base = 0; base < n_prims; base += kBruteTile) {
+    uint32_t cnt = n_prims - base < (uint32_t)kBruteTile ? n_prims - base : (uint32_t)kBruteTile;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt * W; i += blockDim.x) tile[i] = __ldg(prims + (size_t)base * W + i);
+    __syncthreads();
+    if (done) continue;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      if (KIND == kTriangles) {
+        float t, u, v;
+        if (tri_mt(tile[3 * k], tile[3 * k + 1], tile[3 * k + 2], ray.o, ray.d, ray.tmin,
+                   ANY ? ray.tmax : c.t, t, u, v)) {
+          if (ANY) { done = true; break; }
+          c = {t, base + k, u, v};
+        }
+      } else {
+        if (ANY) {
+          float t0, t1, t;
+          if (REF ? sphere_ref(tile[k], ray.o, ray.d, t0, t1)
+                  : sphere_closest(tile[k], ray.o, ray.d, ray.tmin, ray.tmax, false, t)) {
+            done = true;
+            break;
+          }
+        } else {
+          float t;
+          if (sphere_closest(tile[k], ray.o, ray.d, ray.tmin, c.t, REF, t)) c = {t, base + k, 0.f, 0.f};
+        }
+      }
+    }
+  }
+  if (!ANY && active) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  if (ANY) {
+    bool o = active && done;
+    uint32_t bits = __ballot_sync(0xffffffffu, o);
+    uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+  }
+}
+
+template <int KIND, bool ANY>
+void dispatch_bvh2(int traversal, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
+                   uint32_t* occ, uint32_t* err, cudaStream_t s) {
+  uint32_t g = (n + kThreads - 1) / kThreads;
+  if (traversal == RQ_TRAVERSAL_REFERENCE)
+    k_trace_ref<KIND, ANY><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err);
+  else
+    k_trace_fast<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr);
+}
+
+template <int KIND, bool ANY>
+void dispatch_brute(int traversal, const float4* prims, uint32_t np, const float4* rays, uint32_t n,
+                    float4* hits, uint32_t* occ, cudaStream_t s) {
+  uint32_t g = (n + kThreads - 1) / kThreads;
+  if (traversal == RQ_TRAVERSAL_REFERENCE)
+    k_brute<KIND, ANY, true><<<g, kThreads, 0, s>>>(prims, np, rays, n, hits, occ);
+  else
+    k_brute<KIND, ANY, false><<<g, kThreads, 0, s>>>(prims, np, rays, n, hits, occ);
+}
+
+template <int KIND, bool ANY>
+void dispatch_count(const Bvh2View& v, const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
+                    uint32_t* err, unsigned long long* counters, cudaStream_t s) {
+  uint32_t g = (n + kThreads - 1) / kThreads;
+  k_trace_fast<KIND, ANY, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, counters);
+}
+
+}  // namespace
+
+void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n,
+                               float4* hits, uint32_t* occ, uint32_t* err, unsigned long long* counters,
+                               cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  if (kind == kTriangles) {
+    if (any) dispatch_count<kTriangles, true>(v, rays, n, hits, occ, err, counters, s);
+    else dispatch_count<kTriangles, false>(v, rays, n, hits, occ, err, counters, s);
+  } else {
+    if (any) dispatch_count<kSpheres, true>(v, rays, n, hits, occ, err, counters, s);
+    else dispatch_count<kSpheres, false>(v, rays, n, hits, occ, err, counters, s);
+  }
+}
+
+void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
+                       uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  if (kind == kTriangles) {
+    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, s);
+    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, s);
+  } else {
+    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, s);
+    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, s);
+  }
+}
+
+void launch_trace_brute(int kind, int traversal, bool any, const float4* prims, uint32_t n_prims,
+                        const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
+                        cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  if (kind == kTriangles) {
+    if (any) dispatch_brute<kTriangles, true>(traversal, prims, n_prims, rays, n, hits, occ, s);
+    else dispatch_brute<kTriangles, false>(traversal, prims, n_prims, rays, n, hits, occ, s);
+  } else {
+    if (any) dispatch_brute<kSpheres, true>(traversal, prims, n_prims, rays, n, hits, occ, s);
+    else dispatch_brute<kSpheres, false>(traversal, prims, n_prims, rays, n, hits, occ, s);
+  }
+}
+
+}  // namespace rq

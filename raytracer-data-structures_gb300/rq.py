@@ -1,0 +1,336 @@
+"""Python binding of the engine's C ABI (include/rq.h) over ctypes.
+
+Thin by design: every call goes straight to librq.so.  Arrays are numpy
+(host) or anything exposing a CUDA device pointer (`data_ptr()` of a torch
+tensor, or an int); device buffers are passed with RQ_DEVICE_POINTERS.
+Failures raise RqError carrying the engine's status and message.  There is
+no CPU path: without librq.so or a GPU the calls fail.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librq.so")
+
+BVH, KDTREE, UNIFORM_GRID, LBVH, NONE = 0, 1, 2, 3, 4
+ACC_NAMES = {"BVH": BVH, "KDTREE": KDTREE, "UNIFORM_GRID": UNIFORM_GRID, "LBVH": LBVH, "NONE": NONE}
+TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
+MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1
+DEVICE_POINTERS = 0x1
+MISS = 0xFFFFFFFF
+
+SUCCESS = 0
+STATUS_NAMES = {0: "SUCCESS", 1: "INVALID_ARGUMENT", 2: "UNSUPPORTED", 3: "OUT_OF_MEMORY", 4: "CUDA",
+                5: "STACK_OVERFLOW", 6: "TIMEOUT", 7: "EMPTY_SCENE", 8: "NO_DEVICE"}
+
+RAY_DTYPE = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
+
+
+class Settings(C.Structure):
+    """rq_settings_t: settings.h's fields in order, then engine fields."""
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("fov", C.c_float),
+                ("backgroundColor", C.c_float * 3), ("bias", C.c_float), ("aa_samples", C.c_uint32),
+                ("dataStructure", C.c_int32), ("sceneModel", C.c_int32), ("traversal", C.c_int32),
+                ("morton", C.c_int32), ("kd_max_depth", C.c_int32), ("reserved", C.c_int32 * 5)]
+
+
+class AccelInfo(C.Structure):
+    _fields_ = [("type", C.c_int32), ("prim_kind", C.c_int32), ("n_prims", C.c_uint32),
+                ("n_nodes", C.c_uint32), ("n_slots", C.c_uint32), ("max_depth", C.c_uint32),
+                ("root_bounds", C.c_float * 6), ("device_bytes", C.c_uint64)]
+
+
+class RqError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Load librq.so, compiling it from csrc/ first when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise ImportError(f"{LIB_PATH} is missing: build the engine first")
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("rq_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = C.CDLL(LIB_PATH)
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int32
+    sig = {
+        "rq_settings_default": (None, [vp]),
+        "rq_create": (i32, [vp, C.c_int, vp]),
+        "rq_destroy": (i32, [vp]),
+        "rq_get_settings": (i32, [vp, vp]),
+        "rq_set_settings": (i32, [vp, vp]),
+        "rq_set_stream": (i32, [vp, vp]),
+        "rq_synchronize": (i32, [vp]),
+        "rq_last_error": (C.c_char_p, [vp]),
+        "rq_status_string": (C.c_char_p, [i32]),
+        "rq_scene_create_triangles": (i32, [vp, vp, u32, vp, u32, u32, vp]),
+        "rq_scene_create_spheres": (i32, [vp, vp, u32, u32, vp]),
+        "rq_scene_update": (i32, [vp, vp, vp, vp, u32]),
+        "rq_scene_destroy": (i32, [vp]),
+        "rq_build": (i32, [vp, vp, i32, vp]),
+        "rq_accel_rebuild": (i32, [vp, vp]),
+        "rq_accel_destroy": (i32, [vp]),
+        "rq_accel_get_info": (i32, [vp, vp]),
+        "rq_accel_export_bvh2": (i32, [vp, vp, vp, vp, vp]),
+        "rq_accel_export_kd": (i32, [vp, vp, vp, vp]),
+        "rq_trace_closest": (i32, [vp, vp, vp, u32, vp, u32]),
+        "rq_trace_any": (i32, [vp, vp, vp, u32, vp, u32]),
+        "rq_morton_codes": (i32, [vp, vp, vp, u32]),
+        "rq_sort_pairs": (i32, [vp, vp, vp, u32, u32, u32]),
+        "rq_render_reference": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+        "rq_trace_counters": (i32, [vp, vp, vp, u32, i32, vp, vp, u32]),
+        "rq_kernel_launch_count": (C.c_uint64, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    """Host numpy array -> (pointer, 0); device buffer -> (pointer, DEVICE_POINTERS)."""
+    if a is None:
+        return None, 0
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data, 0
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr(), DEVICE_POINTERS
+    return int(a), DEVICE_POINTERS
+
+
+def default_settings(**kw):
+    s = Settings()
+    load().rq_settings_default(C.byref(s))
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+class Scene:
+    def __init__(self, engine, handle, kind, n):
+        self.engine, self.handle, self.kind, self.n = engine, handle, kind, n
+
+    def update(self, data, idx=None):
+        p, fl = _ptr(data)
+        pi, _ = _ptr(idx)
+        self.engine._check(load().rq_scene_update(self.engine.ctx, self.handle, p, pi, fl))
+
+    def close(self):
+        if self.handle:
+            load().rq_scene_destroy(self.handle)
+            self.handle = None
+
+
+class Accel:
+    def __init__(self, engine, handle, scene, acc_type):
+        self.engine, self.handle, self.scene, self.type = engine, handle, scene, acc_type
+
+    def info(self):
+        inf = AccelInfo()
+        self.engine._check(load().rq_accel_get_info(self.handle, C.byref(inf)))
+        return inf
+
+    def rebuild(self):
+        self.engine._check(load().rq_accel_rebuild(self.engine.ctx, self.handle))
+
+    def close(self):
+        if self.handle:
+            load().rq_accel_destroy(self.handle)
+            self.handle = None
+
+
+class Engine:
+    """One context on one device (rq_create)."""
+
+    def __init__(self, device=0, settings=None):
+        lib = load()
+        self.ctx = C.c_void_p()
+        st = lib.rq_create(C.byref(settings) if settings is not None else None, device, C.byref(self.ctx))
+        if st != SUCCESS:
+            raise RqError(st, lib.rq_status_string(st).decode())
+
+    # -- plumbing
+    def _check(self, st):
+        if st != SUCCESS:
+            raise RqError(st, (load().rq_last_error(self.ctx) or b"").decode())
+
+    def close(self):
+        if self.ctx:
+            load().rq_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def settings(self):
+        s = Settings()
+        self._check(load().rq_get_settings(self.ctx, C.byref(s)))
+        return s
+
+    @settings.setter
+    def settings(self, s):
+        self._check(load().rq_set_settings(self.ctx, C.byref(s)))
+
+    def configure(self, **kw):
+        s = self.settings
+        for k, v in kw.items():
+            setattr(s, k, v)
+        self.settings = s
+
+    def set_stream(self, stream_ptr):
+        self._check(load().rq_set_stream(self.ctx, stream_ptr))
+
+    def synchronize(self):
+        self._check(load().rq_synchronize(self.ctx))
+
+    # -- scenes and builds
+    def scene_triangles(self, verts, idx):
+        if isinstance(verts, np.ndarray):
+            verts = np.ascontiguousarray(verts, np.float32)
+            idx = np.ascontiguousarray(idx, np.uint32)
+            nv, nt = verts.size // 3, idx.size // 3
+        else:
+            nv, nt = verts.numel() // 3, idx.numel() // 3
+        pv, fl = _ptr(verts)
+        pi, _ = _ptr(idx)
+        h = C.c_void_p()
+        self._check(load().rq_scene_create_triangles(self.ctx, pv, nv, pi, nt, fl, C.byref(h)))
+        return Scene(self, h, 0, nt)
+
+    def scene_spheres(self, sph):
+        if isinstance(sph, np.ndarray):
+            sph = np.ascontiguousarray(sph, np.float32)
+            n = sph.size // 4
+        else:
+            n = sph.numel() // 4
+        p, fl = _ptr(sph)
+        h = C.c_void_p()
+        self._check(load().rq_scene_create_spheres(self.ctx, p, n, fl, C.byref(h)))
+        return Scene(self, h, 1, n)
+
+    def build(self, scene, acc_type):
+        if isinstance(acc_type, str):
+            acc_type = ACC_NAMES[acc_type]
+        h = C.c_void_p()
+        self._check(load().rq_build(self.ctx, scene.handle, acc_type, C.byref(h)))
+        return Accel(self, h, scene, acc_type)
+
+    # -- queries
+    def trace_closest(self, accel, rays, hits=None):
+        if isinstance(rays, np.ndarray):
+            rays = np.ascontiguousarray(rays, RAY_DTYPE)
+            n = len(rays)
+            hits = np.zeros(n, HIT_DTYPE) if hits is None else hits
+        else:
+            n = rays.numel() * rays.element_size() // 32
+        pr, fl = _ptr(rays)
+        ph, _ = _ptr(hits)
+        self._check(load().rq_trace_closest(self.ctx, accel.handle, pr, n, ph, fl))
+        return hits
+
+    def trace_any(self, accel, rays, bits=None):
+        if isinstance(rays, np.ndarray):
+            rays = np.ascontiguousarray(rays, RAY_DTYPE)
+            n = len(rays)
+            bits = np.zeros((n + 31) // 32, np.uint32) if bits is None else bits
+        else:
+            n = rays.numel() * rays.element_size() // 32
+        pr, fl = _ptr(rays)
+        pb, _ = _ptr(bits)
+        self._check(load().rq_trace_any(self.ctx, accel.handle, pr, n, pb, fl))
+        return bits
+
+    def trace_counters(self, accel, rays, any_hit=False):
+        """FAST query plus (internal nodes visited, primitives tested) summed over the rays."""
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        n = len(rays)
+        out = np.zeros((n + 31) // 32, np.uint32) if any_hit else np.zeros(n, HIT_DTYPE)
+        cnt = np.zeros(2, np.uint64)
+        self._check(load().rq_trace_counters(self.ctx, accel.handle, rays.ctypes.data, n, int(any_hit),
+                                             out.ctypes.data, cnt.ctypes.data, 0))
+        return out, cnt
+
+    # -- component kernels
+    def morton_codes(self, scene):
+        out = np.zeros(scene.n, np.uint32)
+        self._check(load().rq_morton_codes(self.ctx, scene.handle, out.ctypes.data, 0))
+        return out
+
+    def sort_pairs(self, keys, vals, key_bits=32):
+        if isinstance(keys, np.ndarray):
+            keys = np.array(keys, np.uint32, copy=True)
+            vals = np.array(vals, np.uint32, copy=True)
+            n = len(keys)
+        else:
+            n = keys.numel()
+        pk, fl = _ptr(keys)
+        pv, _ = _ptr(vals)
+        self._check(load().rq_sort_pairs(self.ctx, pk, pv, n, key_bits, fl))
+        return keys, vals
+
+    def export_bvh2(self, accel):
+        inf = accel.info()
+        nodes = np.zeros((inf.n_nodes, 16), np.float32)
+        order = np.zeros(inf.n_slots, np.uint32)
+        codes = np.zeros(inf.n_prims, np.uint32) if accel.type == LBVH else None
+        self._check(load().rq_accel_export_bvh2(self.ctx, accel.handle, nodes.ctypes.data, order.ctypes.data,
+                                                codes.ctypes.data if codes is not None else None))
+        return nodes, order, codes, np.array(inf.root_bounds, np.float32), inf
+
+    def export_kd(self, accel):
+        inf = accel.info()
+        nodes = np.zeros((inf.n_nodes, 3), np.int32)
+        pidx = np.zeros(max(inf.n_slots, 1), np.int32)
+        self._check(load().rq_accel_export_kd(self.ctx, accel.handle, nodes.ctypes.data, pidx.ctypes.data))
+        return nodes, pidx[:inf.n_slots], np.array(inf.root_bounds, np.float32), inf
+
+    def render_reference(self, accel, settings=None, jitter=None, surface_rgb=None):
+        s = settings if settings is not None else self.settings
+        npix = s.width * s.height
+        pixels = np.zeros(npix * 3, np.uint8)
+        rgb = np.zeros(npix * 3, np.float32)
+        jit = np.ascontiguousarray(jitter, np.float64) if jitter is not None else None
+        srgb = np.ascontiguousarray(surface_rgb, np.float32)
+        self._check(load().rq_render_reference(self.ctx, accel.handle, C.byref(s),
+                                               jit.ctypes.data if jit is not None else None,
+                                               srgb.ctypes.data, pixels.ctypes.data, rgb.ctypes.data))
+        return pixels, rgb.reshape(-1, 3)
+
+
+def kernel_launch_count():
+    return int(load().rq_kernel_launch_count())
+
+
+def make_rays(org, dirs, tmin=0.0, tmax=np.inf):
+    dirs = np.asarray(dirs, np.float32)
+    r = np.zeros(len(dirs), RAY_DTYPE)
+    r["org"] = np.broadcast_to(np.asarray(org, np.float32), dirs.shape)
+    r["dir"] = dirs
+    r["tmin"] = tmin
+    r["tmax"] = tmax
+    return r
+
+
+def unpack_bits(bits, n):
+    b = np.asarray(bits, np.uint32)
+    return ((b[np.arange(n) >> 5] >> (np.arange(n) & 31).astype(np.uint32)) & 1).astype(np.uint8)

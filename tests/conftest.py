@@ -30,3 +30,28 @@ def golden(name):
 @pytest.fixture(scope="session")
 def bunny():
     return golden("bunny")
+
+
+@pytest.fixture(scope="session")
+def rqm():
+    import rq
+    return rq
+
+
+@pytest.fixture()
+def engine():
+    import rq
+    eng = rq.Engine(0)
+    yield eng
+    eng.close()
+
+
+def bvh2_from_export(oracle, nodes, order, root, codes=None):
+    """Engine-exported BVH2 arrays as an oracle Bvh2."""
+    return oracle.Bvh2(np.ascontiguousarray(nodes, np.float32), len(nodes), root, order, codes)
+
+
+def sphere_surface_colors(n):
+    c = np.tile(np.array([0.8, 0.7, 0.0], np.float32), (n, 1))
+    c[-1] = 0.0
+    return c
