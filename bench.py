@@ -39,7 +39,7 @@ UNIT = "Grays/s"
 WORKLOAD = ("LBVH build + incoherent traversal: 998,000-triangle fBm heightfield (1001x500), "
             "1920x1080x4 jittered primary closest-hit + cosine secondary closest-hit + shadow any-hit")
 SEED = 20261203
-EYE, TARGET, FOV = (0.0, -1.9, 1.9), (0.0, 0.15, 0.0), 40.0
+EYE, TARGET, FOV = (0.0, -0.6, 1.1), (0.0, 0.0, 0.0), 40.0  # the view lies inside the heightfield
 LIGHT = (1.5, -1.0, 3.0)
 RAY_BYTES, HIT_BYTES, NODE_BYTES, TRI_BYTES = 32, 16, 64, 48
 
@@ -53,10 +53,11 @@ def dist_env():
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_inputs():
+def make_inputs(small=False):
     import scenes
     verts, idx = scenes.heightfield(1001, 500, amplitude=0.3, octaves=5, seed=SEED % 1000)
-    primary = scenes.pinhole_rays(1920, 1080, 4, eye=EYE, target=TARGET, fov_deg=FOV, seed=SEED + 1)
+    w, h = (960, 540) if small else (1920, 1080)  # --small: profiling case, same mesh
+    primary = scenes.pinhole_rays(w, h, 4, eye=EYE, target=TARGET, fov_deg=FOV, seed=SEED + 1)
     return verts, idx, primary
 
 
@@ -153,9 +154,11 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # One stream for everything: torch ops, CUDA events and the engine's work.
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
 
-    verts, idx, primary = make_inputs()
+    verts, idx, primary = make_inputs(args.small)
     n_tri = len(idx)
     eng = rq.Engine(local)
     eng.set_stream(stream.cuda_stream)
@@ -362,7 +365,10 @@ class CpuBaseline:
         self.cores = os.cpu_count() or 1
         self.prims, aabb, cen = O.tri_prims(verts, idx)
         t0 = time.perf_counter()
-        self.bvh = O.build_median(aabb, cen, compat=True)
+        # The reference's partition + nth_element median build; on meshes its
+        # degenerate nodes (all centroids at or above the midpoint) would recurse
+        # forever, so the oracle's rule (such a node becomes one leaf) is used.
+        self.bvh = O.build_median(aabb, cen, compat=False)
         self.build_s = time.perf_counter() - t0
         self.n_tri = len(idx)
         self.counts = counts
@@ -456,6 +462,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--small", action="store_true", help="960x540x4 rays (profiling case)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

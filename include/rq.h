@@ -150,7 +150,9 @@ rq_status_t rq_create(const rq_settings_t* settings, int device, rq_ctx_t* out);
 rq_status_t rq_destroy(rq_ctx_t ctx);
 rq_status_t rq_get_settings(rq_ctx_t ctx, rq_settings_t* out);
 rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* settings);
-/* cudaStream_t passed as void*; NULL selects the engine's own stream. */
+/* All later work of the context goes to this cudaStream_t (passed as void*,
+ * used as given: NULL is the CUDA legacy default stream).  A new context
+ * starts on a non-blocking stream of its own. */
 rq_status_t rq_set_stream(rq_ctx_t ctx, void* cuda_stream);
 rq_status_t rq_synchronize(rq_ctx_t ctx);
 const char* rq_last_error(rq_ctx_t ctx);

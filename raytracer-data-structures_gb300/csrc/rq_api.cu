@@ -215,7 +215,7 @@ rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
 
 rq_status_t rq_set_stream(rq_ctx_t ctx, void* stream) {
   if (!ctx) return RQ_ERROR_INVALID_ARGUMENT;
-  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  ctx->stream = static_cast<cudaStream_t>(stream);
   return RQ_SUCCESS;
 }
 
