@@ -234,6 +234,27 @@ rq_status_t rq_morton_codes(rq_ctx_t ctx, rq_scene_t scene, uint32_t* codes, uin
 rq_status_t rq_sort_pairs(rq_ctx_t ctx, uint32_t* keys, uint32_t* values, uint32_t n,
                           uint32_t key_bits, uint32_t flags);
 
+/* The same sort for callers that must not allocate device memory while they
+ * run: a serving loop held to a fixed memory budget, code whose device memory
+ * belongs to another allocator, or a latency-critical loop where cudaMalloc /
+ * cudaFree would synchronize the device.  This entry point has no counterpart
+ * in the reference.
+ *  - keys and values are device pointers on the current device; no context is
+ *    needed.  Work is enqueued on cuda_stream (NULL: the legacy default
+ *    stream) and the call returns once the sort has finished on it.
+ *  - No memory is allocated: the working memory is one fixed array of about
+ *    9.5 MB that every GPU loading this library holds until the process exits.
+ *    It bounds n to RQ_SORT_NOALLOC_MAX_PAIRS; larger n returns
+ *    RQ_ERROR_INVALID_ARGUMENT.
+ *  - The first call on each device looks up the array's device address; make
+ *    that first call before any stream capture.
+ *  - All calls on a device share the array, so calls that overlap on the GPU
+ *    (other streams, other host threads) race and must be serialized by the
+ *    caller. */
+#define RQ_SORT_NOALLOC_MAX_PAIRS (1u << 20)
+rq_status_t rq_sort_pairs_noalloc(uint32_t* keys, uint32_t* values, uint32_t n, uint32_t key_bits,
+                                  void* cuda_stream);
+
 /* ------------------------------------------------------------ render step */
 
 /* render() (main.cpp:541-566) with castRay's shading (main.cpp:390-497) for

@@ -94,6 +94,7 @@ def load(build_if_missing=True):
         "rq_render_reference": (i32, [vp, vp, vp, vp, vp, vp, vp]),
         "rq_trace_counters": (i32, [vp, vp, vp, u32, i32, vp, vp, u32]),
         "rq_kernel_launch_count": (C.c_uint64, []),
+        "rq_sort_pairs_noalloc": (i32, [vp, vp, u32, u32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -315,6 +316,15 @@ class Engine:
                                                jit.ctypes.data if jit is not None else None,
                                                srgb.ctypes.data, pixels.ctypes.data, rgb.ctypes.data))
         return pixels, rgb.reshape(-1, 3)
+
+
+SORT_NOALLOC_MAX_PAIRS = 1 << 20
+
+
+def sort_pairs_noalloc(keys_ptr, vals_ptr, n, key_bits=32, stream_ptr=None):
+    """rq_sort_pairs_noalloc on device buffers (pointers as ints); returns the status.
+    Allocates nothing: for callers that cannot allocate device memory mid-run."""
+    return int(load().rq_sort_pairs_noalloc(keys_ptr, vals_ptr, n, key_bits, stream_ptr))
 
 
 def kernel_launch_count():
