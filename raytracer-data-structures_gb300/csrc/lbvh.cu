@@ -183,3 +183,27 @@ void launch_prims_by_id(int kind, const float* verts, const uint32_t* idx, const
 }
 
 }  // namespace rq
+
+namespace rq {
+namespace {
+
+__global__ void __launch_bounds__(kThreads) k_prims_gather(int kind, const float* __restrict__ verts,
+                                                           const uint32_t* __restrict__ idx,
+                                                           const float4* __restrict__ sph,
+                                                           const uint32_t* __restrict__ order, uint32_t n,
+                                                           float4* __restrict__ prims) {
+  uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  emit_prim(kind, verts, idx, sph, __ldg(order + j), prims, j);
+}
+
+}  // namespace
+
+void launch_prims_gather(int kind, const float* verts, const uint32_t* idx, const float4* sph,
+                         const uint32_t* order, uint32_t n, float4* prims, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  k_prims_gather<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kind, verts, idx, sph, order, n, prims);
+}
+
+}  // namespace rq

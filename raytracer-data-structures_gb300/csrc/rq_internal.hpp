@@ -80,6 +80,17 @@ void launch_refit(int kind, const float* verts, const uint32_t* idx, const float
 void launch_prims_by_id(int kind, const float* verts, const uint32_t* idx, const float4* sph,
                         uint32_t n, float4* prims, float* aabb6, cudaStream_t s);
 
+// Payload gathered in slot order (order[slot] = primitive id).
+void launch_prims_gather(int kind, const float* verts, const uint32_t* idx, const float4* sph,
+                         const uint32_t* order, uint32_t n, float4* prims, cudaStream_t s);
+
+// ----------------------------------------------------------------- scan
+// Exclusive prefix sum of n 32-bit values; tmp holds scan_tmp_words(n) words;
+// total (may be null) receives the sum.
+size_t scan_tmp_words(uint64_t n);
+void launch_scan_excl(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp, uint32_t* total,
+                      cudaStream_t s);
+
 // ------------------------------------------------------------ traversal
 struct Bvh2View {
   const float4* nodes;
