@@ -425,8 +425,12 @@ struct KdBuilder {
     } else if (np == 1) {
       w[0] = prims[0];
     } else {
+      // Leaf lists in primitive-id order: the reference's order inside a
+      // leaf comes from an unstable edge sort, so only the set is its own.
       w[0] = (int32_t)prim_idx.size();
-      prim_idx.insert(prim_idx.end(), prims.begin(), prims.end());
+      std::vector<int> sorted(prims);
+      std::sort(sorted.begin(), sorted.end());
+      prim_idx.insert(prim_idx.end(), sorted.begin(), sorted.end());
     }
   }
 

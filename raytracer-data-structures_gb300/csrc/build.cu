@@ -149,7 +149,7 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
                        q.occ, st);
   } else if (type == RQ_KDTREE) {
     KdView v{a.kd_nodes.as<const int4>(), a.kd_idx.as<const int32_t>(), a.prims.as<const float4>(),
-             a.root.as<const float>()};
+             a.root.as<const float>(), a.n_nodes};
     launch_trace_kd(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
   } else {
     Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),

@@ -1,13 +1,830 @@
-// SAH KD-tree build and traversal (accelerators.h:715-1086) on the GPU.
+// SAH KD tree on the GPU: constructKDTreeNew / buildTree (accelerators.h:815-988)
+// built breadth first, then laid out depth first exactly as the reference lays
+// it out (below child = node + 1, above child = next free node after the below
+// subtree, accelerators.h:940-947), plus its traversal (kdtreeIntersect,
+// accelerators.h:997-1086).
+//
+// Parameters are the reference's effective ones: maxPrims = 5, isectCost = 80,
+// traversalCost = 1, emptyBonus = 0 (the global `char emptyBonus = 0.5f`
+// truncates, accelerators.h:767-770); maxDepth = round(8 + 1.3 log2 N).
+//
+// Per level, for every node still splitting:
+//  * its primitive list is kept sorted by id, so a stable sort of its edges by
+//    (node, t, start-before-end) orders ties by primitive id;
+//  * two prefix sums give nBelow / nAbove at every edge and the SAH cost is
+//    evaluated with the reference's float operations (no fused multiply-add);
+//  * a 64-bit atomicMin of (cost, edge index) per node takes the first
+//    cheapest edge (buildTree's strict <);
+//  * a node with no candidate on its longest axis retries the next axis, up
+//    to twice (:915-919), in further passes over only those nodes;
+//  * the leaf rules (maxPrims, depth, 4x old cost under 16 primitives, three
+//    bad refines, :843, :920-925) decide; primitives whose start edge precedes
+//    the split go below, those whose end edge follows it go above (:928-934).
+// Leaves list their primitives by id (the reference's order inside a leaf
+// comes from an unstable sort).
+#include <algorithm>
+#include <vector>
+
 #include "rq_build.hpp"
+#include "rq_device.cuh"
 
 namespace rq {
+namespace {
 
-BuildResult build_kd_tree(const SceneView&, int, AccelBuffers&, BuildScratch&, uint32_t*, cudaStream_t) {
-  return BuildResult::error(RQ_ERROR_UNSUPPORTED, "KD builder not available yet");
+constexpr int kThreads = 256;
+constexpr int kMaxPrims = 5;
+constexpr float kIsect = 80.f, kTrav = 1.f, kEmptyBonus = 0.f;
+constexpr unsigned long long kNone = ~0ull;
+
+inline unsigned grid(uint64_t n) { return n ? (unsigned)((n + kThreads - 1) / kThreads) : 1u; }
+
+__device__ __forceinline__ uint32_t float_key(float f) {
+  uint32_t b = __float_as_uint(__fadd_rn(f, 0.0f));
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
 }
 
-void launch_trace_kd(int, int, bool, const KdView&, const float4*, uint32_t, float4*, uint32_t*, uint32_t*,
-                     cudaStream_t) {}
+// Level-local node state.
+struct LevelNodes {
+  float* box;         // 6 per node
+  int32_t* depth;
+  int32_t* bad;       // badRefines
+  uint32_t* rs;       // first ref
+  uint32_t* rc;       // ref count
+  int32_t* axis0;
+  int32_t* eval;      // axis evaluated in the current pass, -1 when not pending
+  int32_t* retries;
+  unsigned long long* best;  // (cost key << 32) | edge offset
+  uint32_t* edge_base;
+  int32_t* state;     // 0 undecided, 1 leaf, 2 interior
+  int32_t* best_axis;
+  uint32_t* best_off;
+  float* tsplit;
+  int32_t* pass_found;  // pass in which the split was found
+};
+
+// Pre-leaf test and first axis (:843, :860).
+__global__ void k_node_init(LevelNodes L, uint32_t M) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  const float* b = L.box + 6 * (size_t)k;
+  L.best[k] = kNone;
+  L.retries[k] = 0;
+  L.pass_found[k] = -1;
+  L.best_axis[k] = -1;
+  if ((int)L.rc[k] <= kMaxPrims || L.depth[k] == 0) {
+    L.state[k] = 1;
+    L.eval[k] = -1;
+    return;
+  }
+  float ax = __fsub_rn(b[3], b[0]), ay = __fsub_rn(b[4], b[1]), az = __fsub_rn(b[5], b[2]);
+  int a = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
+  L.state[k] = 0;
+  L.axis0[k] = a;
+  L.eval[k] = a;
+}
+
+__global__ void k_pending_flags(const uint32_t* __restrict__ ref_node, uint32_t R, const int32_t* __restrict__ eval,
+                                uint32_t* __restrict__ flag) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > R) return;
+  flag[r] = r < R && eval[ref_node[r]] >= 0 ? 1u : 0u;
+}
+
+// Two edges per pending ref: (min, start) and (max, end) along the node's axis.
+__global__ void k_edges(const uint32_t* __restrict__ ref_prim, const uint32_t* __restrict__ ref_node, uint32_t R,
+                        const uint32_t* __restrict__ flag, const uint32_t* __restrict__ epos, LevelNodes L,
+                        const float* __restrict__ aabb, unsigned long long* __restrict__ keys,
+                        uint32_t* __restrict__ vals, uint32_t E, uint32_t* err) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R || !flag[r]) return;
+  const uint32_t k = ref_node[r];
+  const int a = L.eval[k];
+  const uint32_t e = 2 * epos[r];
+  if (e + 1 >= E || a < 0 || a > 2) { atomicOr(err, kErrCorrupt); return; }
+  if (r == L.rs[k]) L.edge_base[k] = e;
+  const float* q = aabb + 6 * (size_t)ref_prim[r];
+  const unsigned long long hi = (unsigned long long)k << 33;
+  keys[e] = hi | ((unsigned long long)float_key(__ldg(q + a)) << 1) | 0ull;
+  keys[e + 1] = hi | ((unsigned long long)float_key(__ldg(q + 3 + a)) << 1) | 1ull;
+  vals[e] = r;
+  vals[e + 1] = r;
+}
+
+__global__ void k_edge_flags(const unsigned long long* __restrict__ keys, uint32_t E, uint32_t* __restrict__ fs,
+                             uint32_t* __restrict__ fe) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > E) return;
+  const bool end = i < E && (keys[i] & 1ull);
+  fs[i] = i < E && !end ? 1u : 0u;
+  fe[i] = end ? 1u : 0u;
+}
+
+// SAH cost of splitting at every edge (buildTree :883-912, same float ops).
+__global__ void k_cost(const unsigned long long* __restrict__ keys, uint32_t E, const uint32_t* __restrict__ ss,
+                       const uint32_t* __restrict__ se, LevelNodes L) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const unsigned long long key = keys[i];
+  const uint32_t k = (uint32_t)(key >> 33);
+  const int axis = L.eval[k];
+  const float t = key_float((uint32_t)(key >> 1));
+  const float* b = L.box + 6 * (size_t)k;
+  const float lo = b[axis], hi = b[3 + axis];
+  if (!(t > lo && t < hi)) return;
+  const uint32_t base = L.edge_base[k];
+  const uint32_t n = L.rc[k];
+  const uint32_t nBelow = ss[i] - ss[base];
+  const uint32_t nEndIncl = se[i] - se[base] + (uint32_t)(key & 1ull);
+  const uint32_t nAbove = n - nEndIncl;
+  float d[3] = {__fsub_rn(b[3], b[0]), __fsub_rn(b[4], b[1]), __fsub_rn(b[5], b[2])};
+  float totalSA = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[1]), __fmul_rn(d[0], d[2])),
+                                            __fmul_rn(d[1], d[2])));
+  float invTotalSA = __fdiv_rn(1.f, totalSA);
+  const int o0 = (axis + 1) % 3, o1 = (axis + 2) % 3;
+  float dd = __fmul_rn(d[o0], d[o1]), ds = __fadd_rn(d[o0], d[o1]);
+  float belowSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(t, lo), ds)));
+  float aboveSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(hi, t), ds)));
+  float pB = __fmul_rn(belowSA, invTotalSA), pA = __fmul_rn(aboveSA, invTotalSA);
+  float eb = (nAbove == 0 || nBelow == 0) ? kEmptyBonus : 0.f;
+  float cost = __fadd_rn(kTrav, __fmul_rn(__fmul_rn(kIsect, __fsub_rn(1.f, eb)),
+                                          __fadd_rn(__fmul_rn(pB, (float)nBelow), __fmul_rn(pA, (float)nAbove))));
+  const unsigned long long ck = ((unsigned long long)float_key(cost) << 32) | (unsigned long long)(i - base);
+  atomicMin(L.best + k, ck);
+}
+
+// After a pass: found split -> leaf/interior decision (:920-925); none -> next axis.
+__global__ void k_pass_decide(LevelNodes L, uint32_t M, int pass) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= M || L.eval[k] < 0) return;
+  const unsigned long long b = L.best[k];
+  if (b != kNone) {
+    const float bestCost = key_float((uint32_t)(b >> 32));
+    const float oldCost = __fmul_rn(kIsect, (float)L.rc[k]);
+    int bad = L.bad[k] + (bestCost > oldCost ? 1 : 0);
+    L.bad[k] = bad;
+    const bool leaf = (bestCost > __fmul_rn(4.f, oldCost) && L.rc[k] < 16) || bad == 3;
+    L.state[k] = leaf ? 1 : 2;
+    L.best_axis[k] = L.eval[k];
+    L.best_off[k] = (uint32_t)(b & 0xFFFFFFFFull);
+    L.pass_found[k] = pass;
+    L.eval[k] = -1;
+    return;
+  }
+  int r = L.retries[k] + 1;
+  L.retries[k] = r;
+  if (r <= 2) {
+    L.eval[k] = (L.axis0[k] + r) % 3;
+  } else {
+    L.state[k] = 1;  // no split found on any axis
+    L.eval[k] = -1;
+  }
+}
+
+// Below/above sides from the winning pass's sorted edges (:928-934).
+__global__ void k_classify(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t E,
+                           LevelNodes L, int pass, uint32_t* __restrict__ below, uint32_t* __restrict__ above,
+                           uint32_t R, uint32_t* err) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const unsigned long long key = keys[i];
+  const uint32_t k = (uint32_t)(key >> 33);
+  if (L.pass_found[k] != pass || L.state[k] != 2) return;
+  const uint32_t off = i - L.edge_base[k], best = L.best_off[k];
+  const uint32_t r = vals[i];
+  if (r >= R) { atomicOr(err, kErrCorrupt); return; }
+  if (key & 1ull) above[r] = off > best ? 1u : 0u;
+  else below[r] = off < best ? 1u : 0u;
+  if (off == best) L.tsplit[k] = key_float((uint32_t)(key >> 1));
+}
+
+__global__ void k_flag_of_state(LevelNodes L, uint32_t M, int want, uint32_t* __restrict__ out, int with_count) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > M) return;
+  out[k] = (k < M && L.state[k] == want) ? (with_count ? L.rc[k] : 1u) : 0u;
+}
+
+// Global node table (breadth-first ids).
+struct Table {
+  int32_t* leaf;        // 1 leaf, 0 interior
+  int32_t* axis;
+  float* split;
+  uint32_t* child0;
+  uint32_t* child1;
+  uint32_t* count;      // leaf primitive count
+  uint32_t* pool_off;   // leaf primitives in the pool
+};
+
+// Interior nodes spawn their two children; every node fills its table entry.
+__global__ void k_spawn(LevelNodes L, uint32_t M, const uint32_t* __restrict__ irank, const uint32_t* __restrict__ sB,
+                        const uint32_t* __restrict__ sA, const uint32_t* __restrict__ lrank_cnt, uint32_t pool_base,
+                        uint32_t level_base, uint32_t next_base, Table T, LevelNodes N,
+                        uint32_t* __restrict__ child_cnt, uint32_t M2, uint32_t* err) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  const uint32_t g = level_base + k;
+  const uint32_t rs = L.rs[k], rc = L.rc[k];
+  if (L.state[k] != 2) {
+    T.leaf[g] = 1;
+    T.count[g] = rc;
+    T.pool_off[g] = pool_base + lrank_cnt[k];
+    return;
+  }
+  const uint32_t c = 2 * irank[k];
+  if (c + 1 >= M2 + 1 || L.best_axis[k] < 0) { atomicOr(err, kErrCorrupt); return; }
+  const int axis = L.best_axis[k];
+  const float ts = L.tsplit[k];
+  T.leaf[g] = 0;
+  T.axis[g] = axis;
+  T.split[g] = ts;
+  T.child0[g] = next_base + c;
+  T.child1[g] = next_base + c + 1;
+  const float* b = L.box + 6 * (size_t)k;
+  for (int side = 0; side < 2; ++side) {
+    float* nb = N.box + 6 * (size_t)(c + side);
+    for (int q = 0; q < 6; ++q) nb[q] = b[q];
+    if (side == 0) nb[3 + axis] = ts;  // bounds0.max[axis] = tSplit
+    else nb[axis] = ts;                // bounds1.min[axis] = tSplit
+    N.depth[c + side] = L.depth[k] - 1;
+    N.bad[c + side] = L.bad[k];
+  }
+  child_cnt[c] = sB[rs + rc] - sB[rs];
+  child_cnt[c + 1] = sA[rs + rc] - sA[rs];
+}
+
+__global__ void k_set_ref_starts(LevelNodes N, uint32_t M2, const uint32_t* __restrict__ child_cnt,
+                                 const uint32_t* __restrict__ child_off) {
+  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= M2) return;
+  N.rs[c] = child_off[c];
+  N.rc[c] = child_cnt[c];
+}
+
+// Stable filter of every interior node's refs into its children; leaf refs to the pool.
+__global__ void k_emit_refs(const uint32_t* __restrict__ ref_prim, const uint32_t* __restrict__ ref_node, uint32_t R,
+                            LevelNodes L, const uint32_t* __restrict__ irank, const uint32_t* __restrict__ below,
+                            const uint32_t* __restrict__ above, const uint32_t* __restrict__ sB,
+                            const uint32_t* __restrict__ sA, LevelNodes N, uint32_t* __restrict__ out_prim,
+                            uint32_t* __restrict__ out_node, const uint32_t* __restrict__ lrank_cnt,
+                            uint32_t pool_base, uint32_t* __restrict__ pool, uint32_t R2, uint32_t pool_cap,
+                            uint32_t* err) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const uint32_t k = ref_node[r];
+  const uint32_t p = ref_prim[r];
+  const uint32_t rs = L.rs[k];
+  if (L.state[k] != 2) {
+    const uint32_t q = pool_base + lrank_cnt[k] + (r - rs);
+    if (q >= pool_cap) { atomicOr(err, kErrCorrupt); return; }
+    pool[q] = p;
+    return;
+  }
+  const uint32_t c = 2 * irank[k];
+  if (below[r]) {
+    const uint32_t o = N.rs[c] + (sB[r] - sB[rs]);
+    if (o >= R2) { atomicOr(err, kErrCorrupt); return; }
+    out_prim[o] = p;
+    out_node[o] = c;
+  }
+  if (above[r]) {
+    const uint32_t o = N.rs[c + 1] + (sA[r] - sA[rs]);
+    if (o >= R2) { atomicOr(err, kErrCorrupt); return; }
+    out_prim[o] = p;
+    out_node[o] = c + 1;
+  }
+}
+
+// Depth-first layout: subtree sizes bottom-up, positions top-down.
+__global__ void k_sizes(Table T, uint32_t lo, uint32_t hi, uint32_t* __restrict__ size, uint32_t total,
+                        uint32_t* err) {
+  uint32_t g = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= hi) return;
+  if (!T.leaf[g] && (T.child0[g] >= total || T.child1[g] >= total)) { atomicOr(err, kErrCorrupt); size[g] = 1; return; }
+  size[g] = T.leaf[g] ? 1u : 1u + size[T.child0[g]] + size[T.child1[g]];
+}
+
+__global__ void k_positions(Table T, uint32_t lo, uint32_t hi, const uint32_t* __restrict__ size,
+                            uint32_t* __restrict__ pos, uint32_t total) {
+  uint32_t g = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= hi || T.leaf[g]) return;
+  if (T.child0[g] >= total || T.child1[g] >= total) return;
+  const uint32_t p = pos[g];
+  pos[T.child0[g]] = p + 1;
+  pos[T.child1[g]] = p + 1 + size[T.child0[g]];
+}
+
+__global__ void k_leaf_counts(Table T, uint32_t total, const uint32_t* __restrict__ pos, uint32_t* __restrict__ cnt) {
+  uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g > total) return;
+  if (g == total) { cnt[total] = 0; return; }
+  if (pos[g] >= total) return;
+  cnt[pos[g]] = (T.leaf[g] && T.count[g] >= 2) ? T.count[g] : 0u;
+}
+
+// Final KdAccelNode words (accelerators.h:718-761) and leaf primitive indices.
+__global__ void k_write_nodes(Table T, uint32_t total, const uint32_t* __restrict__ pos,
+                              const uint32_t* __restrict__ off, const uint32_t* __restrict__ pool,
+                              int4* __restrict__ nodes, int32_t* __restrict__ prim_idx, uint32_t n_idx,
+                              uint32_t pool_cap, uint32_t* err) {
+  uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total) return;
+  const uint32_t p = pos[g];
+  if (p >= total) { atomicOr(err, kErrCorrupt); return; }
+  if (T.leaf[g] && (T.pool_off[g] + T.count[g] > pool_cap ||
+                    (T.count[g] >= 2 && off[p] + T.count[g] > n_idx))) {
+    atomicOr(err, kErrCorrupt);
+    return;
+  }
+  if (!T.leaf[g] && T.child1[g] >= total) { atomicOr(err, kErrCorrupt); return; }
+  if (T.leaf[g]) {
+    const uint32_t np = T.count[g];
+    int w0 = 0;
+    if (np == 1) w0 = (int)pool[T.pool_off[g]];
+    else if (np >= 2) {
+      w0 = (int)off[p];
+      for (uint32_t i = 0; i < np; ++i) prim_idx[off[p] + i] = (int)pool[T.pool_off[g] + i];
+    }
+    nodes[p] = make_int4(w0, 3 | (int)(np << 2), (int)np, 0);
+  } else {
+    nodes[p] = make_int4(__float_as_int(T.split[g]), T.axis[g] | (int)(pos[T.child1[g]] << 2), 0, 0);
+  }
+}
+
+// ------------------------------------------------------------- traversal
+
+struct Todo {
+  int node;
+  float tMin, tMax;
+};
+
+template <int KIND, bool ANY, bool REF>
+__global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, const float4* __restrict__ rays,
+                                                  uint32_t n, float4* __restrict__ hits,
+                                                  uint32_t* __restrict__ occ, uint32_t* err) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  bool occluded = false;
+  if (r < n) {
+    float4 ra = __ldg(rays + 2 * (size_t)r), rb = __ldg(rays + 2 * (size_t)r + 1);
+    F3 o = {ra.x, ra.y, ra.z}, d = {rb.x, rb.y, rb.z};
+    const float rtmin = ra.w, rtmax = rb.w;
+    float best = rtmax, bu = 0.f, bv = 0.f;
+    uint32_t bprim = kMiss;
+    F3 inv = {__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)};
+    const float* R = kd.root;
+    float tMin, tMax;
+    bool in;
+    if (REF) {
+      in = box_ref(o, d, R[0], R[3], R[1], R[4], R[2], R[5], tMin, tMax);
+    } else {
+      float tn;
+      in = slab_fast(o, inv, R[0], R[3], R[1], R[4], R[2], R[5], rtmin, best, tn);
+      float tx0 = __fmul_rn(__fsub_rn(R[0], o.x), inv.x), tx1 = __fmul_rn(__fsub_rn(R[3], o.x), inv.x);
+      float ty0 = __fmul_rn(__fsub_rn(R[1], o.y), inv.y), ty1 = __fmul_rn(__fsub_rn(R[4], o.y), inv.y);
+      float tz0 = __fmul_rn(__fsub_rn(R[2], o.z), inv.z), tz1 = __fmul_rn(__fsub_rn(R[5], o.z), inv.z);
+      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best));
+      tMin = tn;
+      tMax = __fmul_rn(tf, kWiden);
+    }
+    if (in) {
+      Todo todo[kStackSize];
+      int tp = 0, node = 0;
+      const float oo[3] = {o.x, o.y, o.z}, dv[3] = {d.x, d.y, d.z}, iv[3] = {inv.x, inv.y, inv.z};
+      uint32_t steps = 0;
+      for (;;) {
+        if (++steps > 2u * n_nodes + 8u) { atomicOr(err, kErrCorrupt); break; }
+        if (!REF && best < tMin) break;
+        const int4 w = __ldg(kd.nodes + node);
+        if ((w.y & 3) != 3) {
+          const int axis = w.y & 3;
+          const float split = __int_as_float(w.x);
+          const float tPlane = __fmul_rn(__fsub_rn(split, oo[axis]), iv[axis]);
+          const bool belowFirst = (oo[axis] < split) || (oo[axis] == split && dv[axis] <= 0.f);
+          const int above = w.y >> 2;
+          const int first = belowFirst ? node + 1 : above, second = belowFirst ? above : node + 1;
+          if (tPlane > tMax || tPlane <= 0.f) {
+            node = first;
+          } else if (tPlane < tMin) {
+            node = second;
+          } else {
+            if (tp >= kStackSize) { atomicOr(err, kErrStackOverflow); break; }
+            todo[tp++] = {second, tPlane, tMax};
+            node = first;
+            tMax = tPlane;
+          }
+          continue;
+        }
+        const int np = w.z;
+        bool done = false;
+        for (int i = 0; i < np; ++i) {
+          const uint32_t id = (uint32_t)(np == 1 ? w.x : __ldg(kd.prim_idx + w.x + i));
+          if (KIND == kTriangles) {
+            const float4* q = kd.prims + 3 * (size_t)id;
+            float t, u, v;
+            if (tri_mt(__ldg(q), __ldg(q + 1), __ldg(q + 2), o, d, rtmin, ANY ? rtmax : best, t, u, v)) {
+              if (ANY) { done = true; break; }
+              best = t; bprim = id; bu = u; bv = v;
+            }
+          } else {
+            const float4 s = __ldg(kd.prims + id);
+            if (ANY || REF) {
+              float t0, t1, t;
+              if (REF ? sphere_ref(s, o, d, t0, t1) : sphere_closest(s, o, d, rtmin, rtmax, false, t)) {
+                if (ANY) { done = true; break; }
+              }
+            }
+            if (!ANY) {
+              float t;
+              if (sphere_closest(s, o, d, rtmin, best, REF, t)) { best = t; bprim = id; bu = bv = 0.f; }
+            }
+          }
+        }
+        if (done) { occluded = true; break; }
+        if (tp > 0) {
+          --tp;
+          node = todo[tp].node;
+          tMin = todo[tp].tMin;
+          tMax = todo[tp].tMax;
+        } else {
+          break;
+        }
+      }
+    }
+    if (!ANY) hits[r] = make_float4(best, __uint_as_float(bprim), bu, bv);
+  }
+  if (ANY) {
+    uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+    uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+  }
+}
+
+template <int KIND, bool ANY>
+void dispatch_kd(int traversal, const KdView& v, uint32_t n_nodes, const float4* rays, uint32_t n, float4* hits,
+                 uint32_t* occ, uint32_t* err, cudaStream_t s) {
+  const unsigned g = (n + 127) / 128;
+  if (traversal == RQ_TRAVERSAL_REFERENCE)
+    k_trace_kd<KIND, ANY, true><<<g, 128, 0, s>>>(v, n_nodes, rays, n, hits, occ, err);
+  else
+    k_trace_kd<KIND, ANY, false><<<g, 128, 0, s>>>(v, n_nodes, rays, n, hits, occ, err);
+}
+
+__global__ void k_box_union(const float* __restrict__ aabb, uint32_t n, int32_t* lohi) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = fminf(lo[a], aabb[6 * (size_t)p + a]);
+      hi[a] = fmaxf(hi[a], aabb[6 * (size_t)p + 3 + a]);
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+      hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(lohi + a, float_to_ordered(lo[a]));
+      atomicMax(lohi + 3 + a, float_to_ordered(hi[a]));
+    }
+}
+
+__global__ void k_iota(uint32_t* v, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+__global__ void k_root_box(const int32_t* lohi, float* box, float* root) {
+  int q = threadIdx.x;
+  if (q < 6) {
+    float v = ordered_to_float(lohi[q]);
+    box[q] = v;
+    root[q] = v;
+  }
+}
+
+// Grow a buffer keeping its first `used` bytes.
+cudaError_t grow_keep(DevBuf& b, size_t bytes, size_t used, cudaStream_t st) {
+  if (bytes <= b.cap && b.p) return cudaSuccess;
+  void* p = nullptr;
+  size_t want = bytes + bytes / 2 + 256;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) return e;
+  if (used && b.p) {
+    e = cudaMemcpyAsync(p, b.p, used, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return e;
+    }
+  }
+  if (b.p) cudaFree(b.p);
+  b.p = p;
+  b.cap = want;
+  return cudaSuccess;
+}
+
+#define KD_TRY(call, what)                                           \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) return BuildResult::cuda_error(e_, what); \
+  } while (0)
+
+// Level node arrays carved from one buffer.
+LevelNodes carve(char* base, uint32_t cap) {
+  LevelNodes L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { char* p = base + o; o += (bytes + 255) & ~size_t(255); return p; };
+  L.box = (float*)take((size_t)cap * 24);
+  L.depth = (int32_t*)take((size_t)cap * 4);
+  L.bad = (int32_t*)take((size_t)cap * 4);
+  L.rs = (uint32_t*)take((size_t)cap * 4);
+  L.rc = (uint32_t*)take((size_t)cap * 4);
+  L.axis0 = (int32_t*)take((size_t)cap * 4);
+  L.eval = (int32_t*)take((size_t)cap * 4);
+  L.retries = (int32_t*)take((size_t)cap * 4);
+  L.best = (unsigned long long*)take((size_t)cap * 8);
+  L.edge_base = (uint32_t*)take((size_t)cap * 4);
+  L.state = (int32_t*)take((size_t)cap * 4);
+  L.best_axis = (int32_t*)take((size_t)cap * 4);
+  L.best_off = (uint32_t*)take((size_t)cap * 4);
+  L.tsplit = (float*)take((size_t)cap * 4);
+  L.pass_found = (int32_t*)take((size_t)cap * 4);
+  return L;
+}
+size_t level_bytes(uint32_t cap) { return (size_t)cap * 100 + 16 * 256; }
+
+Table table_at(char* base, uint32_t cap) {
+  Table T;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { char* p = base + o; o += (bytes + 255) & ~size_t(255); return p; };
+  T.leaf = (int32_t*)take((size_t)cap * 4);
+  T.axis = (int32_t*)take((size_t)cap * 4);
+  T.split = (float*)take((size_t)cap * 4);
+  T.child0 = (uint32_t*)take((size_t)cap * 4);
+  T.child1 = (uint32_t*)take((size_t)cap * 4);
+  T.count = (uint32_t*)take((size_t)cap * 4);
+  T.pool_off = (uint32_t*)take((size_t)cap * 4);
+  return T;
+}
+size_t table_bytes(uint32_t cap) { return (size_t)cap * 28 + 8 * 256; }
+
+int bitlen(uint32_t v) {
+  int b = 0;
+  while (v) { ++b; v >>= 1; }
+  return b;
+}
+
+}  // namespace
+
+void launch_trace_kd(int kind, int traversal, bool any, const KdView& v, const float4* rays, uint32_t n,
+                     float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  const uint32_t nn = v.n_nodes;
+  if (kind == kTriangles) {
+    if (any) dispatch_kd<kTriangles, true>(traversal, v, nn, rays, n, hits, occ, err, s);
+    else dispatch_kd<kTriangles, false>(traversal, v, nn, rays, n, hits, occ, err, s);
+  } else {
+    if (any) dispatch_kd<kSpheres, true>(traversal, v, nn, rays, n, hits, occ, err, s);
+    else dispatch_kd<kSpheres, false>(traversal, v, nn, rays, n, hits, occ, err, s);
+  }
+}
+
+BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a, BuildScratch& sc, uint32_t* err,
+                          cudaStream_t st) {
+  const uint32_t n = s.n;
+  int l2 = 0;
+  for (uint32_t v = n; v > 1; v >>= 1) ++l2;
+  // maxDepth = round(8 + 1.3 * Log2Int(N)) (accelerators.h:957-958)
+  const int depth0 = max_depth_cfg > 0 ? max_depth_cfg : (int)std::round(8 + 1.3f * l2);
+  const size_t payload = s.kind == kTriangles ? 48 : 16;
+  KD_TRY(a.prims.ensure((size_t)n * payload), "KD payload");
+  KD_TRY(a.root.ensure(32), "KD root");
+  // primitive boxes (and payload by id)
+  KD_TRY(sc.m0.ensure((size_t)n * 24), "KD scratch");
+  float* aabb = sc.m0.as<float>();
+  launch_prims_by_id(s.kind, s.verts, s.idx, s.sph, n, a.prims.as<float4>(), aabb, st);
+  KD_TRY(cudaGetLastError(), "KD prims");
+  // root bounds: union of every primitive box
+  KD_TRY(sc.lohi.ensure(64), "KD scratch");
+  int32_t* lohi = sc.lohi.as<int32_t>();
+  launch_init_bounds(lohi, st);
+  count_launch();
+  k_box_union<<<std::min<uint32_t>(grid(n), 1024u), kThreads, 0, st>>>(aabb, n, lohi);
+
+  // refs of the current level, double buffered: prim, node
+  uint32_t R = n, M = 1;
+  KD_TRY(sc.m1.ensure((size_t)n * 8 * 2), "KD scratch");
+  uint32_t* ref_prim = sc.m1.as<uint32_t>();
+  uint32_t* ref_node = ref_prim + (size_t)n;
+  count_launch();
+  k_iota<<<grid(n), kThreads, 0, st>>>(ref_prim, n);
+  KD_TRY(cudaMemsetAsync(ref_node, 0, (size_t)n * 4, st), "KD init");
+  // level 0 node
+  KD_TRY(sc.m3.ensure(level_bytes(1)), "KD scratch");
+  LevelNodes L = carve(sc.m3.as<char>(), 1);
+  {
+    const int32_t h_depth = depth0, h_bad = 0;
+    const uint32_t h_rs = 0, h_rc = n;
+    KD_TRY(cudaMemcpyAsync(L.depth, &h_depth, 4, cudaMemcpyHostToDevice, st), "KD init");
+    KD_TRY(cudaMemcpyAsync(L.bad, &h_bad, 4, cudaMemcpyHostToDevice, st), "KD init");
+    KD_TRY(cudaMemcpyAsync(L.rs, &h_rs, 4, cudaMemcpyHostToDevice, st), "KD init");
+    KD_TRY(cudaMemcpyAsync(L.rc, &h_rc, 4, cudaMemcpyHostToDevice, st), "KD init");
+    count_launch();
+    k_root_box<<<1, 32, 0, st>>>(lohi, L.box, a.root.as<float>());
+  }
+  DevBuf& tabbuf = sc.m5;
+  DevBuf& poolbuf = sc.m6;
+  uint32_t table_cap = 0, total = 0, pool_used = 0;
+  std::vector<uint32_t> level_lo;
+  for (int level = 0; M > 0; ++level) {
+    if (level > 200) return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "KD tree deeper than 200 levels");
+    level_lo.push_back(total);
+    // table capacity
+    if (total + M > table_cap) {
+      uint32_t ncap = (total + M) * 2 + 1024;
+      DevBuf nb;
+      KD_TRY(nb.ensure(table_bytes(ncap)), "KD table");
+      if (table_cap) {
+        Table Told = table_at(tabbuf.as<char>(), table_cap), Tnew = table_at(nb.as<char>(), ncap);
+        const size_t bytes = (size_t)total * 4;
+        KD_TRY(cudaMemcpyAsync(Tnew.leaf, Told.leaf, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaMemcpyAsync(Tnew.axis, Told.axis, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaMemcpyAsync(Tnew.split, Told.split, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaMemcpyAsync(Tnew.child0, Told.child0, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaMemcpyAsync(Tnew.child1, Told.child1, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaMemcpyAsync(Tnew.count, Told.count, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaMemcpyAsync(Tnew.pool_off, Told.pool_off, bytes, cudaMemcpyDeviceToDevice, st), "KD table");
+        KD_TRY(cudaStreamSynchronize(st), "KD table");
+      }
+      tabbuf.release();
+      tabbuf = nb;
+      nb.p = nullptr;
+      nb.cap = 0;
+      table_cap = ncap;
+    }
+    Table T = table_at(tabbuf.as<char>(), table_cap);
+    // per-ref scratch: flags / scans (R + 1 each)
+    KD_TRY(sc.m2.ensure(((size_t)R + 1) * 4 * 6 + scan_tmp_words(2ull * R + 2) * 4 + 64), "KD scratch");
+    uint32_t* flag = sc.m2.as<uint32_t>();
+    uint32_t* epos = flag + (R + 1);
+    uint32_t* below = epos + (R + 1);
+    uint32_t* above = below + (R + 1);
+    uint32_t* sB = above + (R + 1);
+    uint32_t* sA = sB + (R + 1);
+    uint32_t* tmp = sA + (R + 1);
+    uint32_t* tot = tmp + scan_tmp_words(2ull * R + 2) + 4;
+    KD_TRY(cudaMemsetAsync(below, 0, ((size_t)R + 1) * 8, st), "KD flags");  // below + above
+    count_launch();
+    k_node_init<<<grid(M), kThreads, 0, st>>>(L, M);
+    // edge arrays: keys (u64) x2, vals x2, start/end flags and scans
+    for (int pass = 0; pass < 3; ++pass) {
+      count_launch();
+      k_pending_flags<<<grid(R + 1), kThreads, 0, st>>>(ref_node, R, L.eval, flag);
+      launch_scan_excl(flag, epos, (uint64_t)R + 1, tmp, tot, st);
+      uint32_t pend = 0;
+      KD_TRY(cudaMemcpyAsync(&pend, tot, 4, cudaMemcpyDeviceToHost, st), "KD pass");
+      KD_TRY(cudaStreamSynchronize(st), "KD pass");
+      if (pend == 0) break;
+      const uint32_t E = 2 * pend;
+      const int passes = (33 + bitlen(M - 1) + 7) / 8;
+      KD_TRY(sc.keys.ensure((size_t)E * 8 * 2 + 64), "KD edges");
+      KD_TRY(sc.vals.ensure((size_t)E * 4 * 2 + 64), "KD edges");
+      KD_TRY(sc.m4.ensure(((size_t)E + 1) * 16 + scan_tmp_words((uint64_t)E + 1) * 4 +
+                          (2048 + 16 + sort_status_words64(E, passes)) * 4 + 256), "KD edges");
+      unsigned long long* keys = sc.keys.as<unsigned long long>();
+      unsigned long long* keys_alt = keys + E;
+      uint32_t* vals = sc.vals.as<uint32_t>();
+      uint32_t* vals_alt = vals + E;
+      uint32_t* fs = sc.m4.as<uint32_t>();
+      uint32_t* fe = fs + (E + 1);
+      uint32_t* ss = fe + (E + 1);
+      uint32_t* se = ss + (E + 1);
+      uint32_t* etmp = se + (E + 1);
+      uint32_t* zero = etmp + scan_tmp_words((uint64_t)E + 1) + 4;
+      const size_t zwords = 2048 + 16 + sort_status_words64(E, passes);
+      count_launch();
+      k_edges<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, flag, epos, L, aabb, keys, vals, E, err);
+      KD_TRY(cudaMemsetAsync(zero, 0, zwords * 4, st), "KD sort");
+      launch_histogram64(reinterpret_cast<uint64_t*>(keys), E, passes, zero, st);
+      launch_onesweep64(reinterpret_cast<uint64_t*>(keys), vals, E, passes, reinterpret_cast<uint64_t*>(keys_alt),
+                        vals_alt, zero, zero + 2048 + 16, zero + 2048, err, st);
+      count_launch(3);
+      k_edge_flags<<<grid((uint64_t)E + 1), kThreads, 0, st>>>(keys, E, fs, fe);
+      launch_scan_excl(fs, ss, (uint64_t)E + 1, etmp, nullptr, st);
+      launch_scan_excl(fe, se, (uint64_t)E + 1, etmp, nullptr, st);
+      k_cost<<<grid(E), kThreads, 0, st>>>(keys, E, ss, se, L);
+      k_pass_decide<<<grid(M), kThreads, 0, st>>>(L, M, pass);
+      count_launch();
+      k_classify<<<grid(E), kThreads, 0, st>>>(keys, vals, E, L, pass, below, above, R, err);
+      KD_TRY(cudaGetLastError(), "KD pass");
+    }
+    // interior ranks and leaf pool offsets
+    KD_TRY(sc.m7.ensure(((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 4 + 64), "KD scratch");
+    uint32_t* iflag = sc.m7.as<uint32_t>();
+    uint32_t* irank = iflag + (M + 1);
+    uint32_t* lcnt = irank + (M + 1);
+    uint32_t* lofs = lcnt + (M + 1);
+    uint32_t* mtmp = lofs + (M + 1);
+    uint32_t* mtot = mtmp + scan_tmp_words((uint64_t)M + 1) + 4;
+    count_launch(2);
+    k_flag_of_state<<<grid(M + 1), kThreads, 0, st>>>(L, M, 2, iflag, 0);
+    launch_scan_excl(iflag, irank, (uint64_t)M + 1, mtmp, mtot, st);
+    uint32_t interiors = 0;
+    KD_TRY(cudaMemcpyAsync(&interiors, mtot, 4, cudaMemcpyDeviceToHost, st), "KD level");
+    k_flag_of_state<<<grid(M + 1), kThreads, 0, st>>>(L, M, 1, lcnt, 1);
+    launch_scan_excl(lcnt, lofs, (uint64_t)M + 1, mtmp, mtot, st);
+    uint32_t leaf_refs = 0;
+    KD_TRY(cudaMemcpyAsync(&leaf_refs, mtot, 4, cudaMemcpyDeviceToHost, st), "KD level");
+    launch_scan_excl(below, sB, (uint64_t)R + 1, tmp, nullptr, st);
+    launch_scan_excl(above, sA, (uint64_t)R + 1, tmp, nullptr, st);
+    KD_TRY(cudaStreamSynchronize(st), "KD level");
+    // next level nodes and child ref counts
+    const uint32_t M2 = 2 * interiors;
+    DevBuf& nextbuf = (level & 1) ? sc.m3 : sc.keys_alt;  // alternate level buffers
+    DevBuf& curbuf = (level & 1) ? sc.keys_alt : sc.m3;
+    (void)curbuf;
+    KD_TRY(nextbuf.ensure(level_bytes(M2 ? M2 : 1) + ((size_t)M2 + 1) * 8 + scan_tmp_words((uint64_t)M2 + 1) * 4 + 64),
+           "KD scratch");
+    LevelNodes N = carve(nextbuf.as<char>(), M2 ? M2 : 1);
+    uint32_t* ccnt = reinterpret_cast<uint32_t*>(nextbuf.as<char>() + level_bytes(M2 ? M2 : 1));
+    uint32_t* coff = ccnt + (M2 + 1);
+    uint32_t* ctmp = coff + (M2 + 1);
+    // leaf pool growth
+    KD_TRY(grow_keep(poolbuf, ((size_t)pool_used + leaf_refs + 1) * 4, (size_t)pool_used * 4, st), "KD pool");
+    // lofs holds offsets relative to this level; shift by pool_used in the kernels
+    count_launch();
+    k_spawn<<<grid(M), kThreads, 0, st>>>(L, M, irank, sB, sA, lofs, pool_used, total, total + M, T, N, ccnt, M2,
+                                          err);
+    KD_TRY(cudaGetLastError(), "KD spawn");
+    uint32_t R2 = 0;
+    if (M2) {
+      KD_TRY(cudaMemsetAsync(ccnt + M2, 0, 4, st), "KD spawn");
+      launch_scan_excl(ccnt, coff, (uint64_t)M2 + 1, ctmp, mtot, st);
+      count_launch();
+      k_set_ref_starts<<<grid(M2), kThreads, 0, st>>>(N, M2, ccnt, coff);
+      KD_TRY(cudaMemcpyAsync(&R2, mtot, 4, cudaMemcpyDeviceToHost, st), "KD spawn");
+      KD_TRY(cudaStreamSynchronize(st), "KD spawn");
+    }
+    // refs of the next level (separate buffer), leaf refs to the pool
+    KD_TRY(sc.kd_refs.ensure(((size_t)R2 + 1) * 8), "KD refs");
+    uint32_t* out_prim = sc.kd_refs.as<uint32_t>();
+    uint32_t* out_node = out_prim + (R2 + 1);
+    count_launch();
+    k_emit_refs<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, L, irank, below, above, sB, sA, N, out_prim,
+                                              out_node, lofs, pool_used, poolbuf.as<uint32_t>(), R2,
+                                              (uint32_t)(poolbuf.cap / 4), err);
+    KD_TRY(cudaGetLastError(), "KD emit");
+    pool_used += leaf_refs;
+    total += M;
+    // swap ref buffers
+    KD_TRY(cudaStreamSynchronize(st), "KD level");
+    std::swap(sc.m1, sc.kd_refs);  // the children's refs become the current refs
+    ref_prim = sc.m1.as<uint32_t>();
+    ref_node = ref_prim + (R2 + 1);
+    R = R2;
+    M = M2;
+    L = N;
+  }
+  // depth-first layout
+  level_lo.push_back(total);
+  Table T = table_at(tabbuf.as<char>(), table_cap);
+  // size, pos, cnt, off: four arrays of total + 2 words
+  KD_TRY(sc.m7.ensure(((size_t)total + 2) * 16 + scan_tmp_words((uint64_t)total + 2) * 4 + 64), "KD layout");
+  uint32_t* size = sc.m7.as<uint32_t>();
+  uint32_t* pos = size + (total + 1);
+  uint32_t* cnt = pos + (total + 1);
+  uint32_t* off = cnt + (total + 1);
+  uint32_t* ltmp = off + (total + 2);
+  uint32_t* ltot = ltmp + scan_tmp_words((uint64_t)total + 2) + 4;
+  for (int lv = (int)level_lo.size() - 2; lv >= 0; --lv) {
+    count_launch();
+    k_sizes<<<grid(level_lo[lv + 1] - level_lo[lv]), kThreads, 0, st>>>(T, level_lo[lv], level_lo[lv + 1], size,
+                                                                         total, err);
+  }
+  KD_TRY(cudaMemsetAsync(pos, 0, 4, st), "KD layout");
+  for (size_t lv = 0; lv + 1 < level_lo.size(); ++lv) {
+    count_launch();
+    k_positions<<<grid(level_lo[lv + 1] - level_lo[lv]), kThreads, 0, st>>>(T, level_lo[lv], level_lo[lv + 1], size,
+                                                                             pos, total);
+  }
+  count_launch();
+  k_leaf_counts<<<grid((uint64_t)total + 1), kThreads, 0, st>>>(T, total, pos, cnt);
+  launch_scan_excl(cnt, off, (uint64_t)total + 1, ltmp, ltot, st);
+  uint32_t n_idx = 0;
+  KD_TRY(cudaMemcpyAsync(&n_idx, ltot, 4, cudaMemcpyDeviceToHost, st), "KD layout");
+  KD_TRY(cudaStreamSynchronize(st), "KD layout");
+  KD_TRY(a.kd_nodes.ensure((size_t)total * 16), "KD nodes");
+  KD_TRY(a.kd_idx.ensure((size_t)(n_idx ? n_idx : 1) * 4), "KD indices");
+  count_launch();
+  k_write_nodes<<<grid(total), kThreads, 0, st>>>(T, total, pos, off, poolbuf.as<uint32_t>(), a.kd_nodes.as<int4>(),
+                                                  a.kd_idx.as<int32_t>(), n_idx, (uint32_t)(poolbuf.cap / 4), err);
+  KD_TRY(cudaGetLastError(), "KD write");
+  a.n_nodes = total;
+  a.n_slots = n_idx;
+  a.max_depth = (uint32_t)depth0;
+  return {};
+}
 
 }  // namespace rq

@@ -19,22 +19,21 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 15;
-constexpr int kTile = kThreads * kItems;  // 3840
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kFlagAbort = 3u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
 constexpr uint32_t kSpinLimit = 1u << 20;  // polls of one predecessor word before giving up
 
-__global__ void __launch_bounds__(kThreads) k_histogram(const uint32_t* __restrict__ keys, uint32_t n,
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_histogram(const K* __restrict__ keys, uint32_t n,
                                                         int passes, uint32_t* __restrict__ hist) {
-  __shared__ uint32_t sh[4][256];
-  for (int i = threadIdx.x; i < 1024; i += blockDim.x) (&sh[0][0])[i] = 0;
+  __shared__ uint32_t sh[sizeof(K)][256];
+  for (int i = threadIdx.x; i < (int)sizeof(K) * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
   __syncthreads();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    uint32_t k = __ldg(keys + i);
-    for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & 255u], 1u);
+    K k = __ldg(keys + i);
+    for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(uint32_t)(k >> (8 * p)) & 255u], 1u);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
@@ -70,26 +69,30 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
   return r;
 }
 
+template <typename K, int kItems>
 struct __align__(16) OnesweepSmem {
+  static constexpr int kTile = kThreads * kItems;
+  K keys[kTile];
   uint32_t warp_hist[kWarps][256];
   uint32_t digit_start[256];
   uint32_t global_base[256];
   uint32_t scan_tmp[kWarps];
-  uint32_t keys[kTile];
   uint32_t vals[kTile];
   uint32_t tile;
   int abort;
 };
 
-__global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restrict__ kin,
+template <typename K, int kItems>
+__global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin,
-                                                       uint32_t* __restrict__ kout,
+                                                       K* __restrict__ kout,
                                                        uint32_t* __restrict__ vout, uint32_t n,
                                                        int shift, const uint32_t* __restrict__ hist,
                                                        uint32_t* status, uint32_t* tile_counter,
                                                        uint32_t* err) {
+  constexpr int kTile = kThreads * kItems;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  OnesweepSmem& sm = *reinterpret_cast<OnesweepSmem*>(smem_raw);
+  OnesweepSmem<K, kItems>& sm = *reinterpret_cast<OnesweepSmem<K, kItems>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
@@ -102,12 +105,13 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   const uint64_t base = (uint64_t)tile * kTile;
 
   // Warp-striped load: element order (warp, item, lane) = input order.
-  uint32_t keys[kItems], vals[kItems], rank[kItems];
+  K keys[kItems];
+  uint32_t vals[kItems], rank[kItems];
 #pragma unroll
   for (int k = 0; k < kItems; ++k) {
     uint64_t i = base + (uint64_t)warp * (32 * kItems) + (uint64_t)k * 32 + lane;
     bool ok = i < n;
-    keys[k] = ok ? __ldg(kin + i) : 0u;
+    keys[k] = ok ? __ldg(kin + i) : K(0);
     vals[k] = ok ? __ldg(vin + i) : 0u;
   }
 
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   for (int k = 0; k < kItems; ++k) {
     uint64_t i = base + (uint64_t)warp * (32 * kItems) + (uint64_t)k * 32 + lane;
     bool ok = i < n;
-    uint32_t d = ok ? ((keys[k] >> shift) & 255u) : 256u;
+    uint32_t d = ok ? ((uint32_t)(keys[k] >> shift) & 255u) : 256u;
     uint32_t peers = __match_any_sync(0xffffffffu, d);
     int leader = __ffs(peers) - 1;
     uint32_t below = __popc(peers & ((1u << lane) - 1u));
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   for (int k = 0; k < kItems; ++k) {
     uint64_t i = base + (uint64_t)warp * (32 * kItems) + (uint64_t)k * 32 + lane;
     if (i < n) {
-      uint32_t d = (keys[k] >> shift) & 255u;
+      uint32_t d = (uint32_t)(keys[k] >> shift) & 255u;
       uint32_t pos = sm.digit_start[d] + sm.warp_hist[warp][d] + rank[k];
       sm.keys[pos] = keys[k];
       sm.vals[pos] = vals[k];
@@ -190,8 +194,8 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
 
   const uint32_t valid = (uint64_t)n - base < (uint64_t)kTile ? (uint32_t)(n - base) : (uint32_t)kTile;
   for (uint32_t i = tid; i < valid; i += kThreads) {
-    uint32_t key = sm.keys[i];
-    uint32_t d = (key >> shift) & 255u;
+    K key = sm.keys[i];
+    uint32_t d = (uint32_t)(key >> shift) & 255u;
     uint32_t gpos = sm.global_base[d] + (i - sm.digit_start[d]);
     if (gpos < n) {
       kout[gpos] = key;
@@ -200,43 +204,75 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restric
   }
 }
 
+constexpr int kItems32 = 15;  // 3,840 keys per tile
+constexpr int kItems64 = 10;  // 2,560 keys per tile (64-bit keys)
+
+template <typename K, int ITEMS>
+void onesweep_passes(K* keys, uint32_t* vals, uint32_t n, int passes, K* keys_alt, uint32_t* vals_alt,
+                     const uint32_t* hist, uint32_t* status, uint32_t* counters, uint32_t* err, cudaStream_t s) {
+  using Smem = OnesweepSmem<K, ITEMS>;
+  static_assert(sizeof(Smem) <= 48 * 1024, "onesweep shared memory over the default limit");
+  const uint32_t tile = kThreads * ITEMS;
+  const uint32_t tiles = (n + tile - 1) / tile;
+  K* src_k = keys;
+  uint32_t* src_v = vals;
+  K* dst_k = keys_alt;
+  uint32_t* dst_v = vals_alt;
+  for (int p = 0; p < passes; ++p) {
+    count_launch();
+    k_onesweep<K, ITEMS><<<tiles, kThreads, sizeof(Smem), s>>>(src_k, src_v, dst_k, dst_v, n, 8 * p,
+                                                               hist + 256 * p, status + (size_t)p * tiles * 256,
+                                                               counters + p, err);
+    K* tk = src_k; src_k = dst_k; dst_k = tk;
+    uint32_t* tv = src_v; src_v = dst_v; dst_v = tv;
+  }
+  if (src_k != keys) {
+    cudaMemcpyAsync(keys, src_k, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(vals, src_v, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
+  }
+}
+
+template <typename K>
+void histogram(const K* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
+  if (n == 0) return;
+  uint32_t g = (n + kThreads * 8 - 1) / (kThreads * 8);
+  if (g > 2048) g = 2048;
+  count_launch();
+  k_histogram<K><<<g, kThreads, 0, s>>>(keys, n, passes, hist);
+}
+
 }  // namespace
 
-uint32_t sort_tiles(uint32_t n) { return (n + kTile - 1) / kTile; }
+uint32_t sort_tiles(uint32_t n) { return (n + kThreads * kItems32 - 1) / (kThreads * kItems32); }
 
 size_t sort_status_words(uint32_t n, int passes) {
   return (size_t)passes * sort_tiles(n) * 256;
 }
 
 void launch_histogram(const uint32_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
-  if (n == 0) return;
-  uint32_t g = (n + kThreads * 8 - 1) / (kThreads * 8);
-  if (g > 2048) g = 2048;
-  count_launch();
-  k_histogram<<<g, kThreads, 0, s>>>(keys, n, passes, hist);
+  histogram<uint32_t>(keys, n, passes, hist, s);
 }
 
 void launch_onesweep(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
                      uint32_t* err, cudaStream_t s) {
   if (n <= 1) return;
-  const size_t smem = sizeof(OnesweepSmem);  // ~40 KB: below the 48 KB default limit
-  static_assert(sizeof(OnesweepSmem) <= 48 * 1024, "onesweep shared memory over the default limit");
-  const uint32_t tiles = sort_tiles(n);
-  uint32_t* src_k = keys;
-  uint32_t* src_v = vals;
-  uint32_t* dst_k = sc.keys_alt;
-  uint32_t* dst_v = sc.vals_alt;
-  for (int p = 0; p < passes; ++p) {
-    count_launch();
-    k_onesweep<<<tiles, kThreads, smem, s>>>(src_k, src_v, dst_k, dst_v, n, 8 * p, sc.hist + 256 * p,
-                                             sc.status + (size_t)p * tiles * 256, sc.counters + p, err);
-    uint32_t* tk = src_k; src_k = dst_k; dst_k = tk;
-    uint32_t* tv = src_v; src_v = dst_v; dst_v = tv;
-  }
-  if (src_k != keys) {
-    cudaMemcpyAsync(keys, src_k, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(vals, src_v, (size_t)n * 4, cudaMemcpyDeviceToDevice, s);
-  }
+  onesweep_passes<uint32_t, kItems32>(keys, vals, n, passes, sc.keys_alt, sc.vals_alt, sc.hist, sc.status,
+                                      sc.counters, err, s);
+}
+
+size_t sort_status_words64(uint32_t n, int passes) {
+  return (size_t)passes * ((n + kThreads * kItems64 - 1) / (kThreads * kItems64)) * 256;
+}
+
+void launch_histogram64(const uint64_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s) {
+  histogram<uint64_t>(keys, n, passes, hist, s);
+}
+
+void launch_onesweep64(uint64_t* keys, uint32_t* vals, uint32_t n, int passes, uint64_t* keys_alt,
+                       uint32_t* vals_alt, const uint32_t* hist, uint32_t* status, uint32_t* counters,
+                       uint32_t* err, cudaStream_t s) {
+  if (n <= 1) return;
+  onesweep_passes<uint64_t, kItems64>(keys, vals, n, passes, keys_alt, vals_alt, hist, status, counters, err, s);
 }
 
 }  // namespace rq

@@ -57,6 +57,14 @@ void launch_histogram(const uint32_t* keys, uint32_t n, int passes, uint32_t* hi
 void launch_onesweep(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
                      uint32_t* err, cudaStream_t s);
 
+// 64-bit keys, 32-bit values (tiles of 2,560 keys).  hist: 256 words per pass
+// (up to 8 passes); status: sort_status_words64 words; counters: one per pass.
+size_t sort_status_words64(uint32_t n, int passes);
+void launch_histogram64(const uint64_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
+void launch_onesweep64(uint64_t* keys, uint32_t* vals, uint32_t n, int passes, uint64_t* keys_alt,
+                       uint32_t* vals_alt, const uint32_t* hist, uint32_t* status, uint32_t* counters,
+                       uint32_t* err, cudaStream_t s);
+
 // --------------------------------------------------------- Morton codes
 void launch_init_bounds(int32_t* lohi, cudaStream_t s);
 void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t* lohi,
@@ -116,6 +124,7 @@ struct KdView {
   const int32_t* prim_idx;
   const float4* prims;    // primitive-id order
   const float* root;      // 6 floats
+  uint32_t n_nodes;
 };
 void launch_trace_kd(int kind, int traversal, bool any, const KdView& v, const float4* rays,
                      uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s);
