@@ -15,6 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librq.so")
+DRIVER = os.path.join(HERE, "rq_render")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Exact-arithmetic parity relies on explicit __f*_rn intrinsics; -fmad=false
 # additionally keeps nvcc from contracting any remaining a*b+c.
@@ -35,11 +36,14 @@ def sources():
 
 def _newest_input():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "rq.h")]
+    files += [os.path.join(HERE, "host", f) for f in os.listdir(os.path.join(HERE, "host"))]
     return max(os.path.getmtime(f) for f in files)
 
 
 def build(force=False, verbose=False):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_input():
+        if not os.path.exists(DRIVER):
+            build_driver()
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     cc = nvcc()
@@ -64,7 +68,20 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+def build_driver():
+    """The C++ host program over the C ABI (host/rq_render_main.cpp)."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(HERE, "host"),
+           os.path.join(HERE, "host", "rq_render_main.cpp"), "-L", HERE, "-lrq", "-Wl,-rpath,$ORIGIN",
+           "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":
