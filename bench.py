@@ -100,7 +100,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -194,15 +194,46 @@ def run_ours(args):
 
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
+    # Ray reordering per ray class, chosen by timing both settings (results are
+    # identical either way; only the speed differs).
+    sort_choice = {"primary": 0, "secondary": 0, "shadow": 0}
+
+    def trace_class(name, marks=None):
+        eng.configure(ray_sort=sort_choice[name])
+        if name == "primary":
+            eng.trace_closest(acc, d_prim, d_hits_p)
+        elif name == "secondary":
+            eng.trace_closest(acc, d_sec, d_hits_s)
+        else:
+            eng.trace_any(acc, d_sh, d_bits)
+
+    for name in sort_choice:
+        best = None
+        for opt in (rq.RAY_SORT_NONE, rq.RAY_SORT_OCTANT_MORTON):
+            sort_choice[name] = opt
+            times = []
+            for _ in range(3):
+                a0, a1 = ev(), ev()
+                a0.record(stream)
+                trace_class(name)
+                a1.record(stream)
+                torch.cuda.synchronize(dev)
+                times.append(a0.elapsed_time(a1))
+            t = min(times)
+            if best is None or t < best[0]:
+                best = (t, opt)
+        sort_choice[name] = best[1]
+    log(f"[bench] ray_sort per class: {sort_choice}")
+
     def step(marks=None):
         if marks: marks[0].record(stream)
         acc.rebuild()
         if marks: marks[1].record(stream)
-        eng.trace_closest(acc, d_prim, d_hits_p)
+        trace_class("primary")
         if marks: marks[2].record(stream)
-        eng.trace_closest(acc, d_sec, d_hits_s)
+        trace_class("secondary")
         if marks: marks[3].record(stream)
-        eng.trace_any(acc, d_sh, d_bits)
+        trace_class("shadow")
         if marks: marks[4].record(stream)
 
     for _ in range(args.warmup):
@@ -255,6 +286,34 @@ def run_ours(args):
                                            * (RAY_BYTES + HIT_BYTES)) / (kern[dom] * 1e-3) / 1e9) / peak, 4)
                 if dom != "build" else None}
 
+    # The same rays through the other builders of the dataStructure switch.
+    structures = {"LBVH": {"build_ms": round(build_ms, 4), "trace_ms": round(prim_ms + sec_ms + sh_ms, 4),
+                           "grays_s": round(total_rays / ((prim_ms + sec_ms + sh_ms) * 1e-3) / 1e9, 4)}}
+    if not args.skip_structures:
+        for name in ("BVH", "KDTREE"):
+            other = eng.build(scene, name)
+            bms, tms = [], []
+            for k in range(3):
+                m = [ev() for _ in range(3)]
+                flush.zero_()
+                m[0].record(stream)
+                other.rebuild()
+                m[1].record(stream)
+                eng.trace_closest(other, d_prim, d_hits_p)
+                eng.trace_closest(other, d_sec, d_hits_s)
+                eng.trace_any(other, d_sh, d_bits)
+                m[2].record(stream)
+                torch.cuda.synchronize(dev)
+                if k:
+                    bms.append(m[0].elapsed_time(m[1]))
+                    tms.append(m[1].elapsed_time(m[2]))
+            eng.synchronize()
+            inf = other.info()
+            structures[name] = {"build_ms": round(float(np.mean(bms)), 3), "trace_ms": round(float(np.mean(tms)), 4),
+                                "grays_s": round(total_rays / (float(np.mean(tms)) * 1e-3) / 1e9, 4),
+                                "nodes": int(inf.n_nodes)}
+            other.close()
+
     e2e = None
     if rank == 0 and not args.skip_e2e:
         e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args)
@@ -271,7 +330,8 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "dataStructure": "LBVH", "triangles": n_tri, "primary_rays": n_p,
                        "secondary_rays": n_s, "shadow_rays": n_sh, "seed": SEED,
                        "l2": "flushed before every timed step (256 MB write); rays exceed L2",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                       "ray_sort": sort_choice},
             "lbvh_build_mtri_s": round(n_tri / (build_ms * 1e-3) / 1e6, 2),
             "closest_grays_s": round((n_p + n_s) / ((prim_ms + sec_ms) * 1e-3) / 1e9, 4),
             "any_grays_s": round(n_sh / (sh_ms * 1e-3) / 1e9, 4),
@@ -284,6 +344,7 @@ def run_ours(args):
             "build_roofline": {"achieved": round(build_bytes / (build_ms * 1e-3) / 1e9, 1), "peak": peak,
                                "unit": "GB/s", "bytes_per_tri": build_bytes_per_tri(),
                                "frac": round(build_bytes / (build_ms * 1e-3) / 1e9 / peak, 4)},
+            "structures": structures,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),
         }
         print(json.dumps(out), flush=True)
@@ -456,13 +517,14 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--small", action="store_true", help="960x540x4 rays (profiling case)")
+    ap.add_argument("--skip-structures", action="store_true", help="skip the BVH / KDTREE comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

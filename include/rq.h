@@ -77,8 +77,17 @@ typedef struct rq_settings_t {
   int32_t traversal;          /* rq_traversal_t, RQ_TRAVERSAL_FAST */
   int32_t morton;             /* rq_morton_t, RQ_MORTON_SCENE_BOUNDS */
   int32_t kd_max_depth;       /* <= 0: round(8 + 1.3 log2 N) as the reference (accelerators.h:958) */
-  int32_t reserved[5];
+  int32_t ray_sort;           /* rq_ray_sort_t: reorder large FAST batches for coherence */
+  int32_t reserved[4];
 } rq_settings_t;
+
+/* Ray reordering before FAST BVH2 traversal of batches of at least 65,536
+ * rays.  Results are written in the caller's order either way and do not
+ * change; only the speed does. */
+typedef enum rq_ray_sort_t {
+  RQ_RAY_SORT_NONE = 0,
+  RQ_RAY_SORT_OCTANT_MORTON = 1 /* direction octant, then 27-bit Morton code of the origin */
+} rq_ray_sort_t;
 
 /* How rays meet boxes and primitives. */
 typedef enum rq_traversal_t {

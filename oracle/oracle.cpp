@@ -168,19 +168,44 @@ inline bool box_ref(V3 o, V3 d, const float* lo, const float* hi, float& tMin, f
   return true;
 }
 
-// Engine slab test: reciprocal direction, (b - o) * inv with no fused
-// multiply-add, NaN-ignoring fminf/fmaxf, interval clipped to [tmin, tfar]
-// and the far end widened by 1 + 2*gamma(3) (Ize 2013) so that a box is never
-// rejected because of rounding.  The engine's kernels perform exactly these
-// operations in this order.
-inline bool box_fast(V3 o, V3 inv, float lx, float hx, float ly, float hy, float lz, float hz,
+// Engine slab test.  Per ray: inv = 1/d, noi = -(o * inv) and eps = 2^-21 *
+// the largest finite |o * inv|.  Per box: plane distances fmaf(b, inv, noi)
+// (one correctly rounded fused multiply-add, as the engine's kernels do),
+// NaN-ignoring fminf/fmaxf, interval clipped to [tmin, tfar], far end widened
+// by the relative 1 + 2*gamma(3) (Ize 2013) and the absolute eps, so that no
+// box the ray truly meets is rejected because of rounding.  The engine's
+// kernels perform exactly these operations in this order.
+struct SlabRay {
+  V3 inv, noi;
+  float eps;
+};
+inline SlabRay slab_ray(V3 o, V3 d) {
+  SlabRay s;
+  s.inv = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+  float ox = o.x * s.inv.x, oy = o.y * s.inv.y, oz = o.z * s.inv.z;
+  s.noi = {-ox, -oy, -oz};
+  float m = 0.f;
+  if (std::fabs(ox) <= FLT_MAX) m = fmaxf(m, std::fabs(ox));
+  if (std::fabs(oy) <= FLT_MAX) m = fmaxf(m, std::fabs(oy));
+  if (std::fabs(oz) <= FLT_MAX) m = fmaxf(m, std::fabs(oz));
+  s.eps = m * 0x1p-21f;
+  return s;
+}
+inline float slab_exit(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                       float tfar_in) {
+  float tx0 = std::fmaf(lx, r.inv.x, r.noi.x), tx1 = std::fmaf(hx, r.inv.x, r.noi.x);
+  float ty0 = std::fmaf(ly, r.inv.y, r.noi.y), ty1 = std::fmaf(hy, r.inv.y, r.noi.y);
+  float tz0 = std::fmaf(lz, r.inv.z, r.noi.z), tz1 = std::fmaf(hz, r.inv.z, r.noi.z);
+  return fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar_in));
+}
+inline bool box_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
                      float tmin, float tfar_in, float& tnear_out) {
-  float tx0 = (lx - o.x) * inv.x, tx1 = (hx - o.x) * inv.x;
-  float ty0 = (ly - o.y) * inv.y, ty1 = (hy - o.y) * inv.y;
-  float tz0 = (lz - o.z) * inv.z, tz1 = (hz - o.z) * inv.z;
+  float tx0 = std::fmaf(lx, r.inv.x, r.noi.x), tx1 = std::fmaf(hx, r.inv.x, r.noi.x);
+  float ty0 = std::fmaf(ly, r.inv.y, r.noi.y), ty1 = std::fmaf(hy, r.inv.y, r.noi.y);
+  float tz0 = std::fmaf(lz, r.inv.z, r.noi.z), tz1 = std::fmaf(hz, r.inv.z, r.noi.z);
   float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
   float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar_in));
-  tf = tf * kWiden;
+  tf = std::fmaf(tf, kWiden, r.eps);
   tnear_out = tn;
   return tn <= tf;
 }
@@ -217,7 +242,7 @@ void trace_one_bvh2(int kind, int mode, int query, const float* nodes, uint32_t 
   hit.prim = kMiss;
   hit.u = hit.v = 0.f;
   occ = 0;
-  V3 inv = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+  const SlabRay sr = slab_ray(o, d);
   // Root box.
   {
     bool ok;
@@ -226,7 +251,7 @@ void trace_one_bvh2(int kind, int mode, int query, const float* nodes, uint32_t 
       ok = box_ref(o, d, rb, rb + 3, a, b);
     } else {
       float tn;
-      ok = box_fast(o, inv, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, best, tn);
+      ok = box_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, best, tn);
     }
     if (!ok) return;
   }
@@ -250,8 +275,8 @@ void trace_one_bvh2(int kind, int mode, int query, const float* nodes, uint32_t 
         if (hr) stack.push_back({ch[1], ch[3]});
         if (hl) { cur = {ch[0], ch[2]}; continue; }
       } else {
-        hl = box_fast(o, inv, n[0], n[1], n[2], n[3], n[8], n[9], ray.tmin, best, tl);
-        hr = box_fast(o, inv, n[4], n[5], n[6], n[7], n[10], n[11], ray.tmin, best, tr);
+        hl = box_fast(sr, n[0], n[1], n[2], n[3], n[8], n[9], ray.tmin, best, tl);
+        hr = box_fast(sr, n[4], n[5], n[6], n[7], n[10], n[11], ray.tmin, best, tr);
         if (hl && hr) {
           Entry nearE = {ch[0], ch[2]}, farE = {ch[1], ch[3]};
           if (tr < tl) std::swap(nearE, farE);
@@ -326,14 +351,11 @@ void trace_one_kd(int kind, int mode, int query, const KdView& kd, const int32_t
     if (!box_ref(o, d, rb, rb + 3, tMin, tMax)) return;
   } else {
     float tn;
-    if (!box_fast(o, inv, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, best, tn)) return;
-    // exit distance of the root box, clipped the same way
-    float tx0 = (rb[0] - o.x) * inv.x, tx1 = (rb[3] - o.x) * inv.x;
-    float ty0 = (rb[1] - o.y) * inv.y, ty1 = (rb[4] - o.y) * inv.y;
-    float tz0 = (rb[2] - o.z) * inv.z, tz1 = (rb[5] - o.z) * inv.z;
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best));
+    const SlabRay sr = slab_ray(o, d);
+    if (!box_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, best, tn)) return;
+    // exit distance of the root box, clipped and widened the same way
     tMin = tn;
-    tMax = tf * kWiden;
+    tMax = std::fmaf(slab_exit(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], best), kWiden, sr.eps);
   }
   KdTodo todo[64];
   int todoPos = 0;

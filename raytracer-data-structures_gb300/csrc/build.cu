@@ -158,6 +158,31 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
   }
 }
 
+BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers& a, const rq_settings_t& cfg,
+                                bool any, const QueryTarget& q, BuildScratch& sc, uint32_t* err, cudaStream_t st) {
+  const bool bvh2 = type == RQ_LBVH || type == RQ_BVH;
+  if (!bvh2 || cfg.traversal != RQ_TRAVERSAL_FAST || cfg.ray_sort != RQ_RAY_SORT_OCTANT_MORTON ||
+      q.n < kRaySortMin) {
+    launch_query(type, s, a, cfg.traversal, any, q, err, st);
+    RQ_B(cudaGetLastError(), "trace launch");
+    return {};
+  }
+  // Coherence order: sort (octant | origin Morton, index) pairs, then trace
+  // through the permutation; results keep the caller's order.
+  RQ_B(sc.keys.ensure((size_t)q.n * 4), "ray sort scratch");
+  RQ_B(sc.vals.ensure((size_t)q.n * 4), "ray sort scratch");
+  uint32_t* keys = sc.keys.as<uint32_t>();
+  uint32_t* perm = sc.vals.as<uint32_t>();
+  launch_ray_keys(q.rays, q.n, a.root.as<const float>(), keys, perm, st);
+  BuildResult r = sort_pairs(keys, perm, q.n, 4, true, sc, err, st);
+  if (!r.ok()) return r;
+  Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+             a.root.as<const float>(), a.n_nodes, a.n_slots};
+  launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm);
+  RQ_B(cudaGetLastError(), "trace launch");
+  return {};
+}
+
 BuildResult trace_counted(int type, const SceneView& s, const AccelBuffers& a, bool any, const QueryTarget& q,
                           unsigned long long* counters, uint32_t* err, cudaStream_t st) {
   if (type != RQ_LBVH && type != RQ_BVH)

@@ -379,13 +379,10 @@ __global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, c
       in = box_ref(o, d, R[0], R[3], R[1], R[4], R[2], R[5], tMin, tMax);
     } else {
       float tn;
-      in = slab_fast(o, inv, R[0], R[3], R[1], R[4], R[2], R[5], rtmin, best, tn);
-      float tx0 = __fmul_rn(__fsub_rn(R[0], o.x), inv.x), tx1 = __fmul_rn(__fsub_rn(R[3], o.x), inv.x);
-      float ty0 = __fmul_rn(__fsub_rn(R[1], o.y), inv.y), ty1 = __fmul_rn(__fsub_rn(R[4], o.y), inv.y);
-      float tz0 = __fmul_rn(__fsub_rn(R[2], o.z), inv.z), tz1 = __fmul_rn(__fsub_rn(R[5], o.z), inv.z);
-      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best));
+      const SlabRay sr = slab_ray(o, d);
+      in = slab_fast(sr, R[0], R[3], R[1], R[4], R[2], R[5], rtmin, best, tn);
       tMin = tn;
-      tMax = __fmul_rn(tf, kWiden);
+      tMax = __fmaf_rn(slab_exit(sr, R[0], R[3], R[1], R[4], R[2], R[5], best), kWiden, sr.eps);
     }
     if (in) {
       Todo todo[kStackSize];

@@ -492,8 +492,10 @@ static rq_status_t trace(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint3
   q.n = n;
   q.hits = any ? nullptr : static_cast<float4*>(d_out);
   q.occ = any ? static_cast<uint32_t*>(d_out) : nullptr;
-  launch_query(a->type, scene_view(a->scene), a->buf, ctx->settings.traversal, any, q, ctx->d_err, ctx->stream);
-  RQ_TRY(check_launch(ctx, "trace launch"));
+  BuildResult br = launch_query_sorted(a->type, scene_view(a->scene), a->buf, ctx->settings, any, q, ctx->scratch,
+                                       ctx->d_err, ctx->stream);
+  if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+  if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
   if (!dev) {
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     return collect_device_errors(ctx);

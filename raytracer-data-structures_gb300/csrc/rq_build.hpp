@@ -94,6 +94,11 @@ struct QueryTarget {
   float4* hits = nullptr;
   uint32_t* occ = nullptr;
 };
+// Batches of at least this many rays are reordered when settings.ray_sort asks.
+constexpr uint32_t kRaySortMin = 65536;
+struct QueryTarget;
+BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers& a, const rq_settings_t& cfg,
+                                bool any, const QueryTarget& q, BuildScratch& sc, uint32_t* err, cudaStream_t st);
 void launch_query(int type, const SceneView& s, const AccelBuffers& a, int traversal, bool any,
                   const QueryTarget& q, uint32_t* err, cudaStream_t st);
 

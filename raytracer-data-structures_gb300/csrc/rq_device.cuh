@@ -91,19 +91,49 @@ __device__ __forceinline__ bool sphere_closest(const float4& s, F3 o, F3 d, floa
 
 // ---------------------------------------------------------------- boxes
 
-// Engine slab test on one child box: (b - o) * inv, NaN-ignoring min/max,
-// clipped to [tmin, tfar], far end widened by kWiden.
-__device__ __forceinline__ bool slab_fast(F3 o, F3 inv, float lx, float hx, float ly, float hy,
-                                          float lz, float hz, float tmin, float tfar,
-                                          float& tnear) {
-  float tx0 = __fmul_rn(__fsub_rn(lx, o.x), inv.x), tx1 = __fmul_rn(__fsub_rn(hx, o.x), inv.x);
-  float ty0 = __fmul_rn(__fsub_rn(ly, o.y), inv.y), ty1 = __fmul_rn(__fsub_rn(hy, o.y), inv.y);
-  float tz0 = __fmul_rn(__fsub_rn(lz, o.z), inv.z), tz1 = __fmul_rn(__fsub_rn(hz, o.z), inv.z);
+// Per-ray constants of the engine's slab test: inv = 1/d (correctly rounded),
+// noi = -(o * inv), and eps = 2^-21 * max over axes of the finite |o * inv|.
+struct SlabRay {
+  F3 inv, noi;
+  float eps;
+};
+__device__ __forceinline__ SlabRay slab_ray(F3 o, F3 d) {
+  SlabRay s;
+  s.inv = {__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)};
+  float ox = __fmul_rn(o.x, s.inv.x), oy = __fmul_rn(o.y, s.inv.y), oz = __fmul_rn(o.z, s.inv.z);
+  s.noi = {-ox, -oy, -oz};
+  float m = 0.f;
+  const float ax = fabsf(ox), ay = fabsf(oy), az = fabsf(oz);
+  if (ax <= 3.402823466e38f) m = fmaxf(m, ax);
+  if (ay <= 3.402823466e38f) m = fmaxf(m, ay);
+  if (az <= 3.402823466e38f) m = fmaxf(m, az);
+  s.eps = __fmul_rn(m, 0x1p-21f);
+  return s;
+}
+
+// Engine slab test on one box: plane distances b*inv - o*inv with one fused
+// multiply-add each, NaN-ignoring min/max, clipped to [tmin, tfar].  The far
+// end is widened by kWiden (relative rounding) and eps (the absolute error
+// of the fused form, proportional to |o*inv|), so no box that the ray truly
+// meets is rejected.
+__device__ __forceinline__ bool slab_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz,
+                                          float hz, float tmin, float tfar, float& tnear) {
+  float tx0 = __fmaf_rn(lx, r.inv.x, r.noi.x), tx1 = __fmaf_rn(hx, r.inv.x, r.noi.x);
+  float ty0 = __fmaf_rn(ly, r.inv.y, r.noi.y), ty1 = __fmaf_rn(hy, r.inv.y, r.noi.y);
+  float tz0 = __fmaf_rn(lz, r.inv.z, r.noi.z), tz1 = __fmaf_rn(hz, r.inv.z, r.noi.z);
   float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
   float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar));
-  tf = __fmul_rn(tf, kWiden);
+  tf = __fmaf_rn(tf, kWiden, r.eps);
   tnear = tn;
   return tn <= tf;
+}
+// Exit distance of the same box (before widening).
+__device__ __forceinline__ float slab_exit(const SlabRay& r, float lx, float hx, float ly, float hy, float lz,
+                                           float hz, float tfar) {
+  float tx0 = __fmaf_rn(lx, r.inv.x, r.noi.x), tx1 = __fmaf_rn(hx, r.inv.x, r.noi.x);
+  float ty0 = __fmaf_rn(ly, r.inv.y, r.noi.y), ty1 = __fmaf_rn(hy, r.inv.y, r.noi.y);
+  float tz0 = __fmaf_rn(lz, r.inv.z, r.noi.z), tz1 = __fmaf_rn(hz, r.inv.z, r.noi.z);
+  return fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar));
 }
 
 // boundingBoxIntersection (accelerators.h:628-666): division per axis, swap,

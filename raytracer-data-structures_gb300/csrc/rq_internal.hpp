@@ -108,8 +108,14 @@ struct Bvh2View {
   uint32_t n_internal;
   uint32_t n_slots;
 };
+// perm (optional): trace ray perm[i] in thread i (results stay in caller order).
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
-                       uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s);
+                       uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
+                       const uint32_t* perm = nullptr);
+// Coherence sort keys: direction octant (3 bits) + 27-bit Morton code of the
+// origin in the root box; vals = identity.
+void launch_ray_keys(const float4* rays, uint32_t n, const float* root, uint32_t* keys, uint32_t* vals,
+                     cudaStream_t s);
 // FAST traversal that also sums internal-node visits and primitive tests
 // into counters[0..1] (the inputs of the traversal byte model).
 void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n,

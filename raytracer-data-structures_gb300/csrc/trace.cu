@@ -82,21 +82,26 @@ __device__ __forceinline__ uint32_t test_count(const float4* __restrict__ prims,
   return (uint32_t)count;
 }
 
+// perm (may be null): thread i traces ray perm[i] and writes that ray's result
+// (a reordering for coherence that leaves every result where the caller
+// expects it).  With perm, any-hit bits are set with atomicOr on a zeroed array.
 template <int KIND, bool ANY, bool COUNT = false>
 __global__ void __launch_bounds__(kThreads) k_trace_fast(Bvh2View bvh, const float4* __restrict__ rays,
                                                          uint32_t n, float4* __restrict__ hits,
                                                          uint32_t* __restrict__ occ, uint32_t* err,
-                                                         unsigned long long* counters = nullptr) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+                                                         unsigned long long* counters = nullptr,
+                                                         const uint32_t* __restrict__ perm = nullptr) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t r = (perm && i < n) ? __ldg(perm + i) : i;
   bool occluded = false;
   uint32_t visits = 0, tests = 0;
-  if (r < n) {
+  if (i < n) {
     Ray ray = load_ray(rays, r);
     Closest c = {ray.tmax, kMiss, 0.f, 0.f};
-    F3 inv = {__frcp_rn(ray.d.x), __frcp_rn(ray.d.y), __frcp_rn(ray.d.z)};
+    const SlabRay sr = slab_ray(ray.o, ray.d);
     float tn;
     const float* rb = bvh.root;
-    if (slab_fast(ray.o, inv, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
+    if (slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
       int2 stack[kStackSize];
       int sp = 0;
       int cur = bvh.n_internal ? 0 : -1;
@@ -113,8 +118,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_fast(Bvh2View bvh, const flo
           if (COUNT) ++visits;
           const float tfar = ANY ? ray.tmax : c.t;
           float tl, tr;
-          bool hl = slab_fast(ray.o, inv, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
-          bool hr = slab_fast(ray.o, inv, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+          bool hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+          bool hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
           if (hl && hr) {
             int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
             if (tr < tl) { int2 s = nearE; nearE = farE; farE = s; }
@@ -142,9 +147,13 @@ __global__ void __launch_bounds__(kThreads) k_trace_fast(Bvh2View bvh, const flo
     if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
   }
   if (ANY) {
-    uint32_t bits = __ballot_sync(0xffffffffu, occluded);
-    uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
-    if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+    if (perm) {
+      if (occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+    } else {
+      uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+      uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+      if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+    }
   }
   if (COUNT) {
     unsigned long long v = visits, t = tests;
@@ -268,12 +277,12 @@ __global__ void __launch_bounds__(kThreads) k_brute(const float4* __restrict__ p
 
 template <int KIND, bool ANY>
 void dispatch_bvh2(int traversal, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
-                   uint32_t* occ, uint32_t* err, cudaStream_t s) {
+                   uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s) {
   uint32_t g = (n + kThreads - 1) / kThreads;
   if (traversal == RQ_TRAVERSAL_REFERENCE)
     k_trace_ref<KIND, ANY><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err);
   else
-    k_trace_fast<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr);
+    k_trace_fast<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr, perm);
 }
 
 template <int KIND, bool ANY>
@@ -310,16 +319,54 @@ void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const floa
 }
 
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
-                       uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s) {
+                       uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
+                       const uint32_t* perm) {
   if (n == 0) return;
   count_launch();
+  if (traversal == RQ_TRAVERSAL_REFERENCE) perm = nullptr;
+  if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
   if (kind == kTriangles) {
-    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, s);
-    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, s);
+    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, perm, s);
+    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, perm, s);
   } else {
-    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, s);
-    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, s);
+    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, perm, s);
+    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, perm, s);
   }
+}
+
+// Sort key of a ray for coherent tracing: the direction octant in the top
+// three bits, then a 27-bit Morton code of the origin inside the scene box.
+__global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ rays, uint32_t n,
+                                                  const float* __restrict__ root, uint32_t* __restrict__ keys,
+                                                  uint32_t* __restrict__ vals) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+  const float o[3] = {a.x, a.y, a.z};
+  uint32_t q[3];
+  for (int k = 0; k < 3; ++k) {
+    float lo = root[k], ext = root[3 + k] - root[k];
+    float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
+    u = fminf(fmaxf(u * 512.f, 0.f), 511.f);
+    q[k] = (uint32_t)u;
+  }
+  auto spread = [](uint32_t v) {  // 9 bits -> every third bit
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+  };
+  const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
+  keys[i] = (oct << 27) | (spread(q[0]) << 2) | (spread(q[1]) << 1) | spread(q[2]);
+  vals[i] = i;
+}
+
+void launch_ray_keys(const float4* rays, uint32_t n, const float* root, uint32_t* keys, uint32_t* vals,
+                     cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  k_ray_keys<<<(n + 255) / 256, 256, 0, s>>>(rays, n, root, keys, vals);
 }
 
 void launch_trace_brute(int kind, int traversal, bool any, const float4* prims, uint32_t n_prims,

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "librq.so")
 BVH, KDTREE, UNIFORM_GRID, LBVH, NONE = 0, 1, 2, 3, 4
 ACC_NAMES = {"BVH": BVH, "KDTREE": KDTREE, "UNIFORM_GRID": UNIFORM_GRID, "LBVH": LBVH, "NONE": NONE}
 TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
+RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON = 0, 1
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1
 DEVICE_POINTERS = 0x1
 MISS = 0xFFFFFFFF
@@ -34,7 +35,8 @@ class Settings(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("fov", C.c_float),
                 ("backgroundColor", C.c_float * 3), ("bias", C.c_float), ("aa_samples", C.c_uint32),
                 ("dataStructure", C.c_int32), ("sceneModel", C.c_int32), ("traversal", C.c_int32),
-                ("morton", C.c_int32), ("kd_max_depth", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("morton", C.c_int32), ("kd_max_depth", C.c_int32), ("ray_sort", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class AccelInfo(C.Structure):
