@@ -165,7 +165,7 @@ def run_ours(args):
     d_verts = torch.from_numpy(verts).to(dev)
     d_idx = torch.from_numpy(idx.view(np.int32)).to(dev)
     scene = eng.scene_triangles(d_verts, d_idx)
-    acc = eng.build(scene, rq.LBVH)
+    acc = eng.build(scene, rq.LBVH)  # binary tree for the first primary pass
 
     def dev_rays(r):
         return torch.from_numpy(np.ascontiguousarray(r).view(np.uint8)).to(dev)
@@ -186,44 +186,65 @@ def run_ours(args):
     total_rays = n_p + n_s + n_sh
     log(f"[bench] tris={n_tri} primary={n_p} secondary={n_s} shadow={n_sh}")
 
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    # Autotuning over the engine's speed-only options (results are identical
+    # under every choice): BVH node width (binary or collapsed 4-wide, fixed
+    # at build time, the collapse counted in the build phase) and ray
+    # reordering per ray class.  Each candidate is timed on the real rays.
+    def timed(fn, reps=3):
+        times = []
+        for _ in range(reps):
+            a0, a1 = ev(), ev()
+            a0.record(stream)
+            fn()
+            a1.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(a0.elapsed_time(a1))
+        return min(times)
+
+    def class_call(a, name):
+        if name == "primary":
+            return lambda: eng.trace_closest(a, d_prim, d_hits_p)
+        if name == "secondary":
+            return lambda: eng.trace_closest(a, d_sec, d_hits_s)
+        return lambda: eng.trace_any(a, d_sh, d_bits)
+
+    tuning = {}
+    best = None
+    for width in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4):
+        eng.configure(node_width=width, ray_sort=rq.RAY_SORT_NONE)
+        cand = eng.build(scene, rq.LBVH)
+        choice, total = {}, timed(cand.rebuild)
+        for name in ("primary", "secondary", "shadow"):
+            opts = {}
+            for opt in (rq.RAY_SORT_NONE, rq.RAY_SORT_OCTANT_MORTON):
+                eng.configure(ray_sort=opt)
+                opts[opt] = timed(class_call(cand, name))
+            choice[name] = min(opts, key=opts.get)
+            total += opts[choice[name]]
+        tuning[f"width{max(width, 2)}"] = {"est_step_ms": round(total, 4), "ray_sort": choice}
+        if best is None or total < best[0]:
+            if best is not None:
+                best[1].close()
+            best = (total, cand, width, choice)
+        else:
+            cand.close()
+    acc.close()
+    _, acc, node_width, sort_choice = best
+    eng.configure(node_width=node_width)
+    node_bytes = 128 if node_width == rq.NODE_WIDTH_4 else NODE_BYTES
+    log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}")
+
     # Traversal work of each query on these exact rays (the byte model's inputs).
     counts = {}
     for name, rays, anyhit in (("primary", primary, False), ("secondary", secondary, False), ("shadow", shadow, True)):
         _, cnt = eng.trace_counters(acc, rays, any_hit=anyhit)
         counts[name] = (int(cnt[0]), int(cnt[1]))
 
-    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
-
-    # Ray reordering per ray class, chosen by timing both settings (results are
-    # identical either way; only the speed differs).
-    sort_choice = {"primary": 0, "secondary": 0, "shadow": 0}
-
     def trace_class(name, marks=None):
         eng.configure(ray_sort=sort_choice[name])
-        if name == "primary":
-            eng.trace_closest(acc, d_prim, d_hits_p)
-        elif name == "secondary":
-            eng.trace_closest(acc, d_sec, d_hits_s)
-        else:
-            eng.trace_any(acc, d_sh, d_bits)
-
-    for name in sort_choice:
-        best = None
-        for opt in (rq.RAY_SORT_NONE, rq.RAY_SORT_OCTANT_MORTON):
-            sort_choice[name] = opt
-            times = []
-            for _ in range(3):
-                a0, a1 = ev(), ev()
-                a0.record(stream)
-                trace_class(name)
-                a1.record(stream)
-                torch.cuda.synchronize(dev)
-                times.append(a0.elapsed_time(a1))
-            t = min(times)
-            if best is None or t < best[0]:
-                best = (t, opt)
-        sort_choice[name] = best[1]
-    log(f"[bench] ray_sort per class: {sort_choice}")
+        class_call(acc, name)()
 
     def step(marks=None):
         if marks: marks[0].record(stream)
@@ -273,7 +294,7 @@ def run_ours(args):
 
     def trace_bytes(name, n, closest=True):
         v, t = counts[name]
-        return n * RAY_BYTES + (n * HIT_BYTES if closest else ((n + 31) // 32) * 4) + v * NODE_BYTES + t * TRI_BYTES
+        return n * RAY_BYTES + (n * HIT_BYTES if closest else ((n + 31) // 32) * 4) + v * node_bytes + t * TRI_BYTES
 
     build_bytes = build_bytes_per_tri() * n_tri
     alg = {"build": build_bytes, "trace_primary": trace_bytes("primary", n_p),
@@ -299,9 +320,9 @@ def run_ours(args):
                 m[0].record(stream)
                 other.rebuild()
                 m[1].record(stream)
-                eng.trace_closest(other, d_prim, d_hits_p)
-                eng.trace_closest(other, d_sec, d_hits_s)
-                eng.trace_any(other, d_sh, d_bits)
+                for cls in ("primary", "secondary", "shadow"):
+                    eng.configure(ray_sort=sort_choice[cls])
+                    class_call(other, cls)()
                 m[2].record(stream)
                 torch.cuda.synchronize(dev)
                 if k:
@@ -316,7 +337,7 @@ def run_ours(args):
 
     e2e = None
     if rank == 0 and not args.skip_e2e:
-        e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args)
+        e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
@@ -331,13 +352,13 @@ def run_ours(args):
                        "secondary_rays": n_s, "shadow_rays": n_sh, "seed": SEED,
                        "l2": "flushed before every timed step (256 MB write); rays exceed L2",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                       "ray_sort": sort_choice},
+                       "node_width": max(node_width, 2), "ray_sort": sort_choice, "tuning": tuning},
             "lbvh_build_mtri_s": round(n_tri / (build_ms * 1e-3) / 1e6, 2),
             "closest_grays_s": round((n_p + n_s) / ((prim_ms + sec_ms) * 1e-3) / 1e9, 4),
             "any_grays_s": round(n_sh / (sh_ms * 1e-3) / 1e9, 4),
             "phase_ms": {"build": round(build_ms, 4), "trace_primary": round(prim_ms, 4),
                          "trace_secondary": round(sec_ms, 4), "trace_shadow": round(sh_ms, 4)},
-            "traversal_work": {k: {"nodes_per_ray": round(v[0] / max(1, {"primary": n_p, "secondary": n_s, "shadow": n_sh}[k]), 3),
+            "traversal_work": {k: {"node_bytes": node_bytes, "nodes_per_ray": round(v[0] / max(1, {"primary": n_p, "secondary": n_s, "shadow": n_sh}[k]), 3),
                                    "tris_per_ray": round(v[1] / max(1, {"primary": n_p, "secondary": n_s, "shadow": n_sh}[k]), 3)}
                                for k, v in counts.items()},
             "roofline": roofline,
@@ -363,7 +384,7 @@ def build_bytes_per_tri():
     return 6 + 26 + 64 + 28 + 150
 
 
-def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args):
+def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice):
     import torch
     import rq
 
@@ -387,8 +408,11 @@ def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args):
     def step():
         scene.update(hv, hi)
         acc.rebuild()
+        eng.configure(ray_sort=sort_choice["primary"])
         eng.trace_closest(acc, hp, out_p)
+        eng.configure(ray_sort=sort_choice["secondary"])
         eng.trace_closest(acc, hs, out_s)
+        eng.configure(ray_sort=sort_choice["shadow"])
         eng.trace_any(acc, hsh, out_b)
 
     for _ in range(max(1, args.warmup)):

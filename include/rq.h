@@ -78,8 +78,20 @@ typedef struct rq_settings_t {
   int32_t morton;             /* rq_morton_t, RQ_MORTON_SCENE_BOUNDS */
   int32_t kd_max_depth;       /* <= 0: round(8 + 1.3 log2 N) as the reference (accelerators.h:958) */
   int32_t ray_sort;           /* rq_ray_sort_t: reorder large FAST batches for coherence */
-  int32_t reserved[4];
+  int32_t node_width;         /* rq_node_width_t: BVH node fan-out for FAST queries (RQ_BVH, RQ_LBVH) */
+  int32_t reserved[3];
 } rq_settings_t;
+
+/* Node fan-out of BVH structures (RQ_BVH, RQ_LBVH), fixed when the structure
+ * is built.  RQ_NODE_WIDTH_4 adds a collapsed 4-wide copy of the binary tree
+ * (every even-depth node merged with its internal children: one 128-byte
+ * node holds up to four child boxes) that FAST queries walk instead.  Hits
+ * and occlusion bits are those of the binary tree; REFERENCE queries and
+ * rq_accel_export_bvh2 keep using the binary nodes. */
+typedef enum rq_node_width_t {
+  RQ_NODE_WIDTH_2 = 0, /* binary nodes (2 is accepted too) */
+  RQ_NODE_WIDTH_4 = 4
+} rq_node_width_t;
 
 /* Ray reordering before FAST BVH2 traversal of batches of at least 65,536
  * rays.  Results are written in the caller's order either way and do not
@@ -146,6 +158,8 @@ typedef struct rq_accel_info_t {
   uint32_t max_depth;      /* KD: depth limit used */
   float root_bounds[6];    /* min xyz, max xyz */
   uint64_t device_bytes;   /* device memory held by the structure */
+  uint32_t node_width;     /* BVH2 structures: 2, or 4 with a collapsed 4-wide copy; else 0 */
+  uint32_t n_wide_nodes;   /* nodes of the 4-wide copy */
 } rq_accel_info_t;
 
 /* ------------------------------------------------------------ lifecycle */
@@ -208,6 +222,13 @@ rq_status_t rq_accel_get_info(rq_accel_t accel, rq_accel_info_t* info);
 rq_status_t rq_accel_export_bvh2(rq_ctx_t ctx, rq_accel_t accel, float* nodes, uint32_t* order,
                                  uint32_t* sorted_codes);
 rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t accel, int32_t* nodes, int32_t* prim_idx);
+/* The collapsed 4-wide nodes of a structure built with RQ_NODE_WIDTH_4:
+ * n_nodes receives the count; nodes (may be NULL) receives n_nodes * 32 words
+ * [lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] link[4] count[4]].  A
+ * child with link >= 0 is a 4-wide node, link < 0 a leaf holding slots
+ * [~link, ~link + count) of the binary tree's order; unused children have
+ * count -1.  No reference counterpart: the reference's trees are binary. */
+rq_status_t rq_accel_export_bvh4(rq_ctx_t ctx, rq_accel_t accel, float* nodes, uint32_t* n_nodes);
 
 /* ---------------------------------------------------------------- queries */
 

@@ -989,6 +989,172 @@ int orc_trace_bvh2(int kind, int mode, int query, const float* nodes16, uint32_t
   return 0;
 }
 
+// Order-preserving unsigned image of a non-NaN float.
+static inline uint32_t float_order_key(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+uint32_t orc_collapse_bvh4(const float* nodes16, uint32_t n_internal, float* nodes32) {
+  if (n_internal == 0) return 0;
+  auto link = [&](uint32_t b, int side) {
+    int32_t v;
+    std::memcpy(&v, nodes16 + 16 * (size_t)b + 12 + side, 4);
+    return v;
+  };
+  auto cnt = [&](uint32_t b, int side) {
+    int32_t v;
+    std::memcpy(&v, nodes16 + 16 * (size_t)b + 14 + side, 4);
+    return v;
+  };
+  // depth by breadth-first walk from the root
+  std::vector<int32_t> depth(n_internal, -1);
+  std::vector<uint32_t> q{0};
+  depth[0] = 0;
+  for (size_t h = 0; h < q.size(); ++h)
+    for (int side = 0; side < 2; ++side) {
+      int32_t c = link(q[h], side);
+      if (c >= 0) {
+        depth[c] = depth[q[h]] + 1;
+        q.push_back((uint32_t)c);
+      }
+    }
+  std::vector<uint32_t> idx4(n_internal, 0);
+  uint32_t n4 = 0;
+  for (uint32_t b = 0; b < n_internal; ++b)
+    if (depth[b] % 2 == 0) idx4[b] = n4++;
+  // child box of binary node b, side s: {lo.x, hi.x, lo.y, hi.y, lo.z, hi.z}
+  auto box = [&](uint32_t b, int s, float* o) {
+    const float* n = nodes16 + 16 * (size_t)b;
+    o[0] = n[4 * s + 0]; o[1] = n[4 * s + 1]; o[2] = n[4 * s + 2]; o[3] = n[4 * s + 3];
+    o[4] = n[8 + 2 * s]; o[5] = n[9 + 2 * s];
+  };
+  for (uint32_t b = 0; b < n_internal; ++b) {
+    if (depth[b] % 2) continue;
+    float* w = nodes32 + 32 * (size_t)idx4[b];
+    for (int k = 0; k < 4; ++k) {
+      w[k] = INFINITY; w[4 + k] = -INFINITY; w[8 + k] = INFINITY; w[12 + k] = -INFINITY;
+      w[16 + k] = INFINITY; w[20 + k] = -INFINITY;
+      int32_t z = 0, none = -1;
+      std::memcpy(w + 24 + k, &z, 4);
+      std::memcpy(w + 28 + k, &none, 4);
+    }
+    int slot = 0;
+    auto put = [&](const float* bx, int32_t l, int32_t c) {
+      w[slot] = bx[0]; w[4 + slot] = bx[1]; w[8 + slot] = bx[2]; w[12 + slot] = bx[3];
+      w[16 + slot] = bx[4]; w[20 + slot] = bx[5];
+      std::memcpy(w + 24 + slot, &l, 4);
+      std::memcpy(w + 28 + slot, &c, 4);
+      ++slot;
+    };
+    for (int s = 0; s < 2; ++s) {
+      int32_t c = link(b, s);
+      float bx[6];
+      if (c < 0) {
+        box(b, s, bx);
+        put(bx, c, cnt(b, s));
+      } else {
+        for (int s2 = 0; s2 < 2; ++s2) {
+          int32_t g = link((uint32_t)c, s2);
+          box((uint32_t)c, s2, bx);
+          if (g < 0) put(bx, g, cnt((uint32_t)c, s2));
+          else put(bx, (int32_t)idx4[g], 0);
+        }
+      }
+    }
+  }
+  return n4;
+}
+
+int orc_trace_bvh4(int kind, int query, const float* nodes32, uint32_t n4, const float* rb,
+                   uint32_t n_prims, const uint32_t* order, const float* prims, const orc_ray_t* rays,
+                   uint32_t nrays, orc_hit_t* hits, uint8_t* occluded, uint64_t* counters, int nthreads) {
+  uint64_t visits = 0, tests = 0;
+  int nt = nthreads_or_default(nthreads);
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 256) reduction(+ : visits, tests)
+  for (int64_t r = 0; r < (int64_t)nrays; ++r) {
+    const orc_ray_t& ray = rays[r];
+    V3 o = v3(ray.org), d = v3(ray.dir);
+    orc_hit_t h{ray.tmax, kMiss, 0.f, 0.f};
+    uint8_t occ = 0;
+    float best = ray.tmax;
+    const SlabRay sr = slab_ray(o, d);
+    float tn;
+    if (box_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, best, tn)) {
+      std::vector<Entry> stack;
+      stack.reserve(96);
+      Entry cur = n4 == 0 ? Entry{~0, (int32_t)n_prims} : Entry{0, 0};
+      for (;;) {
+        if (cur.node >= 0) {
+          const float* w = nodes32 + 32 * (size_t)cur.node;
+          ++visits;
+          const float tfar = query == ORC_ANY ? ray.tmax : best;
+          // Hit children ordered by key = (order-preserving bits of the entry
+          // distance, low two bits replaced by the slot): nearest first,
+          // distances within four ulps in slot order.
+          uint32_t key[4];
+          int m = 0;
+          for (int k = 0; k < 4; ++k) {
+            float tk;
+            int32_t ck;
+            std::memcpy(&ck, w + 28 + k, 4);
+            // an unused slot (count -1) is never entered: a slab test alone
+            // cannot reject an inverted box for every ray direction
+            if (ck >= 0 &&
+                box_fast(sr, w[k], w[4 + k], w[8 + k], w[12 + k], w[16 + k], w[20 + k], ray.tmin, tfar, tk))
+              key[m++] = (float_order_key(tk) & ~3u) | (uint32_t)k;
+          }
+          std::sort(key, key + m);
+          int slot[4];
+          for (int q2 = 0; q2 < m; ++q2) slot[q2] = (int)(key[q2] & 3u);
+          if (m > 0) {
+            for (int q2 = m - 1; q2 >= 1; --q2) {
+              int32_t l, c;
+              std::memcpy(&l, w + 24 + slot[q2], 4);
+              std::memcpy(&c, w + 28 + slot[q2], 4);
+              stack.push_back({l, c});
+            }
+            int32_t l, c;
+            std::memcpy(&l, w + 24 + slot[0], 4);
+            std::memcpy(&c, w + 28 + slot[0], 4);
+            cur = {l, c};
+            continue;
+          }
+        } else {
+          uint32_t first = (uint32_t)(~cur.node);
+          bool done = false;
+          for (int32_t k = 0; k < cur.count; ++k) {
+            uint32_t id = order[first + (uint32_t)k];
+            ++tests;
+            if (query == ORC_ANY) {
+              if (test_prim_any(kind, ORC_MODE_FAST, prims, id, o, d, ray.tmin, ray.tmax)) {
+                occ = 1;
+                done = true;
+                break;
+              }
+            } else {
+              float t, u, v;
+              if (test_prim(kind, ORC_MODE_FAST, prims, id, o, d, ray.tmin, best, t, u, v)) {
+                best = t;
+                h = {t, id, u, v};
+              }
+            }
+          }
+          if (done) break;
+        }
+        if (stack.empty()) break;
+        cur = stack.back();
+        stack.pop_back();
+      }
+    }
+    if (hits) hits[r] = h;
+    if (occluded) occluded[r] = occ;
+  }
+  if (counters) { counters[0] += visits; counters[1] += tests; }
+  return 0;
+}
+
 int orc_trace_kd(int kind, int mode, int query, const int32_t* nodes3, uint32_t n_nodes,
                  const int32_t* prim_idx, const float* root_bounds6, const float* prims,
                  const orc_ray_t* rays, uint32_t nrays, orc_hit_t* hits, uint8_t* occluded,

@@ -90,6 +90,21 @@ int orc_trace_kd(int kind, int mode, int query, const int32_t* nodes3, uint32_t 
                  const int32_t* prim_idx, const float* root_bounds6, const float* prims,
                  const orc_ray_t* rays, uint32_t nrays, orc_hit_t* hits, uint8_t* occluded,
                  uint64_t* counters, int nthreads);
+/* Collapsed 4-wide BVH (the engine's node-width option).  Node = 32 words
+ * [lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] link[4] count[4]], made
+ * from a BVH2 by merging every internal node at even depth with its internal
+ * children; children in the order left.left, left.right, right.left,
+ * right.right (a leaf child of the binary node stays one child); unused slots
+ * have lo = +inf, hi = -inf, link 0 and count -1.  Nodes are numbered in binary-index order of the
+ * even-depth nodes.  Returns the node count (nodes32 holds n_internal nodes). */
+uint32_t orc_collapse_bvh4(const float* nodes16, uint32_t n_internal, float* nodes32);
+/* FAST closest/any hit through it: the hit children are ordered by the key
+ * (order-preserving bits of the entry distance with the low two bits
+ * replaced by the slot); the first is visited next, the rest pushed last
+ * first. */
+int orc_trace_bvh4(int kind, int query, const float* nodes32, uint32_t n4, const float* root_bounds6,
+                   uint32_t n_prims, const uint32_t* order, const float* prims, const orc_ray_t* rays,
+                   uint32_t nrays, orc_hit_t* hits, uint8_t* occluded, uint64_t* counters, int nthreads);
 int orc_trace_brute(int kind, int mode, int query, uint32_t n_prims, const float* prims,
                     const orc_ray_t* rays, uint32_t nrays, orc_hit_t* hits, uint8_t* occluded,
                     int nthreads);

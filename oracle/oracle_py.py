@@ -241,6 +241,32 @@ def trace_bvh2(kind, mode, query, bvh, prims, rays, nthreads=0, counters=None):
     return hits if query == CLOSEST else occ
 
 
+def collapse_bvh4(bvh):
+    """Collapsed 4-wide BVH of a Bvh2: (nodes as (n4, 32) float32, n4)."""
+    n = max(bvh.n_internal, 1)
+    out = np.zeros((n, 32), np.float32)
+    if bvh.n_internal == 0:
+        return out[:0], 0
+    lib().orc_collapse_bvh4.restype = C.c_uint32
+    n4 = lib().orc_collapse_bvh4(_p(_c(bvh.nodes, np.float32)), C.c_uint32(bvh.n_internal), _p(out))
+    return out[:n4], int(n4)
+
+
+def trace_bvh4(kind, query, nodes4, bvh, prims, rays, nthreads=0, counters=None):
+    prims = _c(prims, np.float32)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    hits, occ = _trace_out(len(rays), query)
+    cnt = np.zeros(2, np.uint64)
+    nodes = _c(nodes4, np.float32) if len(nodes4) else np.zeros((1, 32), np.float32)
+    lib().orc_trace_bvh4(C.c_int(kind), C.c_int(query), _p(nodes), C.c_uint32(len(nodes4)),
+                         _p(_c(bvh.root_bounds, np.float32)), C.c_uint32(len(bvh.order)),
+                         _p(_c(bvh.order, np.uint32)), _p(prims), _p(rays), C.c_uint32(len(rays)),
+                         _p(hits), _p(occ), _p(cnt), C.c_int(nthreads))
+    if counters is not None:
+        counters += cnt
+    return hits if query == CLOSEST else occ
+
+
 def trace_kd(kind, mode, query, kd, prims, rays, nthreads=0, counters=None):
     prims = _c(prims, np.float32)
     rays = np.ascontiguousarray(rays, RAY_DTYPE)

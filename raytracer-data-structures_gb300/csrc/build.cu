@@ -133,13 +133,24 @@ static BuildResult build_none(const SceneView& s, AccelBuffers& a, cudaStream_t 
 BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, AccelBuffers& a,
                         BuildScratch& sc, uint32_t* err, cudaStream_t st) {
   if (s.n == 0) return BuildResult::error(RQ_ERROR_EMPTY_SCENE, "empty scene");
+  a.node_width = 2;
+  if (type == RQ_LBVH || type == RQ_BVH) {
+    if (cfg.node_width != RQ_NODE_WIDTH_2 && cfg.node_width != 2 && cfg.node_width != RQ_NODE_WIDTH_4)
+      return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "node_width must be 2 or 4");
+    BuildResult r = type == RQ_LBVH ? build_lbvh(s, cfg, a, sc, err, st) : build_median_bvh(s, a, sc, err, st);
+    if (r.ok() && cfg.node_width == RQ_NODE_WIDTH_4) r = collapse_bvh4(a, sc, err, st);
+    return r;
+  }
   switch (type) {
-    case RQ_LBVH: return build_lbvh(s, cfg, a, sc, err, st);
-    case RQ_BVH: return build_median_bvh(s, a, sc, err, st);
     case RQ_KDTREE: return build_kd_tree(s, cfg.kd_max_depth, a, sc, err, st);
     case RQ_NONE: return build_none(s, a, st);
     default: return BuildResult::error(RQ_ERROR_UNSUPPORTED, "unsupported dataStructure");
   }
+}
+
+static Bvh4View bvh4_view(const AccelBuffers& a) {
+  return {a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+          a.root.as<const float>(), a.n_nodes, a.n_slots};
 }
 
 void launch_query(int type, const SceneView& s, const AccelBuffers& a, int traversal, bool any,
@@ -151,6 +162,8 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
     KdView v{a.kd_nodes.as<const int4>(), a.kd_idx.as<const int32_t>(), a.prims.as<const float4>(),
              a.root.as<const float>(), a.n_nodes};
     launch_trace_kd(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
+  } else if (a.node_width == 4 && traversal == RQ_TRAVERSAL_FAST) {
+    launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st);
   } else {
     Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
                a.root.as<const float>(), a.n_nodes, a.n_slots};
@@ -176,9 +189,13 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   launch_ray_keys(q.rays, q.n, a.root.as<const float>(), keys, perm, st);
   BuildResult r = sort_pairs(keys, perm, q.n, 4, true, sc, err, st);
   if (!r.ok()) return r;
-  Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
-             a.root.as<const float>(), a.n_nodes, a.n_slots};
-  launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm);
+  if (a.node_width == 4) {
+    launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
+  } else {
+    Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+               a.root.as<const float>(), a.n_nodes, a.n_slots};
+    launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm);
+  }
   RQ_B(cudaGetLastError(), "trace launch");
   return {};
 }
@@ -187,6 +204,11 @@ BuildResult trace_counted(int type, const SceneView& s, const AccelBuffers& a, b
                           unsigned long long* counters, uint32_t* err, cudaStream_t st) {
   if (type != RQ_LBVH && type != RQ_BVH)
     return BuildResult::error(RQ_ERROR_UNSUPPORTED, "traversal counters exist for BVH2 structures");
+  if (a.node_width == 4) {
+    launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, nullptr, counters);
+    RQ_B(cudaGetLastError(), "counted trace launch");
+    return {};
+  }
   Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
              a.root.as<const float>(), a.n_nodes, a.n_slots};
   launch_trace_bvh2_counted(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, counters, st);

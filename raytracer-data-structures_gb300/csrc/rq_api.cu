@@ -209,6 +209,8 @@ rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.traversal must be FAST or REFERENCE");
   if (s->morton != RQ_MORTON_SCENE_BOUNDS && s->morton != RQ_MORTON_REFERENCE)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.morton must be SCENE_BOUNDS or REFERENCE");
+  if (s->node_width != RQ_NODE_WIDTH_2 && s->node_width != 2 && s->node_width != RQ_NODE_WIDTH_4)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.node_width must be 2 or 4");
   ctx->settings = *s;
   return RQ_SUCCESS;
 }
@@ -427,9 +429,14 @@ rq_status_t rq_accel_get_info(rq_accel_t a, rq_accel_info_t* info) {
   info->n_slots = a->buf.n_slots;
   info->max_depth = a->buf.max_depth;
   info->device_bytes = a->buf.device_bytes();
+  const bool bvh2 = a->type == RQ_BVH || a->type == RQ_LBVH;
+  info->node_width = bvh2 ? a->buf.node_width : 0;
   if (a->buf.root.p) {
-    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(info->root_bounds, a->buf.root.p, 24, cudaMemcpyDeviceToHost, ctx->stream));
+    float words[8];
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(words, a->buf.root.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
     RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::memcpy(info->root_bounds, words, 24);
+    if (bvh2 && a->buf.node_width == 4) std::memcpy(&info->n_wide_nodes, words + 6, 4);
   }
   return RQ_SUCCESS;
 }
@@ -447,6 +454,23 @@ rq_status_t rq_accel_export_bvh2(rq_ctx_t ctx, rq_accel_t a, float* nodes, uint3
   if (sorted_codes && a->type == RQ_LBVH)
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(sorted_codes, a->buf.codes.p, (size_t)a->scene->n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_accel_export_bvh4(rq_ctx_t ctx, rq_accel_t a, float* nodes, uint32_t* n_nodes) {
+  if (!a || !n_nodes) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel or count");
+  RQ_TRY(bind(ctx));
+  if ((a->type != RQ_BVH && a->type != RQ_LBVH) || a->buf.node_width != 4)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "not built with node_width 4");
+  uint32_t n4 = 0;
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(&n4, a->buf.root.as<uint32_t>() + 6, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (n4 > a->buf.n4_cap) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed 4-wide node count");
+  *n_nodes = n4;
+  if (nodes && n4) {
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(nodes, a->buf.nodes4.p, (size_t)n4 * 128, cudaMemcpyDeviceToHost, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
   return RQ_SUCCESS;
 }
 

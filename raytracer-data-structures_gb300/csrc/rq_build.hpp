@@ -23,16 +23,20 @@ struct AccelBuffers {
   DevBuf root;         // 8 floats: root box (min xyz, max xyz)
   DevBuf kd_nodes;     // KD: int4 per node
   DevBuf kd_idx;       // KD: primitive indices
+  DevBuf nodes4;       // collapsed 4-wide nodes, 128 B each (node_width 4)
   uint32_t n_nodes = 0;
   uint32_t n_slots = 0;
   uint32_t max_depth = 0;
+  uint32_t node_width = 2;  // BVH2 structures: 2, or 4 when nodes4 holds the collapsed tree
+  uint32_t n4_cap = 0;      // bound of the 4-wide node count (exact count: root word 6)
   void release() {
     nodes.release(); prims.release(); order.release(); codes.release(); root.release();
-    kd_nodes.release(); kd_idx.release();
-    n_nodes = n_slots = max_depth = 0;
+    kd_nodes.release(); kd_idx.release(); nodes4.release();
+    n_nodes = n_slots = max_depth = n4_cap = 0;
+    node_width = 2;
   }
   size_t device_bytes() const {
-    return nodes.cap + prims.cap + order.cap + codes.cap + root.cap + kd_nodes.cap + kd_idx.cap;
+    return nodes.cap + prims.cap + order.cap + codes.cap + root.cap + kd_nodes.cap + kd_idx.cap + nodes4.cap;
   }
 };
 
@@ -87,6 +91,10 @@ BuildResult build_median_bvh(const SceneView& s, AccelBuffers& a, BuildScratch& 
                              cudaStream_t st);
 BuildResult build_kd_tree(const SceneView& s, int max_depth, AccelBuffers& a, BuildScratch& sc,
                           uint32_t* err, cudaStream_t st);
+// Collapsed 4-wide copy of the binary nodes in a.nodes (a.nodes4; node count
+// into the root buffer's word 6).
+uint32_t bvh4_node_cap(uint32_t n_internal);
+BuildResult collapse_bvh4(AccelBuffers& a, BuildScratch& sc, uint32_t* err, cudaStream_t st);
 
 struct QueryTarget {
   const float4* rays = nullptr;

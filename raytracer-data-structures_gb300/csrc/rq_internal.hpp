@@ -125,6 +125,19 @@ void launch_trace_brute(int kind, int traversal, bool any, const float4* prims, 
                         const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
                         cudaStream_t s);
 
+// Collapsed 4-wide BVH over the same slot-ordered payload.
+struct Bvh4View {
+  const float4* nodes;    // 8 float4 per node
+  const float4* prims;
+  const uint32_t* order;
+  const float* root;
+  uint32_t n_binary;      // binary internal nodes (0: the root is one leaf)
+  uint32_t n_slots;
+};
+void launch_trace_bvh4(int kind, bool any, const Bvh4View& v, const float4* rays, uint32_t n, float4* hits,
+                       uint32_t* occ, uint32_t* err, cudaStream_t s, const uint32_t* perm = nullptr,
+                       unsigned long long* counters = nullptr);
+
 struct KdView {
   const int4* nodes;      // {word0, word1, word2, 0}
   const int32_t* prim_idx;

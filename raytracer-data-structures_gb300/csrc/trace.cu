@@ -168,6 +168,138 @@ __global__ void __launch_bounds__(kThreads) k_trace_fast(Bvh2View bvh, const flo
   }
 }
 
+// ---------------------------------------------------------------- 4-wide
+// FAST traversal of the collapsed 4-wide BVH: one 128-byte node fetch tests
+// up to four child boxes.  The hit children are ordered by a 32-bit key, the
+// order-preserving bits of the entry distance with the low two bits replaced
+// by the slot (unique keys, so a sorting network gives the same order as any
+// sort); the nearest is visited next and the others pushed farthest first.
+// Three entries per level at most: 96 stack entries cover trees 64 binary
+// levels deep, like the binary walk's 64.
+constexpr int kStack4 = 96;
+
+__device__ __forceinline__ uint32_t order_key(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
+  uint32_t lo = min(a, b), hi = max(a, b);
+  a = lo;
+  b = hi;
+}
+
+__device__ __forceinline__ int pick(const int4& v, uint32_t k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
+template <int KIND, bool ANY, bool COUNT = false>
+__global__ void __launch_bounds__(kThreads) k_trace_bvh4(Bvh4View bvh, const float4* __restrict__ rays,
+                                                         uint32_t n, float4* __restrict__ hits,
+                                                         uint32_t* __restrict__ occ, uint32_t* err,
+                                                         const uint32_t* __restrict__ perm,
+                                                         unsigned long long* counters) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t r = (perm && i < n) ? __ldg(perm + i) : i;
+  bool occluded = false;
+  uint32_t visits = 0, tests = 0;
+  if (i < n) {
+    Ray ray = load_ray(rays, r);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    const SlabRay sr = slab_ray(ray.o, ray.d);
+    float tn;
+    const float* rb = bvh.root;
+    if (slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
+      int2 stack[kStack4];
+      int sp = 0;
+      int cur = bvh.n_binary ? 0 : -1;
+      int cnt = bvh.n_binary ? 0 : (int)bvh.n_slots;
+      // A valid walk visits every node and leaf at most once.
+      const uint32_t max_steps = 2u * (bvh.n_binary + bvh.n_slots) + 8u;
+      uint32_t steps = 0;
+      for (;;) {
+        if (++steps > max_steps) { atomicOr(err, kErrCorrupt); break; }
+        if (cur >= 0) {
+          const float4* nd = bvh.nodes + 8 * (size_t)cur;
+          const float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+          const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+          const int4 lk = __ldg(reinterpret_cast<const int4*>(nd + 6));
+          const int4 ct = __ldg(reinterpret_cast<const int4*>(nd + 7));
+          if (COUNT) ++visits;
+          const float tfar = ANY ? ray.tmax : c.t;
+          float t0, t1, t2, t3;
+          uint32_t k0 = 0xFFFFFFFFu, k1 = 0xFFFFFFFFu, k2 = 0xFFFFFFFFu, k3 = 0xFFFFFFFFu;
+          if (ct.x >= 0 && slab_fast(sr, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, ray.tmin, tfar, t0))
+            k0 = (order_key(t0) & ~3u) | 0u;
+          if (ct.y >= 0 && slab_fast(sr, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, ray.tmin, tfar, t1))
+            k1 = (order_key(t1) & ~3u) | 1u;
+          if (ct.z >= 0 && slab_fast(sr, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, ray.tmin, tfar, t2))
+            k2 = (order_key(t2) & ~3u) | 2u;
+          if (ct.w >= 0 && slab_fast(sr, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, ray.tmin, tfar, t3))
+            k3 = (order_key(t3) & ~3u) | 3u;
+          // A hit key is at most order_key(+inf) | 3 < 0xFFFFFFFF, so misses sort last.
+          const int m = (k0 != 0xFFFFFFFFu) + (k1 != 0xFFFFFFFFu) + (k2 != 0xFFFFFFFFu) + (k3 != 0xFFFFFFFFu);
+          if (m > 0) {
+            cswap(k0, k1);
+            cswap(k2, k3);
+            cswap(k0, k2);
+            cswap(k1, k3);
+            cswap(k1, k2);
+            if (sp + m - 1 > kStack4) { atomicOr(err, kErrStackOverflow); break; }
+            if (m >= 4) stack[sp++] = make_int2(pick(lk, k3 & 3u), pick(ct, k3 & 3u));
+            if (m >= 3) stack[sp++] = make_int2(pick(lk, k2 & 3u), pick(ct, k2 & 3u));
+            if (m >= 2) stack[sp++] = make_int2(pick(lk, k1 & 3u), pick(ct, k1 & 3u));
+            cur = pick(lk, k0 & 3u);
+            cnt = pick(ct, k0 & 3u);
+            continue;
+          }
+        } else {
+          if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, (uint32_t)(~cur), cnt, ray);
+          if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) {
+            occluded = true;
+            break;
+          }
+        }
+        if (sp == 0) break;
+        int2 e = stack[--sp];
+        cur = e.x;
+        cnt = e.y;
+      }
+    }
+    if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  }
+  if (ANY) {
+    if (perm) {
+      if (occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+    } else {
+      uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+      uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+      if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+    }
+  }
+  if (COUNT) {
+    unsigned long long v = visits, t = tests;
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_down_sync(0xffffffffu, v, o);
+      t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(counters, v);
+      atomicAdd(counters + 1, t);
+    }
+  }
+}
+
+template <int KIND, bool ANY>
+void dispatch_bvh4(const Bvh4View& v, const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
+                   uint32_t* err, const uint32_t* perm, unsigned long long* counters, cudaStream_t s) {
+  uint32_t g = (n + kThreads - 1) / kThreads;
+  if (counters)
+    k_trace_bvh4<KIND, ANY, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm, counters);
+  else
+    k_trace_bvh4<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm, nullptr);
+}
+
 // Reference semantics: pre-order, unclipped division slab tests.
 template <int KIND, bool ANY>
 __global__ void __launch_bounds__(kThreads) k_trace_ref(Bvh2View bvh, const float4* __restrict__ rays,
@@ -331,6 +463,21 @@ void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, con
   } else {
     if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, perm, s);
     else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, perm, s);
+  }
+}
+
+void launch_trace_bvh4(int kind, bool any, const Bvh4View& v, const float4* rays, uint32_t n, float4* hits,
+                       uint32_t* occ, uint32_t* err, cudaStream_t s, const uint32_t* perm,
+                       unsigned long long* counters) {
+  if (n == 0) return;
+  count_launch();
+  if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
+  if (kind == kTriangles) {
+    if (any) dispatch_bvh4<kTriangles, true>(v, rays, n, hits, occ, err, perm, counters, s);
+    else dispatch_bvh4<kTriangles, false>(v, rays, n, hits, occ, err, perm, counters, s);
+  } else {
+    if (any) dispatch_bvh4<kSpheres, true>(v, rays, n, hits, occ, err, perm, counters, s);
+    else dispatch_bvh4<kSpheres, false>(v, rays, n, hits, occ, err, perm, counters, s);
   }
 }
 

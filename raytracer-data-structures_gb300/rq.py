@@ -18,6 +18,7 @@ BVH, KDTREE, UNIFORM_GRID, LBVH, NONE = 0, 1, 2, 3, 4
 ACC_NAMES = {"BVH": BVH, "KDTREE": KDTREE, "UNIFORM_GRID": UNIFORM_GRID, "LBVH": LBVH, "NONE": NONE}
 TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
 RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON = 0, 1
+NODE_WIDTH_2, NODE_WIDTH_4 = 0, 4
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1
 DEVICE_POINTERS = 0x1
 MISS = 0xFFFFFFFF
@@ -36,13 +37,14 @@ class Settings(C.Structure):
                 ("backgroundColor", C.c_float * 3), ("bias", C.c_float), ("aa_samples", C.c_uint32),
                 ("dataStructure", C.c_int32), ("sceneModel", C.c_int32), ("traversal", C.c_int32),
                 ("morton", C.c_int32), ("kd_max_depth", C.c_int32), ("ray_sort", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("node_width", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class AccelInfo(C.Structure):
     _fields_ = [("type", C.c_int32), ("prim_kind", C.c_int32), ("n_prims", C.c_uint32),
                 ("n_nodes", C.c_uint32), ("n_slots", C.c_uint32), ("max_depth", C.c_uint32),
-                ("root_bounds", C.c_float * 6), ("device_bytes", C.c_uint64)]
+                ("root_bounds", C.c_float * 6), ("device_bytes", C.c_uint64),
+                ("node_width", C.c_uint32), ("n_wide_nodes", C.c_uint32)]
 
 
 class RqError(RuntimeError):
@@ -89,6 +91,7 @@ def load(build_if_missing=True):
         "rq_accel_get_info": (i32, [vp, vp]),
         "rq_accel_export_bvh2": (i32, [vp, vp, vp, vp, vp]),
         "rq_accel_export_kd": (i32, [vp, vp, vp, vp]),
+        "rq_accel_export_bvh4": (i32, [vp, vp, vp, vp]),
         "rq_trace_closest": (i32, [vp, vp, vp, u32, vp, u32]),
         "rq_trace_any": (i32, [vp, vp, vp, u32, vp, u32]),
         "rq_morton_codes": (i32, [vp, vp, vp, u32]),
@@ -299,6 +302,14 @@ class Engine:
         self._check(load().rq_accel_export_bvh2(self.ctx, accel.handle, nodes.ctypes.data, order.ctypes.data,
                                                 codes.ctypes.data if codes is not None else None))
         return nodes, order, codes, np.array(inf.root_bounds, np.float32), inf
+
+    def export_bvh4(self, accel):
+        """Collapsed 4-wide nodes, (n, 32) float32 (structures built with node_width 4)."""
+        n = C.c_uint32(0)
+        self._check(load().rq_accel_export_bvh4(self.ctx, accel.handle, None, C.byref(n)))
+        nodes = np.zeros((max(n.value, 1), 32), np.float32)
+        self._check(load().rq_accel_export_bvh4(self.ctx, accel.handle, nodes.ctypes.data, C.byref(n)))
+        return nodes[:n.value]
 
     def export_kd(self, accel):
         inf = accel.info()
