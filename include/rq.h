@@ -298,6 +298,44 @@ rq_status_t rq_render_reference(rq_ctx_t ctx, rq_accel_t accel, const rq_setting
                                 const double* jitter, const float* surface_rgb, uint8_t* pixels,
                                 float* rgb_sum);
 
+/* ----------------------------------------------------- render of a view */
+
+/* A pinhole view of any scene (triangles or spheres) with one point light.
+ * The reference renders only its fixed sphere camera (rq_render_reference);
+ * this generalises castRay's shading (main.cpp:390-497) to the triangle
+ * workloads: per sample, at each hit, albedo * (ambient + visible * max(0,
+ * N.L)) with a real shadow ray (the reference's trace_more is a stub), plus
+ * optional mirror bounces; misses add settings.backgroundColor.  Normals face
+ * the incoming ray; shadow and mirror rays start at P + settings.bias * N.
+ * Sample s of pixel (x, y) is jittered by a counter-based generator of
+ * (seed, (y * width + x) * spp + s), so a window reproduces the full image's
+ * pixels exactly. */
+typedef struct rq_view_t {
+  float eye[3];
+  float target[3];
+  float up[3];
+  float fov_deg;        /* vertical field of view, degrees */
+  float light[3];       /* point light position */
+  float albedo[3];      /* surface colour */
+  float ambient;        /* added to max(0, N.L) at every hit */
+  float mirror;         /* reflectance of the mirror bounces, 0..1 */
+  uint32_t bounces;     /* mirror bounces after the camera hit */
+  uint32_t window[4];   /* x0, y0, w, h inside width x height; w or h == 0: the whole image */
+  uint64_t seed;        /* sample jitter */
+} rq_view_t;
+
+/* Render `view` with settings.width x height pixels and settings.aa_samples
+ * samples per pixel through `accel` (any dataStructure; FAST or REFERENCE
+ * traversal and the speed options of the context's settings).  pixels:
+ * w*h*3 bytes (min(1, mean)*255, truncated, as write_into_file,
+ * main.cpp:516-528); rgb (may be NULL): w*h*3 float means before
+ * quantisation; ray_counts (may be NULL, host): camera rays, shadow rays and
+ * mirror rays traced.  RQ_DEVICE_POINTERS: pixels and rgb are device
+ * buffers and the call returns without waiting (ray_counts must then be
+ * NULL).  No reference counterpart beyond the sphere render it generalises. */
+rq_status_t rq_render(rq_ctx_t ctx, rq_accel_t accel, const rq_view_t* view, uint8_t* pixels, float* rgb,
+                      uint64_t* ray_counts, uint32_t flags);
+
 #ifdef __cplusplus
 }
 #endif

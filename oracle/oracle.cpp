@@ -1288,3 +1288,173 @@ void orc_pixels_ref(const float* rgb, uint32_t npix, uint32_t aa, uint8_t* out) 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Render of a view: the engine's rq_render restated (camera, Lambert +
+// ambient with one shadow ray, mirror bounces, pixel resolve).  It
+// generalises castRay's DIFFUSE_AND_GLOSSY shading (main.cpp:390-497) to
+// triangle meshes; every operation is one IEEE single-precision rounding in
+// the engine's order (this file is compiled without contraction).
+
+namespace {
+
+struct F3v {
+  float x, y, z;
+};
+inline F3v fadd(F3v a, F3v b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline F3v fsub(F3v a, F3v b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline F3v fmulv(F3v a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline float fdot(F3v a, F3v b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline F3v fcross(F3v a, F3v b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline F3v fnorm(F3v a) {
+  float n2 = fdot(a, a);
+  if (!(n2 > 0.f)) return a;
+  float inv = 1.0f / std::sqrt(n2);
+  return fmulv(a, inv);
+}
+inline F3v f3(const float* p) { return {p[0], p[1], p[2]}; }
+
+// splitmix64 finaliser (Steele, Lea, Flood 2014), counter-based.
+inline uint64_t mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+inline float jitter01(uint64_t seed, uint64_t sample, uint32_t dim) {
+  uint64_t h = mix64(seed ^ mix64(sample * 2u + dim));
+  return (float)(uint32_t)(h >> 40) * 0x1p-24f;
+}
+
+inline void put_ray(orc_ray_t& r, F3v o, float tmin, F3v d, float tmax) {
+  r.org[0] = o.x; r.org[1] = o.y; r.org[2] = o.z; r.tmin = tmin;
+  r.dir[0] = d.x; r.dir[1] = d.y; r.dir[2] = d.z; r.tmax = tmax;
+}
+inline void put_dead(orc_ray_t& r) { put_ray(r, {0.f, 0.f, 0.f}, 1.f, {0.f, 0.f, 1.f}, 0.f); }
+
+}  // namespace
+
+void orc_view_rays(const orc_view_t* v, orc_ray_t* rays, float* cw) {
+  const uint64_t nray = (uint64_t)v->ww * v->wh * v->spp;
+  const float aspect = (float)v->width / (float)v->height;
+  const F3v eye = f3(v->eye);
+  const F3v fwd = fnorm(fsub(f3(v->target), eye));
+  const F3v right = fnorm(fcross(fwd, f3(v->up)));
+  const F3v upv = fcross(right, fwd);
+  for (uint64_t r = 0; r < nray; ++r) {
+    const uint64_t wp = r / v->spp;
+    const uint32_t s = (uint32_t)(r - wp * v->spp);
+    const uint32_t x = v->x0 + (uint32_t)(wp % v->ww), y = v->y0 + (uint32_t)(wp / v->ww);
+    const uint64_t sample = ((uint64_t)y * v->width + x) * v->spp + s;
+    const float jx = jitter01(v->seed, sample, 0), jy = jitter01(v->seed, sample, 1);
+    const float px = (2.0f * ((float(x) + jx) / float(v->width)) - 1.0f) * v->tan_half * aspect;
+    const float py = (1.0f - 2.0f * ((float(y) + jy) / float(v->height))) * v->tan_half;
+    const F3v d = fnorm(fadd(fadd(fwd, fmulv(right, px)), fmulv(upv, py)));
+    put_ray(rays[r], eye, 0.f, d, INFINITY);
+    cw[4 * r] = cw[4 * r + 1] = cw[4 * r + 2] = 0.f;
+    cw[4 * r + 3] = 1.f;
+  }
+}
+
+void orc_shade_hits(int kind, const float* verts, const uint32_t* idx, const float* sph, const orc_view_t* v,
+                    uint64_t nray, int last, orc_ray_t* rays, const orc_hit_t* hits, orc_ray_t* shadow,
+                    float* cw, float* pend, uint64_t* counters) {
+  const F3v light = f3(v->light), albedo = f3(v->albedo), bg = f3(v->bg);
+  uint64_t n_shadow = 0, n_mirror = 0;
+  for (uint64_t r = 0; r < nray; ++r) {
+    orc_ray_t& ray = rays[r];
+    float* c = cw + 4 * r;
+    float* pe = pend + 4 * r;
+    pe[0] = pe[1] = pe[2] = pe[3] = 0.f;
+    if (!(ray.tmin <= ray.tmax)) {
+      put_dead(shadow[r]);
+      continue;
+    }
+    const orc_hit_t& h = hits[r];
+    const float w = c[3];
+    if (h.prim == kMiss) {
+      c[0] = c[0] + w * bg.x;
+      c[1] = c[1] + w * bg.y;
+      c[2] = c[2] + w * bg.z;
+      c[3] = 0.f;
+      put_dead(ray);
+      put_dead(shadow[r]);
+      continue;
+    }
+    const F3v o = f3(ray.org), d = f3(ray.dir);
+    const F3v p = fadd(o, fmulv(d, h.t));
+    F3v n;
+    if (kind == ORC_TRIANGLES) {
+      const uint32_t* t = idx + 3 * (size_t)h.prim;
+      const F3v a = f3(verts + 3 * (size_t)t[0]), b = f3(verts + 3 * (size_t)t[1]), cc = f3(verts + 3 * (size_t)t[2]);
+      n = fnorm(fcross(fsub(b, a), fsub(cc, a)));
+    } else {
+      n = fnorm(fsub(p, f3(sph + 4 * (size_t)h.prim)));
+    }
+    if (fdot(n, d) > 0.f) n = {-n.x, -n.y, -n.z};
+    const F3v lv = fsub(light, p);
+    const float dist = std::sqrt(fdot(lv, lv));
+    const F3v ld = fmulv(lv, 1.0f / dist);
+    const float ndl = fdot(n, ld);
+    const float f = last ? w : w * (1.0f - v->mirror);
+    const F3v fa = fmulv(albedo, f);
+    c[0] = c[0] + fa.x * v->ambient;
+    c[1] = c[1] + fa.y * v->ambient;
+    c[2] = c[2] + fa.z * v->ambient;
+    const F3v po = fadd(p, fmulv(n, v->bias));
+    if (ndl > 0.f && dist > 0.f) {
+      pe[0] = fa.x * ndl;
+      pe[1] = fa.y * ndl;
+      pe[2] = fa.z * ndl;
+      put_ray(shadow[r], po, 0.f, ld, dist);
+      ++n_shadow;
+    } else {
+      put_dead(shadow[r]);
+    }
+    const float wn = w * v->mirror;
+    bool mirror = false;
+    if (!last && wn > 0.f) {
+      const F3v rd = fsub(d, fmulv(n, 2.0f * fdot(d, n)));
+      put_ray(ray, po, 0.f, rd, INFINITY);
+      mirror = true;
+      ++n_mirror;
+    } else {
+      put_dead(ray);
+    }
+    c[3] = mirror ? wn : 0.f;
+  }
+  if (counters) {
+    counters[0] += n_shadow;
+    counters[1] += n_mirror;
+  }
+}
+
+void orc_shadow_accum(uint64_t nray, const uint8_t* occluded, const float* pend, float* cw) {
+  for (uint64_t r = 0; r < nray; ++r) {
+    const float* p = pend + 4 * r;
+    if (p[0] == 0.f && p[1] == 0.f && p[2] == 0.f) continue;
+    if (occluded[r]) continue;
+    cw[4 * r] = cw[4 * r] + p[0];
+    cw[4 * r + 1] = cw[4 * r + 1] + p[1];
+    cw[4 * r + 2] = cw[4 * r + 2] + p[2];
+  }
+}
+
+void orc_view_pixels(uint64_t npix, uint32_t spp, const float* cw, uint8_t* pixels, float* rgb) {
+  for (uint64_t p = 0; p < npix; ++p) {
+    float s[3] = {0.f, 0.f, 0.f};
+    for (uint32_t k = 0; k < spp; ++k) {
+      const float* c = cw + 4 * (p * spp + k);
+      s[0] = s[0] + c[0];
+      s[1] = s[1] + c[1];
+      s[2] = s[2] + c[2];
+    }
+    const float fs = (float)spp;
+    for (int q = 0; q < 3; ++q) {
+      float m = s[q] / fs;
+      if (rgb) rgb[3 * p + q] = m;
+      m = m < 1.f ? (m > 0.f ? m : 0.f) : 1.f;
+      pixels[3 * p + q] = (uint8_t)(m * 255.f);
+    }
+  }
+}

@@ -118,6 +118,25 @@ void orc_shade_ref(const float* sph, const float* surface_rgb, const orc_ray_t* 
                    float* rgb);
 void orc_pixels_ref(const float* rgb, uint32_t npix, uint32_t aa, uint8_t* out);
 
+/* ---- render of a view (the engine's rq_render; restated, no reference
+ * counterpart beyond castRay's shading, main.cpp:390-497) ---- */
+typedef struct {
+  float eye[3], target[3], up[3], light[3], albedo[3], bg[3];
+  float tan_half, ambient, mirror, bias;
+  uint32_t width, height, spp, x0, y0, ww, wh, bounces;
+  uint64_t seed;
+} orc_view_t;
+/* rays: ww*wh*spp camera rays; cw: 4 floats per ray (colour, weight). */
+void orc_view_rays(const orc_view_t* v, orc_ray_t* rays, float* cw);
+/* One depth: reads hits of `rays`, writes shadow rays and the next mirror
+ * rays (into rays), updates cw, writes pend (4 floats per ray).  counters
+ * (may be NULL): [0] += shadow rays, [1] += mirror rays. */
+void orc_shade_hits(int kind, const float* verts, const uint32_t* idx, const float* sph,
+                    const orc_view_t* v, uint64_t nray, int last, orc_ray_t* rays, const orc_hit_t* hits,
+                    orc_ray_t* shadow, float* cw, float* pend, uint64_t* counters);
+void orc_shadow_accum(uint64_t nray, const uint8_t* occluded, const float* pend, float* cw);
+void orc_view_pixels(uint64_t npix, uint32_t spp, const float* cw, uint8_t* pixels, float* rgb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -334,3 +334,59 @@ def reference_surface_colors(n_spheres):
     c = np.tile(np.array([0.8, 0.7, 0.0], np.float32), (n_spheres, 1))
     c[-1] = 0.0
     return c
+
+
+# ---------------------------------------------------------- render of a view
+
+class View(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("light", C.c_float * 3), ("albedo", C.c_float * 3), ("bg", C.c_float * 3),
+                ("tan_half", C.c_float), ("ambient", C.c_float), ("mirror", C.c_float), ("bias", C.c_float),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("x0", C.c_uint32),
+                ("y0", C.c_uint32), ("ww", C.c_uint32), ("wh", C.c_uint32), ("bounces", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+def make_view(width, height, spp, eye, target, up, fov_deg, light, albedo, ambient=0.1, mirror=0.0,
+              bounces=0, window=(0, 0, 0, 0), seed=1, bg=(1.0, 1.0, 1.0), bias=1e-4):
+    """The engine's view parameters (tan of half the fov in double, rounded once)."""
+    v = View()
+    v.eye[:], v.target[:], v.up[:] = eye, target, up
+    v.light[:], v.albedo[:], v.bg[:] = light, albedo, bg
+    v.tan_half = float(np.float32(np.tan(np.float64(np.float32(fov_deg)) * 3.141592653589793 / 360.0)))
+    v.ambient, v.mirror, v.bias = ambient, mirror, float(np.float32(bias))
+    v.width, v.height, v.spp, v.bounces, v.seed = width, height, spp, bounces, seed
+    whole = window[2] == 0 or window[3] == 0
+    v.x0, v.y0 = (0, 0) if whole else window[:2]
+    v.ww, v.wh = (width, height) if whole else window[2:]
+    return v
+
+
+def render_view(kind, view, closest, anyhit, verts=None, idx=None, sph=None):
+    """Oracle render: closest(rays) -> hits and anyhit(rays) -> uint8 mask are
+    the oracle traversals of the structure under test.  Returns (pixels
+    (h, w, 3) uint8, rgb (h, w, 3) float32, ray counts [camera, shadow, mirror])."""
+    L = lib()
+    nray = view.ww * view.wh * view.spp
+    npix = view.ww * view.wh
+    rays = np.zeros(nray, RAY_DTYPE)
+    shadow = np.zeros(nray, RAY_DTYPE)
+    cw = np.zeros((nray, 4), np.float32)
+    pend = np.zeros((nray, 4), np.float32)
+    cnt = np.zeros(2, np.uint64)
+    L.orc_view_rays(C.byref(view), _p(rays), _p(cw))
+    vv = _c(verts, np.float32) if verts is not None else np.zeros(3, np.float32)
+    ii = _c(idx, np.uint32) if idx is not None else np.zeros(3, np.uint32)
+    ss = _c(sph, np.float32) if sph is not None else np.zeros(4, np.float32)
+    for depth in range(view.bounces + 1):
+        hits = np.ascontiguousarray(closest(rays), HIT_DTYPE)
+        L.orc_shade_hits(C.c_int(kind), _p(vv), _p(ii), _p(ss), C.byref(view), C.c_uint64(nray),
+                         C.c_int(int(depth == view.bounces)), _p(rays), _p(hits), _p(shadow), _p(cw), _p(pend),
+                         _p(cnt))
+        occ = np.ascontiguousarray(anyhit(shadow), np.uint8)
+        L.orc_shadow_accum(C.c_uint64(nray), _p(occ), _p(pend), _p(cw))
+    pix = np.zeros((npix, 3), np.uint8)
+    rgb = np.zeros((npix, 3), np.float32)
+    L.orc_view_pixels(C.c_uint64(npix), C.c_uint32(view.spp), _p(cw), _p(pix), _p(rgb))
+    return (pix.reshape(view.wh, view.ww, 3), rgb.reshape(view.wh, view.ww, 3),
+            np.array([nray, cnt[0], cnt[1]], np.uint64))

@@ -26,6 +26,7 @@ struct rq_context {
   int sm_count = 0;
   DevBuf stage_in, stage_out, stage_aux;
   BuildScratch scratch;
+  RenderScratch render;
 };
 
 struct rq_scene {
@@ -191,6 +192,7 @@ rq_status_t rq_destroy(rq_ctx_t ctx) {
   ctx->stage_out.release();
   ctx->stage_aux.release();
   ctx->scratch.release();
+  ctx->render.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -647,12 +649,64 @@ rq_status_t rq_render_reference(rq_ctx_t ctx, rq_accel_t a, const rq_settings_t*
   // the same double-precision tan the reference calls.
   float fov = 30, aspect = s.width / float(s.height);
   float angle = (float)std::tan(3.141592653589793 * 0.5 * fov / 180.);
-  RenderBuffers rb;
   cudaError_t e = render_reference(a->type, scene_view(a->scene), a->buf, s, angle, aspect, jitter,
                                    surface_rgb, ctx->stage_in, ctx->stage_out, ctx->stage_aux,
                                    pixels, rgb_sum, ctx->d_err, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
   return collect_device_errors(ctx);
+}
+
+rq_status_t rq_render(rq_ctx_t ctx, rq_accel_t a, const rq_view_t* view, uint8_t* pixels, float* rgb,
+                      uint64_t* ray_counts, uint32_t flags) {
+  RQ_TRY(bind(ctx));
+  if (!a || !view || !pixels) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel, view or pixels");
+  const rq_settings_t& s = ctx->settings;
+  const bool dev = (flags & RQ_DEVICE_POINTERS) != 0;
+  if (dev && ray_counts) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "ray_counts needs a synchronous call");
+  if (s.width == 0 || s.height == 0 || s.aa_samples == 0) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "empty image");
+  const bool whole = view->window[2] == 0 || view->window[3] == 0;
+  const uint64_t ww = whole ? s.width : view->window[2], wh = whole ? s.height : view->window[3];
+  if (!whole && ((uint64_t)view->window[0] + ww > s.width || (uint64_t)view->window[1] + wh > s.height))
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "window outside the image");
+  const uint64_t npix = ww * wh, nray = npix * s.aa_samples;
+  if (nray >= (1ull << 31)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "image too large (2^31 samples)");
+  const float geo[] = {view->eye[0], view->eye[1], view->eye[2], view->target[0], view->target[1],
+                       view->target[2], view->up[0], view->up[1], view->up[2], view->light[0],
+                       view->light[1], view->light[2], view->albedo[0], view->albedo[1], view->albedo[2],
+                       view->ambient, view->mirror, view->fov_deg};
+  if (!finite3(geo, sizeof(geo) / sizeof(geo[0])) || !(view->fov_deg > 0.f && view->fov_deg < 180.f) ||
+      !(view->mirror >= 0.f && view->mirror <= 1.f))
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "view: non-finite values, fov outside (0, 180) or mirror outside [0, 1]");
+  // tan of half the field of view, in double on the host, then rounded once
+  const float tan_half = (float)std::tan((double)view->fov_deg * 3.141592653589793 / 360.0);
+  RenderScratch& rs = ctx->render;
+  uint8_t* d_pix = pixels;
+  float* d_rgb = rgb;
+  if (!dev) {
+    const size_t pix_bytes = (npix * 3 + 255) & ~size_t(255);
+    RQ_TRY_CUDA(ctx, rs.out.ensure(pix_bytes + (rgb ? npix * 12 : 0)));
+    d_pix = rs.out.as<uint8_t>();
+    d_rgb = rgb ? reinterpret_cast<float*>(rs.out.as<char>() + pix_bytes) : nullptr;
+  }
+  RQ_TRY_CUDA(ctx, rs.counters.ensure(16));
+  RQ_TRY_CUDA(ctx, cudaMemsetAsync(rs.counters.p, 0, 16, ctx->stream));
+  rq_status_t est = RQ_SUCCESS;
+  cudaError_t e = render_view(a->type, scene_view(a->scene), a->buf, s, *view, tan_half, rs, ctx->scratch, d_pix,
+                              d_rgb, rs.counters.as<unsigned long long>(), ctx->d_err, ctx->stream, &est);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
+  if (est != RQ_SUCCESS) return fail(ctx, est, "render query");
+  if (dev) return RQ_SUCCESS;
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(pixels, d_pix, npix * 3, cudaMemcpyDeviceToHost, ctx->stream));
+  if (rgb) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(rgb, d_rgb, npix * 12, cudaMemcpyDeviceToHost, ctx->stream));
+  uint64_t cnt[2] = {0, 0};
+  if (ray_counts) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(cnt, rs.counters.p, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  RQ_TRY(collect_device_errors(ctx));
+  if (ray_counts) {
+    ray_counts[0] = nray;
+    ray_counts[1] = cnt[0];
+    ray_counts[2] = cnt[1];
+  }
+  return RQ_SUCCESS;
 }
 
 }  // extern "C"

@@ -117,7 +117,21 @@ BuildResult trace_counted(int type, const SceneView& s, const AccelBuffers& a, b
 void launch_validate(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt,
                      const float4* sph, uint32_t n, uint32_t* err, cudaStream_t st);
 
-struct RenderBuffers {};
+// Working arrays of rq_render (grow-only, per context).
+struct RenderScratch {
+  DevBuf rays, shadow, hits, cw, pend, bits, out, counters;
+  void release() {
+    rays.release(); shadow.release(); hits.release(); cw.release(); pend.release(); bits.release();
+    out.release(); counters.release();
+  }
+};
+// Wavefront render of `view` into device buffers pixels (3 B per pixel) and
+// rgb (3 floats per pixel, may be null); counters (2 x u64, device) gain the
+// shadow and mirror rays emitted.  *status reports engine errors.
+cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, const rq_settings_t& cfg,
+                        const rq_view_t& view, float tan_half, RenderScratch& rs, BuildScratch& sc,
+                        uint8_t* pixels, float* rgb, unsigned long long* counters, uint32_t* err,
+                        cudaStream_t st, rq_status_t* status);
 cudaError_t render_reference(int type, const SceneView& s, const AccelBuffers& a,
                              const rq_settings_t& settings, float angle, float aspect,
                              const double* jitter_host, const float* surface_rgb_host,

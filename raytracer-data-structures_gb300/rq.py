@@ -47,6 +47,24 @@ class AccelInfo(C.Structure):
                 ("node_width", C.c_uint32), ("n_wide_nodes", C.c_uint32)]
 
 
+class View(C.Structure):
+    """rq_view_t: a pinhole view with one point light (rq_render)."""
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_deg", C.c_float), ("light", C.c_float * 3), ("albedo", C.c_float * 3),
+                ("ambient", C.c_float), ("mirror", C.c_float), ("bounces", C.c_uint32),
+                ("window", C.c_uint32 * 4), ("seed", C.c_uint64)]
+
+
+def make_view(eye, target, up=(0, 0, 1), fov_deg=40.0, light=(0, 0, 10), albedo=(0.8, 0.8, 0.8),
+              ambient=0.1, mirror=0.0, bounces=0, window=(0, 0, 0, 0), seed=1):
+    v = View()
+    v.eye[:], v.target[:], v.up[:] = eye, target, up
+    v.fov_deg, v.light[:], v.albedo[:] = fov_deg, light, albedo
+    v.ambient, v.mirror, v.bounces, v.seed = ambient, mirror, bounces, seed
+    v.window[:] = window
+    return v
+
+
 class RqError(RuntimeError):
     def __init__(self, status, message):
         self.status = status
@@ -100,6 +118,7 @@ def load(build_if_missing=True):
         "rq_trace_counters": (i32, [vp, vp, vp, u32, i32, vp, vp, u32]),
         "rq_kernel_launch_count": (C.c_uint64, []),
         "rq_sort_pairs_noalloc": (i32, [vp, vp, u32, u32, vp]),
+        "rq_render": (i32, [vp, vp, vp, vp, vp, vp, u32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -329,6 +348,26 @@ class Engine:
                                                jit.ctypes.data if jit is not None else None,
                                                srgb.ctypes.data, pixels.ctypes.data, rgb.ctypes.data))
         return pixels, rgb.reshape(-1, 3)
+
+
+    def render(self, accel, view, pixels=None, rgb=None):
+        """rq_render.  Host arrays (allocated when None): returns (pixels (h, w, 3) uint8,
+        rgb (h, w, 3) float32, ray counts [camera, shadow, mirror]).  Device tensors for
+        pixels (and rgb): enqueued without waiting; returns (pixels, rgb, None)."""
+        s = self.settings
+        whole = view.window[2] == 0 or view.window[3] == 0
+        w, h = (s.width, s.height) if whole else (view.window[2], view.window[3])
+        if pixels is not None and not isinstance(pixels, np.ndarray):
+            pp, fl = _ptr(pixels)
+            pr, _ = _ptr(rgb)
+            self._check(load().rq_render(self.ctx, accel.handle, C.byref(view), pp, pr, None, fl))
+            return pixels, rgb, None
+        pixels = np.zeros((h, w, 3), np.uint8)
+        rgb = np.zeros((h, w, 3), np.float32)
+        cnt = np.zeros(3, np.uint64)
+        self._check(load().rq_render(self.ctx, accel.handle, C.byref(view), pixels.ctypes.data, rgb.ctypes.data,
+                                     cnt.ctypes.data, 0))
+        return pixels, rgb, cnt
 
 
 SORT_NOALLOC_MAX_PAIRS = 1 << 20

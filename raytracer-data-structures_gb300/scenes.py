@@ -105,6 +105,22 @@ def displaced_icosphere(level=6, amplitude=0.15, octaves=3, seed=1, unit_cube=Tr
     return v.astype(np.float32), f.astype(np.uint32)
 
 
+def c1_mesh(seed=1):
+    """The small plain workload's mesh: 81,920-triangle displaced icosphere
+    (level 6, 3-octave value noise, amplitude 0.15) scaled into the unit cube
+    and centred on the origin."""
+    v, f = displaced_icosphere(6, seed=seed)
+    v = v - (v.min(0) + v.max(0)) / 2
+    return v.astype(np.float32), f
+
+
+# The small plain workload's view: 640x480, 1 spp, pinhole at (0, 0, 3)
+# looking at the origin, 40 degree vertical field of view, one point light,
+# Lambert shading with one shadow ray, white background.
+C1_VIEW = dict(eye=(0.0, 0.0, 3.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov_deg=40.0,
+               light=(2.0, 3.0, 4.0), albedo=(0.8, 0.75, 0.7), ambient=0.1, mirror=0.0, bounces=0, seed=11)
+
+
 def heightfield(nx=1001, ny=500, amplitude=0.3, octaves=5, seed=2):
     """(nx-1)*(ny-1)*2 triangles; 1001 x 500 gives 998,000."""
     x = np.linspace(-1.0, 1.0, nx)
