@@ -335,6 +335,10 @@ def run_ours(args):
                                 "nodes": int(inf.n_nodes)}
             other.close()
 
+    render = None
+    if not args.skip_render:
+        render = run_render_legs(eng, stream, dev, args)
+
     e2e = None
     if rank == 0 and not args.skip_e2e:
         e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice)
@@ -366,12 +370,75 @@ def run_ours(args):
                                "unit": "GB/s", "bytes_per_tri": build_bytes_per_tri(),
                                "frac": round(build_bytes / (build_ms * 1e-3) / 1e9 / peak, 4)},
             "structures": structures,
+            "render": render,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),
         }
         print(json.dumps(out), flush=True)
     eng.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_render_legs(eng, stream, dev, args):
+    """The render step (rq_render) on the small plain workload (81,920-triangle
+    icosphere, 640x480, 1 spp, Lambert + shadow ray; BVH, KDTREE and LBVH) and
+    the large one (~10M-triangle merged icospheres, 3840x2160, 4 spp, shadow ray
+    + 2 mirror bounces; LBVH).  Each timed frame = structure rebuild + render
+    into device buffers, L2 flushed before it; rays = camera + shadow + mirror
+    rays actually traced (the engine's counts)."""
+    import torch
+    import rq
+    import scenes
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    saved = eng.settings
+    out = {}
+
+    def leg(verts, idx, structures, width, height, spp, view_kw, frames):
+        eng.configure(width=width, height=height, aa_samples=spp, ray_sort=rq.RAY_SORT_NONE)
+        dv = torch.from_numpy(verts).to(dev)
+        di = torch.from_numpy(idx.view(np.int32)).to(dev)
+        scene = eng.scene_triangles(dv, di)
+        view = rq.make_view(**view_kw)
+        pix = torch.empty(width * height * 3, dtype=torch.uint8, device=dev)
+        res = {"triangles": int(len(idx)), "image": f"{width}x{height}x{spp}", "bounces": view_kw["bounces"]}
+        for name in structures:
+            acc = eng.build(scene, name)
+            _, _, cnt = eng.render(acc, view)  # synchronous: the ray counts
+            rays = int(cnt.sum())
+            for _ in range(2):
+                acc.rebuild()
+                eng.render(acc, view, pix)
+            times, rtimes = [], []
+            for _ in range(frames):
+                flush.zero_()
+                m = [ev() for _ in range(3)]
+                m[0].record(stream)
+                acc.rebuild()
+                m[1].record(stream)
+                eng.render(acc, view, pix)
+                m[2].record(stream)
+                torch.cuda.synchronize(dev)
+                times.append(m[0].elapsed_time(m[2]))
+                rtimes.append(m[1].elapsed_time(m[2]))
+            eng.synchronize()
+            t, tr = float(np.mean(times)), float(np.mean(rtimes))
+            res[name] = {"frame_ms": round(t, 3), "render_ms": round(tr, 3), "build_ms": round(t - tr, 3),
+                         "rays": rays, "ray_counts": [int(c) for c in cnt],
+                         "grays_s": round(rays / (t * 1e-3) / 1e9, 4)}
+            acc.close()
+        scene.close()
+        return res
+
+    v1, f1 = scenes.c1_mesh()
+    out["c1"] = leg(v1, f1, ("BVH", "KDTREE", "LBVH"), 640, 480, 1, scenes.C1_VIEW, 10)
+    if not args.small:
+        v3, f3, _ = scenes.merged_icospheres()
+        out["c3"] = leg(v3, f3, ("LBVH",), 3840, 2160, 4, scenes.C3_VIEW, 3)
+    eng.settings = saved
+    log(f"[bench] render: {out}")
+    return out
 
 
 def build_bytes_per_tri():
@@ -549,6 +616,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--small", action="store_true", help="960x540x4 rays (profiling case)")
     ap.add_argument("--skip-structures", action="store_true", help="skip the BVH / KDTREE comparison")
+    ap.add_argument("--skip-render", action="store_true", help="skip the render-step legs")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

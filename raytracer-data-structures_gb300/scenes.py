@@ -121,6 +121,13 @@ C1_VIEW = dict(eye=(0.0, 0.0, 3.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), 
                light=(2.0, 3.0, 4.0), albedo=(0.8, 0.75, 0.7), ambient=0.1, mirror=0.0, bounces=0, seed=11)
 
 
+# The large workload's view of merged_icospheres() (150 displaced icospheres
+# in [-4, 4]^3): 3840x2160, 4 spp, one shadow ray per hit and two mirror
+# bounces.
+C3_VIEW = dict(eye=(0.0, -12.0, 5.0), target=(0.0, 0.0, 0.0), up=(0.0, 0.0, 1.0), fov_deg=50.0,
+               light=(6.0, -8.0, 10.0), albedo=(0.75, 0.7, 0.65), ambient=0.05, mirror=0.5, bounces=2, seed=33)
+
+
 def heightfield(nx=1001, ny=500, amplitude=0.3, octaves=5, seed=2):
     """(nx-1)*(ny-1)*2 triangles; 1001 x 500 gives 998,000."""
     x = np.linspace(-1.0, 1.0, nx)
