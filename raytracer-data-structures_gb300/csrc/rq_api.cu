@@ -2,6 +2,7 @@
 // and the ray queries, over the kernels of the other translation units.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -16,6 +17,53 @@
 
 using namespace rq;
 
+// Host-buffer queries of at least 2 chunks are streamed: chunk k+1 uploads
+// (one copy stream) and chunk k-1 downloads (another) while chunk k is traced.
+// Chunks alternate between two compute lanes (the context's stream and one
+// more, each with its own sort scratch) so that the slow tail of one chunk's
+// traversal overlaps the start of the next.
+constexpr uint32_t kPipeChunk = 1u << 21;  // rays per chunk: 64 MB up, 32 MB (or 256 KB of bits) down
+constexpr int kPipeSlots = 3;
+struct HostPipe {
+  cudaStream_t up = nullptr, down = nullptr, lane2 = nullptr;
+  BuildScratch scratch2;
+  cudaEvent_t start = nullptr, uploaded[kPipeSlots] = {}, traced[kPipeSlots] = {}, downloaded[kPipeSlots] = {};
+  DevBuf rays[kPipeSlots], out[kPipeSlots];
+  bool ready = false;
+  cudaError_t init() {
+    if (ready) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&lane2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    for (int k = 0; k < kPipeSlots && e == cudaSuccess; ++k) {
+      e = cudaEventCreateWithFlags(&uploaded[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&traced[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&downloaded[k], cudaEventDisableTiming);
+    }
+    ready = e == cudaSuccess;
+    return e;
+  }
+  void release() {
+    for (int k = 0; k < kPipeSlots; ++k) {
+      rays[k].release();
+      out[k].release();
+      if (uploaded[k]) cudaEventDestroy(uploaded[k]);
+      if (traced[k]) cudaEventDestroy(traced[k]);
+      if (downloaded[k]) cudaEventDestroy(downloaded[k]);
+      uploaded[k] = traced[k] = downloaded[k] = nullptr;
+    }
+    if (start) cudaEventDestroy(start);
+    if (up) cudaStreamDestroy(up);
+    if (down) cudaStreamDestroy(down);
+    if (lane2) cudaStreamDestroy(lane2);
+    scratch2.release();
+    start = nullptr;
+    up = down = lane2 = nullptr;
+    ready = false;
+  }
+};
+
 struct rq_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -27,6 +75,7 @@ struct rq_context {
   DevBuf stage_in, stage_out, stage_aux;
   BuildScratch scratch;
   RenderScratch render;
+  HostPipe pipe;
 };
 
 struct rq_scene {
@@ -193,6 +242,7 @@ rq_status_t rq_destroy(rq_ctx_t ctx) {
   ctx->stage_aux.release();
   ctx->scratch.release();
   ctx->render.release();
+  ctx->pipe.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -241,11 +291,6 @@ rq_status_t rq_scene_create_triangles(rq_ctx_t ctx, const float* verts, uint32_t
   if (nt == 0) return fail(ctx, RQ_ERROR_EMPTY_SCENE, "scene has no triangles");
   if (!verts || !idx || nv == 0) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null vertex or index buffer");
   if (nt >= (1u << 30)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "2^30 or more triangles");
-  if (!(flags & RQ_DEVICE_POINTERS)) {
-    if (!finite3(verts, (size_t)nv * 3)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "non-finite vertex");
-    for (size_t i = 0; i < (size_t)nt * 3; ++i)
-      if (idx[i] >= nv) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "triangle index out of range");
-  }
   rq_scene* s = new (std::nothrow) rq_scene();
   if (!s) return RQ_ERROR_OUT_OF_MEMORY;
   s->ctx = ctx;
@@ -257,7 +302,7 @@ rq_status_t rq_scene_create_triangles(rq_ctx_t ctx, const float* verts, uint32_t
   if (e == cudaSuccess) e = s->idx.ensure((size_t)nt * 12);
   if (e == cudaSuccess) e = cudaMemcpyAsync(s->verts.p, verts, (size_t)nv * 12, k, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(s->idx.p, idx, (size_t)nt * 12, k, ctx->stream);
-  if (e == cudaSuccess && (flags & RQ_DEVICE_POINTERS)) {
+  if (e == cudaSuccess) {  // finite vertices, indices < nv: checked on the device
     launch_validate(s->verts.as<float>(), nv, s->idx.as<uint32_t>(), nt, nullptr, 0, ctx->d_err, ctx->stream);
     e = cudaGetLastError();
   }
@@ -287,11 +332,6 @@ rq_status_t rq_scene_create_spheres(rq_ctx_t ctx, const float* sph, uint32_t n, 
   if (n == 0) return fail(ctx, RQ_ERROR_EMPTY_SCENE, "scene has no spheres");
   if (!sph) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null sphere buffer");
   if (n >= (1u << 30)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "2^30 or more spheres");
-  if (!(flags & RQ_DEVICE_POINTERS)) {
-    if (!finite3(sph, (size_t)n * 4)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "non-finite sphere");
-    for (size_t i = 0; i < n; ++i)
-      if (sph[4 * i + 3] < 0.f) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "negative sphere radius");
-  }
   rq_scene* s = new (std::nothrow) rq_scene();
   if (!s) return RQ_ERROR_OUT_OF_MEMORY;
   s->ctx = ctx;
@@ -300,7 +340,7 @@ rq_status_t rq_scene_create_spheres(rq_ctx_t ctx, const float* sph, uint32_t n, 
   cudaMemcpyKind k = (flags & RQ_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   cudaError_t e = s->sph.ensure((size_t)n * 16);
   if (e == cudaSuccess) e = cudaMemcpyAsync(s->sph.p, sph, (size_t)n * 16, k, ctx->stream);
-  if (e == cudaSuccess && (flags & RQ_DEVICE_POINTERS)) {
+  if (e == cudaSuccess) {  // finite, radius >= 0: checked on the device
     launch_validate(nullptr, 0, nullptr, 0, s->sph.as<float4>(), n, ctx->d_err, ctx->stream);
     e = cudaGetLastError();
   }
@@ -325,25 +365,33 @@ rq_status_t rq_scene_update(rq_ctx_t ctx, rq_scene_t s, const float* data, const
   if (!s || !data) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null scene or data");
   RQ_TRY(bind(ctx));
   const bool dev = flags & RQ_DEVICE_POINTERS;
-  size_t bytes = s->kind == kTriangles ? (size_t)s->nv * 12 : (size_t)s->n * 16;
-  if (!dev && !finite3(data, bytes / 4)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "non-finite coordinate");
-  if (idx && s->kind == kTriangles && !dev)
-    for (size_t i = 0; i < (size_t)s->n * 3; ++i)
-      if (idx[i] >= s->nv) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "triangle index out of range");
-  void* dst = s->kind == kTriangles ? s->verts.p : s->sph.p;
-  cudaMemcpyKind k = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dst, data, bytes, k, ctx->stream));
-  if (idx && s->kind == kTriangles)
-    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(s->idx.p, idx, (size_t)s->n * 12, k, ctx->stream));
+  const bool tri = s->kind == kTriangles;
+  const size_t bytes = tri ? (size_t)s->nv * 12 : (size_t)s->n * 16;
+  const size_t idx_bytes = (idx && tri) ? (size_t)s->n * 12 : 0;
+  void* dst = tri ? s->verts.p : s->sph.p;
   if (dev) {
-    launch_validate(s->kind == kTriangles ? s->verts.as<float>() : nullptr, s->kind == kTriangles ? s->nv : 0,
-                    (idx && s->kind == kTriangles) ? s->idx.as<uint32_t>() : nullptr,
-                    (idx && s->kind == kTriangles) ? s->n : 0, s->kind == kSpheres ? s->sph.as<float4>() : nullptr,
-                    s->kind == kSpheres ? s->n : 0, ctx->d_err, ctx->stream);
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dst, data, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (idx_bytes) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(s->idx.p, idx, idx_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch_validate(tri ? s->verts.as<float>() : nullptr, tri ? s->nv : 0, idx_bytes ? s->idx.as<uint32_t>() : nullptr,
+                    idx_bytes ? s->n : 0, tri ? nullptr : s->sph.as<float4>(), tri ? 0 : s->n, ctx->d_err, ctx->stream);
     RQ_TRY(check_launch(ctx, "validate launch"));
     return RQ_SUCCESS;  // device-side validation result arrives with rq_synchronize
   }
-  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  // Host data: upload to a staging buffer, validate there on the device, and
+  // only then replace the scene's geometry, so a rejected update leaves the
+  // scene as it was.
+  const size_t off = (bytes + 255) & ~size_t(255);
+  RQ_TRY_CUDA(ctx, ctx->stage_aux.ensure(off + idx_bytes));
+  char* st = ctx->stage_aux.as<char>();
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(st, data, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  if (idx_bytes) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(st + off, idx, idx_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  launch_validate(tri ? reinterpret_cast<const float*>(st) : nullptr, tri ? s->nv : 0,
+                  idx_bytes ? reinterpret_cast<const uint32_t*>(st + off) : nullptr, idx_bytes ? s->n : 0,
+                  tri ? nullptr : reinterpret_cast<const float4*>(st), tri ? 0 : s->n, ctx->d_err, ctx->stream);
+  RQ_TRY(check_launch(ctx, "validate launch"));
+  RQ_TRY(collect_device_errors(ctx));
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dst, st, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (idx_bytes) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(s->idx.p, st + off, idx_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   return RQ_SUCCESS;
 }
 
@@ -498,6 +546,89 @@ rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t a, int32_t* nodes, int32
 
 // ----------------------------------------------------------------- queries
 
+// Streamed query over host buffers: per chunk, upload on pipe.up, trace on
+// the context's stream, download on pipe.down, with kPipeSlots device slots
+// in rotation (a slot is re-filled only after its previous download).
+static rq_status_t trace_streamed_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n,
+                                          void* out, bool any) {
+  HostPipe& p = ctx->pipe;
+  RQ_TRY_CUDA(ctx, p.init());
+  const size_t out_chunk = any ? kPipeChunk / 8 : (size_t)kPipeChunk * 16;
+  for (int k = 0; k < kPipeSlots; ++k) {
+    RQ_TRY_CUDA(ctx, p.rays[k].ensure((size_t)kPipeChunk * 32));
+    RQ_TRY_CUDA(ctx, p.out[k].ensure(out_chunk));
+  }
+  // copies start after everything already queued on the context's stream
+  RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, p.start, 0));
+  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.down, p.start, 0));
+  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.lane2, p.start, 0));
+  const SceneView sv = scene_view(a->scene);
+  // Chunk plan: a quarter and a half chunk first (a short first upload), full
+  // chunks, then halving chunks at the end (a short last traversal and
+  // download).  Every chunk but the last is a multiple of 32 rays, so
+  // occlusion words never straddle chunks.
+  std::vector<uint32_t> plan;
+  for (uint64_t left = n; left > 0;) {
+    uint64_t size = plan.empty() ? kPipeChunk / 4 : plan.size() == 1 ? kPipeChunk / 2 : kPipeChunk;
+    if (left <= 2ull * kPipeChunk) {
+      uint64_t half = (left / 2) & ~uint64_t(31);
+      size = std::min<uint64_t>(size, std::max<uint64_t>(kPipeChunk / 4, half));
+    }
+    size = std::min<uint64_t>(size, left);
+    plan.push_back((uint32_t)size);
+    left -= size;
+  }
+  uint64_t first = 0;
+  for (uint32_t c = 0; c < (uint32_t)plan.size(); first += plan[c], ++c) {
+    const int sl = (int)(c % kPipeSlots);
+    const uint32_t m = plan[c];
+    if (c >= (uint32_t)kPipeSlots) RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, p.downloaded[sl], 0));
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(p.rays[sl].p, rays + first, (size_t)m * 32, cudaMemcpyHostToDevice, p.up));
+    RQ_TRY_CUDA(ctx, cudaEventRecord(p.uploaded[sl], p.up));
+    cudaStream_t lane = (c & 1) ? p.lane2 : ctx->stream;
+    BuildScratch& lane_scratch = (c & 1) ? p.scratch2 : ctx->scratch;
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(lane, p.uploaded[sl], 0));
+    QueryTarget q;
+    q.rays = p.rays[sl].as<const float4>();
+    q.n = m;
+    q.hits = any ? nullptr : p.out[sl].as<float4>();
+    q.occ = any ? p.out[sl].as<uint32_t>() : nullptr;
+    BuildResult br = launch_query_sorted(a->type, sv, a->buf, ctx->settings, any, q, lane_scratch, ctx->d_err, lane);
+    if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+    if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
+    RQ_TRY_CUDA(ctx, cudaEventRecord(p.traced[sl], lane));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.down, p.traced[sl], 0));
+    if (any) {
+      // chunks are multiples of 32 rays, so bit words never straddle chunks
+      RQ_TRY_CUDA(ctx, cudaMemcpyAsync(static_cast<uint32_t*>(out) + first / 32, p.out[sl].p,
+                                       (size_t)((m + 31) / 32) * 4, cudaMemcpyDeviceToHost, p.down));
+    } else {
+      RQ_TRY_CUDA(ctx, cudaMemcpyAsync(static_cast<rq_hit_t*>(out) + first, p.out[sl].p, (size_t)m * 16,
+                                       cudaMemcpyDeviceToHost, p.down));
+    }
+    RQ_TRY_CUDA(ctx, cudaEventRecord(p.downloaded[sl], p.down));
+  }
+  // the context's stream is ordered after the last download
+  RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, p.down));
+  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, p.start, 0));
+  return RQ_SUCCESS;
+}
+
+static rq_status_t trace_streamed(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, void* out,
+                                  bool any) {
+  rq_status_t st = trace_streamed_enqueue(ctx, a, rays, n, out, any);
+  if (st != RQ_SUCCESS) {
+    // nothing may still read or write the caller's buffers after an error
+    if (ctx->pipe.up) cudaStreamSynchronize(ctx->pipe.up);
+    if (ctx->pipe.lane2) cudaStreamSynchronize(ctx->pipe.lane2);
+    if (ctx->pipe.down) cudaStreamSynchronize(ctx->pipe.down);
+    cudaStreamSynchronize(ctx->stream);
+    return st;
+  }
+  return collect_device_errors(ctx);
+}
+
 static rq_status_t trace(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, void* out,
                          uint32_t flags, bool any) {
   RQ_TRY(bind(ctx));
@@ -505,6 +636,7 @@ static rq_status_t trace(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint3
   if (n == 0) return RQ_SUCCESS;
   if (!rays || !out) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
   const bool dev = flags & RQ_DEVICE_POINTERS;
+  if (!dev && n >= 2 * kPipeChunk) return trace_streamed(ctx, a, rays, n, out, any);
   const float4* d_rays = nullptr;
   RQ_TRY(to_device(ctx, ctx->stage_in, reinterpret_cast<const float4*>(rays), (size_t)n * 32, flags, &d_rays));
   const size_t out_bytes = any ? (size_t)((n + 31) / 32) * 4 : (size_t)n * 16;

@@ -249,3 +249,26 @@ def test_errors_are_reported(engine, rqm):
     acc = engine.build(s, rqm.LBVH)
     h = engine.trace_closest(acc, rqm.make_rays(np.array([0, 0, 5.0]), np.array([[0, 0, -1]], np.float32)))
     assert h["prim"][0] == 0
+
+
+def test_rejected_host_update_keeps_the_scene(engine, oracle, rqm):
+    """Host geometry is validated on the device before it replaces the scene's:
+    a rejected update (NaN vertex, index out of range) changes nothing."""
+    v, f = scenes.displaced_icosphere(4, seed=23)
+    s = engine.scene_triangles(v, f)
+    acc = engine.build(s, "LBVH")
+    lo, hi = oracle.bounds3(v)
+    rays = scenes.incoherent_rays(lo, hi, 5000, seed=24)
+    before = engine.trace_closest(acc, rays)
+    bad = v.copy()
+    bad[7, 1] = np.nan
+    with pytest.raises(rqm.RqError) as e:
+        s.update(bad)
+    assert e.value.status == 1
+    bad_idx = f.copy()
+    bad_idx[3, 2] = len(v)
+    with pytest.raises(rqm.RqError) as e:
+        s.update(v * np.float32(2), bad_idx)
+    assert e.value.status == 1
+    acc.rebuild()
+    assert np.array_equal(engine.trace_closest(acc, rays).view(np.uint32), before.view(np.uint32))

@@ -31,3 +31,35 @@ def test_ray_sort_is_result_neutral(engine, oracle, rqm, acc_name):
     ref = oracle.Bvh2(nodes, len(nodes), root, order)
     want = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, ref, prims, sec)
     assert np.array_equal(got_c.view(np.uint32), want.view(np.uint32))
+
+
+def test_streamed_host_queries_equal_device_queries(engine, rqm):
+    """Host-buffer batches of two or more 2^21-ray chunks are uploaded, traced
+    and downloaded chunk by chunk on three streams; results equal the
+    device-pointer query, for pageable and pinned host memory."""
+    torch = pytest.importorskip("torch")
+    v, f = scenes.heightfield(301, 150, seed=15)
+    acc = engine.build(engine.scene_triangles(v, f), "LBVH")
+    rays = scenes.pinhole_rays(1250, 1000, 4, eye=(0, -0.6, 1.1), target=(0, 0, 0), seed=16)
+    n = len(rays)
+    assert n > 2 * (1 << 21) and n % (1 << 21) != 0  # three chunks, the last partial
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    d_bits = torch.empty(((n + 31) // 32) * 4, dtype=torch.uint8, device="cuda")
+    engine.trace_closest(acc, d_rays, d_hits)
+    engine.trace_any(acc, d_rays, d_bits)
+    engine.synchronize()
+    want_h = d_hits.cpu().numpy().view(np.uint32)
+    want_b = d_bits.cpu().numpy().view(np.uint32)
+    # pageable
+    assert np.array_equal(engine.trace_closest(acc, rays).view(np.uint32).ravel(), want_h)
+    assert np.array_equal(engine.trace_any(acc, rays), want_b)
+    # pinned
+    p_rays = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+    p_rays.numpy()[:] = rays.view(np.uint8)
+    p_hits = torch.empty(n * 16, dtype=torch.uint8, pin_memory=True)
+    hr = p_rays.numpy().view(rqm.RAY_DTYPE)
+    hh = p_hits.numpy().view(rqm.HIT_DTYPE)
+    engine.configure(ray_sort=rqm.RAY_SORT_OCTANT_MORTON)
+    engine.trace_closest(acc, hr, hh)
+    assert np.array_equal(hh.view(np.uint32).ravel(), want_h)
