@@ -212,6 +212,24 @@ rq_status_t rq_build(rq_ctx_t ctx, rq_scene_t scene, int32_t acc_type, rq_accel_
 /* Rebuild in place from the (possibly updated) scene, reusing device memory. */
 rq_status_t rq_accel_rebuild(rq_ctx_t ctx, rq_accel_t accel);
 rq_status_t rq_accel_destroy(rq_accel_t accel);
+
+/* Build one structure per scene.  RQ_LBVH builds the whole batch in one pass
+ * of batched kernels (scene boxes, Morton codes, one segmented radix sort by
+ * (scene, code), Karras topology, refit), the arrays of all scenes back to
+ * back in one allocation that lives until the last of the returned
+ * structures is destroyed; each structure equals the one rq_build would make
+ * from its scene.  The scenes must all hold triangles or all spheres, with
+ * fewer than 2^30 primitives together.  Other types are built scene by
+ * scene.  out receives n handles.  No reference counterpart: the reference
+ * builds one scene per run. */
+rq_status_t rq_build_batched(rq_ctx_t ctx, const rq_scene_t* scenes, uint32_t n, int32_t acc_type,
+                             rq_accel_t* out);
+/* Rebuild all structures of one rq_build_batched call (same handles, same
+ * order) in one pass, after rq_scene_update of any of its scenes.  Enqueued
+ * on the context's stream without waiting.  It allocates nothing once one
+ * build or rebuild has run with the same settings.node_width, so it can be
+ * captured into a CUDA graph (rq_plan_create does). */
+rq_status_t rq_accel_rebuild_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n);
 rq_status_t rq_accel_get_info(rq_accel_t accel, rq_accel_info_t* info);
 
 /* Host copies of a built structure (layouts in the engine documentation):
@@ -249,6 +267,46 @@ rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, u
  * (hits or occlusion bits) as in the plain calls. */
 rq_status_t rq_trace_counters(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n,
                               int32_t any, void* out, uint64_t* counters, uint32_t flags);
+
+/* ------------------------------------------------ many structures at once */
+
+/* Rays of many structures in one persistent, work-stealing launch: rays
+ * [ray_offsets[k], ray_offsets[k+1]) are traced against accels[k]
+ * (ray_offsets: host array of n_accels + 1 non-decreasing entries, first 0).
+ * any = 0: closest hits (16 B per ray) into out; any = 1: occlusion bits.
+ * Results equal the one-structure FAST queries.  The structures must be BVH
+ * structures (RQ_BVH, RQ_LBVH) of one primitive kind and node width.
+ * RQ_DEVICE_POINTERS: rays and out are device buffers and the launch is
+ * enqueued without waiting.  No reference counterpart. */
+rq_status_t rq_trace_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, const rq_ray_t* rays,
+                             const uint32_t* ray_offsets, int32_t any, void* out, uint32_t flags);
+
+/* A captured step over fixed device buffers, replayed as one CUDA graph:
+ * [rq_accel_rebuild_batched of the batch] + the many-structure query of
+ * rq_trace_batched.  rq_plan_create autotunes the query's launch shape
+ * (block of 128 or 256 threads x shallow or deep traversal stack) by timing
+ * each on `rays`, drops shapes whose stack overflows on these trees, then
+ * captures the step.  rays and out are device buffers whose contents may
+ * change between launches; the structures and scenes must outlive the plan.
+ * rebuild = 1 needs accels to be the whole batch of one rq_build_batched
+ * call.  No reference counterpart. */
+typedef struct rq_plan* rq_plan_t;
+typedef struct rq_plan_info_t {
+  uint32_t block_threads;   /* chosen launch shape */
+  uint32_t stack_entries;
+  uint32_t graph_kernels;   /* kernels one launch replays */
+  uint32_t n_rays;
+  uint32_t rebuilds;        /* 1 when the step rebuilds the batch */
+  float shape_ms[4];        /* query time of 128/shallow, 128/deep, 256/shallow, 256/deep; < 0: dropped */
+} rq_plan_info_t;
+rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, int32_t rebuild,
+                           const rq_ray_t* rays, const uint32_t* ray_offsets, int32_t any, void* out,
+                           rq_plan_t* plan);
+/* Enqueue one replay on the context's stream (no host synchronisation;
+ * rq_synchronize reports device-side errors). */
+rq_status_t rq_plan_launch(rq_plan_t plan);
+rq_status_t rq_plan_get_info(rq_plan_t plan, rq_plan_info_t* info);
+rq_status_t rq_plan_destroy(rq_plan_t plan);
 
 /* Kernel launches the engine has made in this process, over all contexts. */
 uint64_t rq_kernel_launch_count(void);

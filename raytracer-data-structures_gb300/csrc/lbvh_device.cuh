@@ -1,0 +1,151 @@
+// Device helpers shared by the single-scene LBVH kernels (morton.cu,
+// lbvh.cu) and the batched ones (batch.cu), so that a batched build performs
+// exactly the operations of a single build.
+#pragma once
+#include "rq_device.cuh"
+#include "rq_internal.hpp"
+
+namespace rq {
+
+// Scene box from the ordered-int accumulators: lo and extent per axis.
+__device__ __forceinline__ void bounds_from(const int32_t* lohi, float* lo, float* ext) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = ordered_to_float(lohi[k]);
+    float hi = ordered_to_float(lohi[3 + k]);
+    ext[k] = __fsub_rn(hi, lo[k]);
+  }
+}
+
+// (c - lo) / ext per axis, 0 where the extent is 0.
+__device__ __forceinline__ uint32_t code_scene(F3 c, const float* lo, const float* ext) {
+  float q0 = ext[0] > 0.f ? __fdiv_rn(__fsub_rn(c.x, lo[0]), ext[0]) : 0.f;
+  float q1 = ext[1] > 0.f ? __fdiv_rn(__fsub_rn(c.y, lo[1]), ext[1]) : 0.f;
+  float q2 = ext[2] > 0.f ? __fdiv_rn(__fsub_rn(c.z, lo[2]), ext[2]) : 0.f;
+  return morton3d(q0, q1, q2);
+}
+
+// Triangle centroid ((v0 + v1) + v2) / 3 per axis.
+__device__ __forceinline__ F3 tri_centroid(const float* __restrict__ verts, const uint32_t* __restrict__ idx,
+                                           uint32_t i) {
+  uint32_t i0 = __ldg(idx + 3 * (size_t)i), i1 = __ldg(idx + 3 * (size_t)i + 1), i2 = __ldg(idx + 3 * (size_t)i + 2);
+  const float* a = verts + 3 * (size_t)i0;
+  const float* b = verts + 3 * (size_t)i1;
+  const float* c = verts + 3 * (size_t)i2;
+  F3 cen;
+  cen.x = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a), __ldg(b)), __ldg(c)), 3.0f);
+  cen.y = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a + 1), __ldg(b + 1)), __ldg(c + 1)), 3.0f);
+  cen.z = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a + 2), __ldg(b + 2)), __ldg(c + 2)), 3.0f);
+  return cen;
+}
+
+// Karras 2012 prefix length between sorted codes i and j (index tiebreak).
+__device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ k, int64_t n, int64_t i, int64_t j,
+                                            uint32_t ki) {
+  if (j < 0 || j >= n) return -1;
+  uint32_t kj = __ldg(k + j);
+  if (ki != kj) return __clz(ki ^ kj);
+  return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+// Children of internal node i (0 <= i < n - 1) of the radix tree over n
+// sorted codes, given the neighbour deltas; returns (left, right) with leaves
+// encoded as ~slot.
+__device__ __forceinline__ int2 karras_children(const uint32_t* __restrict__ codes, int64_t N, int64_t i,
+                                                uint32_t ki, int dprev, int dnext) {
+  int d = (dnext - dprev) > 0 ? 1 : -1;
+  int dmin = d > 0 ? dprev : dnext;
+  int64_t lmax = 2;
+  while (karras_delta(codes, N, i, i + lmax * d, ki) > dmin) lmax *= 2;
+  int64_t l = 0;
+  for (int64_t t = lmax / 2; t >= 1; t /= 2)
+    if (karras_delta(codes, N, i, i + (l + t) * d, ki) > dmin) l += t;
+  int64_t j = i + l * d;
+  int dnode = karras_delta(codes, N, i, j, ki);
+  int64_t s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (karras_delta(codes, N, i, i + (s + t) * d, ki) > dnode) s += t;
+  } while (t > 1);
+  int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+  int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+  int32_t lc = (lo == gamma) ? ~(int32_t)gamma : (int32_t)gamma;
+  int32_t rc = (hi == gamma + 1) ? ~(int32_t)(gamma + 1) : (int32_t)(gamma + 1);
+  return make_int2(lc, rc);
+}
+
+struct Box6 {
+  float lo[3], hi[3];
+};
+
+__device__ __forceinline__ void write_child(float4* nodes, uint32_t node, uint32_t side, const Box6& b) {
+  nodes[4 * (size_t)node + side] = make_float4(b.lo[0], b.hi[0], b.lo[1], b.hi[1]);
+  reinterpret_cast<float2*>(nodes + 4 * (size_t)node + 2)[side] = make_float2(b.lo[2], b.hi[2]);
+}
+
+// Gather primitive `p` into payload slot `slot` (3 float4 per triangle:
+// (v0, id), (v1 - v0, 0), (v2 - v0, 0); 1 float4 per sphere) and return its box.
+__device__ __forceinline__ Box6 emit_prim(int kind, const float* __restrict__ verts,
+                                          const uint32_t* __restrict__ idx,
+                                          const float4* __restrict__ sph, uint32_t p,
+                                          float4* __restrict__ prims, uint32_t slot) {
+  Box6 b;
+  if (kind == kTriangles) {
+    uint32_t i0 = __ldg(idx + 3 * (size_t)p), i1 = __ldg(idx + 3 * (size_t)p + 1),
+             i2 = __ldg(idx + 3 * (size_t)p + 2);
+    F3 a = {__ldg(verts + 3 * (size_t)i0), __ldg(verts + 3 * (size_t)i0 + 1), __ldg(verts + 3 * (size_t)i0 + 2)};
+    F3 c1 = {__ldg(verts + 3 * (size_t)i1), __ldg(verts + 3 * (size_t)i1 + 1), __ldg(verts + 3 * (size_t)i1 + 2)};
+    F3 c2 = {__ldg(verts + 3 * (size_t)i2), __ldg(verts + 3 * (size_t)i2 + 1), __ldg(verts + 3 * (size_t)i2 + 2)};
+    F3 e1 = sub_rn(c1, a), e2 = sub_rn(c2, a);
+    float4* q = prims + 3 * (size_t)slot;
+    q[0] = make_float4(a.x, a.y, a.z, __uint_as_float(p));
+    q[1] = make_float4(e1.x, e1.y, e1.z, 0.f);
+    q[2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+    b.lo[0] = fminf(fminf(a.x, c1.x), c2.x); b.hi[0] = fmaxf(fmaxf(a.x, c1.x), c2.x);
+    b.lo[1] = fminf(fminf(a.y, c1.y), c2.y); b.hi[1] = fmaxf(fmaxf(a.y, c1.y), c2.y);
+    b.lo[2] = fminf(fminf(a.z, c1.z), c2.z); b.hi[2] = fmaxf(fmaxf(a.z, c1.z), c2.z);
+  } else {
+    float4 s = __ldg(sph + p);
+    prims[slot] = s;
+    // centre -/+ radius, main.cpp:686-688
+    b.lo[0] = __fsub_rn(s.x, s.w); b.lo[1] = __fsub_rn(s.y, s.w); b.lo[2] = __fsub_rn(s.z, s.w);
+    b.hi[0] = __fadd_rn(s.x, s.w); b.hi[1] = __fadd_rn(s.y, s.w); b.hi[2] = __fadd_rn(s.z, s.w);
+  }
+  return b;
+}
+
+// Bottom-up refit from leaf slot j: write the leaf box into its parent, then
+// climb while this thread is the second to arrive at a node (atomic count per
+// node), computing the node's box from its two children.  Writes the root
+// box when it reaches node 0.  parent: internal nodes [0, n-1), leaves at
+// (n - 1) + j, each (node << 1) | side.
+__device__ __forceinline__ void refit_climb(uint32_t n, uint32_t j, Box6 b, float4* nodes,
+                                            const uint32_t* __restrict__ parent, uint32_t* flags,
+                                            float* __restrict__ root_out, uint32_t* err) {
+  if (n == 1) {
+    for (int k = 0; k < 3; ++k) { root_out[k] = b.lo[k]; root_out[3 + k] = b.hi[k]; }
+    return;
+  }
+  uint32_t pw = __ldg(parent + (n - 1) + j);
+  for (int level = 0;; ++level) {
+    if (level >= 128) { atomicOr(err, kErrCorrupt); return; }  // Karras trees are at most 64 deep
+    uint32_t node = pw >> 1, side = pw & 1u;
+    write_child(nodes, node, side, b);
+    __threadfence();
+    if (atomicAdd(flags + node, 1u) == 0u) return;  // the sibling's thread finishes this node
+    __threadfence();
+    float4 a = __ldcg(nodes + 4 * (size_t)node);
+    float4 c = __ldcg(nodes + 4 * (size_t)node + 1);
+    float4 z = __ldcg(nodes + 4 * (size_t)node + 2);
+    b.lo[0] = fminf(a.x, c.x); b.hi[0] = fmaxf(a.y, c.y);
+    b.lo[1] = fminf(a.z, c.z); b.hi[1] = fmaxf(a.w, c.w);
+    b.lo[2] = fminf(z.x, z.z); b.hi[2] = fmaxf(z.y, z.w);
+    if (node == 0) {
+      for (int k = 0; k < 3; ++k) { root_out[k] = b.lo[k]; root_out[3 + k] = b.hi[k]; }
+      return;
+    }
+    pw = __ldg(parent + node);
+  }
+}
+
+}  // namespace rq

@@ -1,7 +1,6 @@
 // Morton codes over primitive centroids (accelerators.h:374-394, 575-580),
 // fused with the radix sort's digit histogram so the codes are read once.
-#include "rq_device.cuh"
-#include "rq_internal.hpp"
+#include "lbvh_device.cuh"
 
 namespace rq {
 namespace {
@@ -47,23 +46,6 @@ __global__ void __launch_bounds__(kThreads) k_point_bounds(const float* __restri
   }
 }
 
-__device__ __forceinline__ void bounds_from(const int32_t* lohi, float* lo, float* ext) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    lo[k] = ordered_to_float(lohi[k]);
-    float hi = ordered_to_float(lohi[3 + k]);
-    ext[k] = __fsub_rn(hi, lo[k]);
-  }
-}
-
-// (c - lo) / ext per axis, 0 where the extent is 0.
-__device__ __forceinline__ uint32_t code_scene(F3 c, const float* lo, const float* ext) {
-  float q0 = ext[0] > 0.f ? __fdiv_rn(__fsub_rn(c.x, lo[0]), ext[0]) : 0.f;
-  float q1 = ext[1] > 0.f ? __fdiv_rn(__fsub_rn(c.y, lo[1]), ext[1]) : 0.f;
-  float q2 = ext[2] > 0.f ? __fdiv_rn(__fsub_rn(c.z, lo[2]), ext[2]) : 0.f;
-  return morton3d(q0, q1, q2);
-}
-
 struct SharedHist {
   uint32_t h[4][256];
 };
@@ -96,16 +78,7 @@ __global__ void __launch_bounds__(kThreads) k_morton_tris(const float* __restric
   __syncthreads();
   float lo[3] = {s_lo[0], s_lo[1], s_lo[2]}, ext[3] = {s_ext[0], s_ext[1], s_ext[2]};
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
-    uint32_t i0 = __ldg(idx + 3 * (size_t)i), i1 = __ldg(idx + 3 * (size_t)i + 1),
-             i2 = __ldg(idx + 3 * (size_t)i + 2);
-    const float* a = verts + 3 * (size_t)i0;
-    const float* b = verts + 3 * (size_t)i1;
-    const float* c = verts + 3 * (size_t)i2;
-    F3 cen;
-    cen.x = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a), __ldg(b)), __ldg(c)), 3.0f);
-    cen.y = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a + 1), __ldg(b + 1)), __ldg(c + 1)), 3.0f);
-    cen.z = __fdiv_rn(__fadd_rn(__fadd_rn(__ldg(a + 2), __ldg(b + 2)), __ldg(c + 2)), 3.0f);
-    uint32_t code = code_scene(cen, lo, ext);
+    uint32_t code = code_scene(tri_centroid(verts, idx, i), lo, ext);
     keys[i] = code;
     vals[i] = i;
     if (hist) hist_add(sh, code);

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <random>
 #include <string>
@@ -76,6 +77,20 @@ struct rq_context {
   BuildScratch scratch;
   RenderScratch render;
   HostPipe pipe;
+  DevBuf batch_table;  // views + ray offsets + work counter of rq_trace_batched
+};
+
+struct rq_plan {
+  rq_ctx_t ctx = nullptr;
+  std::vector<rq_accel_t> accels;
+  std::shared_ptr<BatchStore> store;  // set when the plan rebuilds a batch
+  BatchedTrace trace;
+  DevBuf table;
+  int block = 128, deep = 1;
+  float shape_ms[4] = {-1.f, -1.f, -1.f, -1.f};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;
 };
 
 struct rq_scene {
@@ -91,6 +106,8 @@ struct rq_accel {
   rq_scene_t scene = nullptr;
   int type = RQ_NONE;
   AccelBuffers buf;
+  std::shared_ptr<BatchStore> batch;  // set when buf borrows a batched build's arrays
+  uint32_t batch_index = 0;
 };
 
 namespace {
@@ -243,6 +260,7 @@ rq_status_t rq_destroy(rq_ctx_t ctx) {
   ctx->scratch.release();
   ctx->render.release();
   ctx->pipe.release();
+  ctx->batch_table.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -463,7 +481,103 @@ rq_status_t rq_accel_destroy(rq_accel_t a) {
   cudaSetDevice(a->ctx->device);
   cudaStreamSynchronize(a->ctx->stream);
   a->buf.release();
+  a->batch.reset();  // the batch's arrays go with its last structure
   delete a;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_build_batched(rq_ctx_t ctx, const rq_scene_t* scenes, uint32_t n, int32_t acc_type, rq_accel_t* out) {
+  if (!out || !scenes || n == 0) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null or empty scene list");
+  RQ_TRY(bind(ctx));
+  for (uint32_t k = 0; k < n; ++k) out[k] = nullptr;
+  for (uint32_t k = 0; k < n; ++k)
+    if (!scenes[k]) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null scene in the list");
+  auto undo = [&](uint32_t upto) {
+    for (uint32_t k = 0; k < upto; ++k)
+      if (out[k]) rq_accel_destroy(out[k]);
+    for (uint32_t k = 0; k < n; ++k) out[k] = nullptr;
+  };
+  if (acc_type != RQ_LBVH) {  // the other builders run scene by scene
+    for (uint32_t k = 0; k < n; ++k) {
+      rq_status_t st = rq_build(ctx, scenes[k], acc_type, &out[k]);
+      if (st != RQ_SUCCESS) {
+        std::string msg = ctx->last_error;
+        undo(k);
+        return fail(ctx, st, msg);
+      }
+    }
+    return RQ_SUCCESS;
+  }
+  auto store = std::make_shared<BatchStore>();
+  store->kind = scenes[0]->kind;
+  store->n_scenes = n;
+  store->poff.assign(1, 0);
+  store->voff.assign(1, 0);
+  for (uint32_t k = 0; k < n; ++k) {
+    rq_scene_t sc = scenes[k];
+    if (sc->kind != store->kind) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "a batch mixes triangles and spheres");
+    const uint64_t p = (uint64_t)store->poff.back() + sc->n;
+    const uint64_t v = (uint64_t)store->voff.back() + (sc->kind == kTriangles ? sc->nv : sc->n);
+    if (p >= (1ull << 30) || v >= (1ull << 31))
+      return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "batch of 2^30 or more primitives");
+    store->poff.push_back((uint32_t)p);
+    store->voff.push_back((uint32_t)v);
+    store->host_desc.push_back({sc->verts.as<const float>(), sc->idx.as<const uint32_t>(), sc->sph.as<const float4>()});
+  }
+  RQ_TRY_CUDA(ctx, store->allocate());
+  RQ_TRY_CUDA(ctx, store->upload_tables(ctx->stream));
+  BuildResult br = build_batch(*store, ctx->settings.morton, ctx->d_err, ctx->stream);
+  if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+  if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
+  for (uint32_t k = 0; k < n; ++k) {
+    rq_accel* a = new (std::nothrow) rq_accel();
+    if (!a) {
+      undo(k);
+      return fail(ctx, RQ_ERROR_OUT_OF_MEMORY, "accel handle");
+    }
+    a->ctx = ctx;
+    a->scene = scenes[k];
+    a->type = RQ_LBVH;
+    store->view(k, a->buf);
+    a->batch = store;
+    a->batch_index = k;
+    out[k] = a;
+    if (ctx->settings.node_width == RQ_NODE_WIDTH_4) {
+      BuildResult r = collapse_bvh4(a->buf, ctx->scratch, ctx->d_err, ctx->stream);
+      if (!r.ok()) {
+        undo(k + 1);
+        return r.cuda != cudaSuccess ? cuda_fail(ctx, r.cuda, r.what) : fail(ctx, r.status, r.what);
+      }
+    }
+  }
+  rq_status_t st = collect_device_errors(ctx);
+  if (st != RQ_SUCCESS) undo(n);
+  return st;
+}
+
+rq_status_t rq_accel_rebuild_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n) {
+  if (!accels || n == 0 || !accels[0]) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null or empty structure list");
+  RQ_TRY(bind(ctx));
+  std::shared_ptr<BatchStore> store = accels[0]->batch;
+  if (!store) {  // not one batch: rebuild one by one
+    for (uint32_t k = 0; k < n; ++k) RQ_TRY(rq_accel_rebuild(ctx, accels[k]));
+    return RQ_SUCCESS;
+  }
+  if (n != store->n_scenes) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "not the whole batch");
+  for (uint32_t k = 0; k < n; ++k)
+    if (!accels[k] || accels[k]->batch != store || accels[k]->batch_index != k)
+      return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "structures not in the order rq_build_batched returned them");
+  BuildResult br = build_batch(*store, ctx->settings.morton, ctx->d_err, ctx->stream);
+  if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+  if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
+  for (uint32_t k = 0; k < n; ++k) {
+    AccelBuffers& b = accels[k]->buf;
+    b.node_width = 2;
+    if (ctx->settings.node_width == RQ_NODE_WIDTH_4) {
+      BuildResult r = collapse_bvh4(b, ctx->scratch, ctx->d_err, ctx->stream);
+      if (!r.ok()) return r.cuda != cudaSuccess ? cuda_fail(ctx, r.cuda, r.what) : fail(ctx, r.status, r.what);
+    }
+  }
   return RQ_SUCCESS;
 }
 
@@ -669,6 +783,207 @@ rq_status_t rq_trace_closest(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, u
 rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n,
                          uint32_t* occluded_bits, uint32_t flags) {
   return trace(ctx, a, rays, n, occluded_bits, flags, true);
+}
+
+// Device tables of a many-structure query: one Bvh2View per structure (the
+// 4-wide nodes when they were built with node width 4), the ray offsets and
+// the work counter, in `table`; fills t except rays / outputs.
+static rq_status_t batch_tables(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n, const uint32_t* ray_offsets,
+                                bool any, DevBuf& table, BatchedTrace& t) {
+  if (!accels || n == 0 || !ray_offsets) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null or empty structure list");
+  if (ray_offsets[0] != 0) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "ray_offsets[0] must be 0");
+  std::vector<Bvh2View> views(n);
+  for (uint32_t k = 0; k < n; ++k) {
+    rq_accel_t a = accels[k];
+    if (!a || a->ctx != ctx) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null structure or another context's");
+    if (a->type != RQ_BVH && a->type != RQ_LBVH)
+      return fail(ctx, RQ_ERROR_UNSUPPORTED, "many-structure queries walk BVH structures (RQ_BVH, RQ_LBVH)");
+    if (a->scene->kind != accels[0]->scene->kind || a->buf.node_width != accels[0]->buf.node_width)
+      return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "structures mix primitive kinds or node widths");
+    if (ray_offsets[k + 1] < ray_offsets[k]) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "ray_offsets decrease");
+    const AccelBuffers& b = a->buf;
+    views[k] = {b.node_width == 4 ? b.nodes4.as<const float4>() : b.nodes.as<const float4>(), b.prims.as<const float4>(),
+                b.order.as<const uint32_t>(), b.root.as<const float>(), b.n_nodes, b.n_slots};
+  }
+  if (ray_offsets[n] >= (1u << 31)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "2^31 or more rays");
+  const size_t vbytes = ((sizeof(Bvh2View) * n + 15) & ~size_t(15));
+  const size_t obytes = ((4 * ((size_t)n + 1) + 15) & ~size_t(15));
+  RQ_TRY_CUDA(ctx, table.ensure(vbytes + obytes + 16));
+  char* base = table.as<char>();
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(base, views.data(), sizeof(Bvh2View) * n, cudaMemcpyHostToDevice, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(base + vbytes, ray_offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, ctx->stream));
+  RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host tables may change after the call
+  t = BatchedTrace();
+  t.kind = accels[0]->scene->kind;
+  t.any = any;
+  t.width = accels[0]->buf.node_width == 4 ? 4 : 2;
+  t.views = reinterpret_cast<const Bvh2View*>(base);
+  t.roff = reinterpret_cast<const uint32_t*>(base + vbytes);
+  t.n_views = n;
+  t.n = ray_offsets[n];
+  t.work = reinterpret_cast<uint32_t*>(base + vbytes + obytes);
+  t.err = ctx->d_err;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_trace_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, const rq_ray_t* rays,
+                             const uint32_t* ray_offsets, int32_t any, void* out, uint32_t flags) {
+  RQ_TRY(bind(ctx));
+  BatchedTrace t;
+  RQ_TRY(batch_tables(ctx, accels, n_accels, ray_offsets, any != 0, ctx->batch_table, t));
+  if (t.n == 0) return RQ_SUCCESS;
+  if (!rays || !out) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
+  const bool dev = flags & RQ_DEVICE_POINTERS;
+  const float4* d_rays = nullptr;
+  RQ_TRY(to_device(ctx, ctx->stage_in, reinterpret_cast<const float4*>(rays), (size_t)t.n * 32, flags, &d_rays));
+  const size_t out_bytes = any ? (size_t)((t.n + 31) / 32) * 4 : (size_t)t.n * 16;
+  void* d_out = out;
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, ctx->stage_out.ensure(out_bytes));
+    d_out = ctx->stage_out.p;
+  }
+  t.rays = d_rays;
+  t.hits = any ? nullptr : static_cast<float4*>(d_out);
+  t.occ = any ? static_cast<uint32_t*>(d_out) : nullptr;
+  RQ_TRY_CUDA(ctx, launch_trace_batched(t, 128, 1, ctx->stream));
+  if (dev) return RQ_SUCCESS;
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return collect_device_errors(ctx);
+}
+
+// Read and clear the device error word without mapping it to a status.
+static cudaError_t take_device_errors(rq_ctx_t ctx, uint32_t* e) {
+  *e = 0;
+  cudaError_t c = cudaMemcpyAsync(e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (c == cudaSuccess) c = cudaStreamSynchronize(ctx->stream);
+  if (c == cudaSuccess && *e) c = cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream);
+  return c;
+}
+
+rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, int32_t rebuild,
+                           const rq_ray_t* rays, const uint32_t* ray_offsets, int32_t any, void* out,
+                           rq_plan_t* out_plan) {
+  if (!out_plan) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null plan");
+  *out_plan = nullptr;
+  RQ_TRY(bind(ctx));
+  std::unique_ptr<rq_plan> p(new (std::nothrow) rq_plan());
+  if (!p) return RQ_ERROR_OUT_OF_MEMORY;
+  p->ctx = ctx;
+  RQ_TRY(batch_tables(ctx, accels, n_accels, ray_offsets, any != 0, p->table, p->trace));
+  if (p->trace.n > 0 && (!rays || !out)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
+  p->trace.rays = reinterpret_cast<const float4*>(rays);
+  p->trace.hits = any ? nullptr : static_cast<float4*>(out);
+  p->trace.occ = any ? static_cast<uint32_t*>(out) : nullptr;
+  p->accels.assign(accels, accels + n_accels);
+  if (rebuild) {
+    p->store = accels[0]->batch;
+    if (!p->store || p->store->n_scenes != n_accels)
+      return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "a rebuilding plan needs the whole batch of one rq_build_batched call");
+    // one rebuild outside the capture sizes every scratch array it touches
+    RQ_TRY(rq_accel_rebuild_batched(ctx, accels, n_accels));
+    RQ_TRY(collect_device_errors(ctx));
+  }
+  // Autotuning: time every launch shape on these rays; a shape whose stack
+  // overflows on these trees is dropped.
+  const int shapes[4][2] = {{128, 0}, {128, 1}, {256, 0}, {256, 1}};
+  float best = -1.f;
+  if (p->trace.n > 0) {
+    cudaEvent_t e0, e1;
+    RQ_TRY_CUDA(ctx, cudaEventCreate(&e0));
+    RQ_TRY_CUDA(ctx, cudaEventCreate(&e1));
+    for (int k = 0; k < 4; ++k) {
+      float ms = 1e30f;
+      cudaError_t ce = cudaSuccess;
+      for (int rep = 0; rep < 3 && ce == cudaSuccess; ++rep) {
+        ce = cudaEventRecord(e0, ctx->stream);
+        if (ce == cudaSuccess) ce = launch_trace_batched(p->trace, shapes[k][0], shapes[k][1], ctx->stream);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e1, ctx->stream);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+        float t = 0.f;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
+        if (ce == cudaSuccess && rep > 0) ms = std::min(ms, t);
+      }
+      uint32_t derr = 0;
+      if (ce == cudaSuccess) ce = take_device_errors(ctx, &derr);
+      if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(ctx, ce, "plan autotuning");
+      }
+      if (derr & ~kErrStackOverflow) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed structure or input seen while autotuning");
+      }
+      if (derr & kErrStackOverflow) continue;
+      p->shape_ms[k] = ms;
+      if (best < 0.f || ms < best) {
+        best = ms;
+        p->block = shapes[k][0];
+        p->deep = shapes[k][1];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best < 0.f) return fail(ctx, RQ_ERROR_STACK_OVERFLOW, "every launch shape overflowed its traversal stack");
+  }
+  // Capture [rebuild] + query into one graph on a private stream.
+  cudaStream_t cap = nullptr;
+  RQ_TRY_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  const uint64_t k0 = launch_total();
+  cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed);
+  BuildResult br;
+  if (ce == cudaSuccess && p->store) {
+    br = build_batch(*p->store, ctx->settings.morton, ctx->d_err, cap);
+    for (uint32_t k = 0; br.ok() && k < n_accels; ++k)
+      if (accels[k]->buf.node_width == 4) br = collapse_bvh4(accels[k]->buf, ctx->scratch, ctx->d_err, cap);
+  }
+  if (ce == cudaSuccess && br.ok()) ce = launch_trace_batched(p->trace, p->block, p->deep, cap);
+  cudaError_t end = cudaStreamEndCapture(cap, &p->graph);
+  p->kernels = launch_total() - k0;
+  cudaStreamDestroy(cap);
+  if (ce == cudaSuccess && !br.ok()) ce = br.cuda != cudaSuccess ? br.cuda : cudaErrorInvalidValue;
+  if (ce == cudaSuccess) ce = end;
+  if (ce == cudaSuccess) ce = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  if (ce != cudaSuccess) {
+    if (p->graph) cudaGraphDestroy(p->graph);
+    cudaGetLastError();
+    return cuda_fail(ctx, ce, "plan capture");
+  }
+  *out_plan = p.release();
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_plan_launch(rq_plan_t p) {
+  if (!p) return RQ_ERROR_INVALID_ARGUMENT;
+  rq_ctx_t ctx = p->ctx;
+  RQ_TRY(bind(ctx));
+  RQ_TRY_CUDA(ctx, cudaGraphLaunch(p->exec, ctx->stream));
+  count_launch(p->kernels);
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_plan_get_info(rq_plan_t p, rq_plan_info_t* info) {
+  if (!p || !info) return RQ_ERROR_INVALID_ARGUMENT;
+  std::memset(info, 0, sizeof(*info));
+  info->block_threads = (uint32_t)p->block;
+  info->stack_entries = (uint32_t)batched_stack_entries(p->trace.width, p->deep);
+  info->graph_kernels = (uint32_t)p->kernels;
+  info->n_rays = p->trace.n;
+  info->rebuilds = p->store ? 1 : 0;
+  for (int k = 0; k < 4; ++k) info->shape_ms[k] = p->shape_ms[k];
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_plan_destroy(rq_plan_t p) {
+  if (!p) return RQ_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->table.release();
+  delete p;
+  return RQ_SUCCESS;
 }
 
 rq_status_t rq_trace_counters(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, int32_t any,

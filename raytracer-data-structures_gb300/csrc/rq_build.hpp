@@ -1,6 +1,8 @@
 // Build orchestration shared by the C ABI: device buffers of a structure,
 // reusable build scratch, and the per-type build / query entry points.
 #pragma once
+#include <vector>
+
 #include "rq_internal.hpp"
 
 namespace rq {
@@ -95,6 +97,35 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth, AccelBuffers& a, Bu
 // into the root buffer's word 6).
 uint32_t bvh4_node_cap(uint32_t n_internal);
 BuildResult collapse_bvh4(AccelBuffers& a, BuildScratch& sc, uint32_t* err, cudaStream_t st);
+
+// ---------------------------------------------------------- batched build
+struct BatchDesc {  // device copy per scene: its geometry
+  const float* verts;
+  const uint32_t* idx;
+  const float4* sph;
+};
+// All arrays of a batch of LBVH structures, back to back (see batch.cu).
+struct BatchStore {
+  int kind = kTriangles;
+  uint32_t n_scenes = 0;
+  std::vector<uint32_t> poff, voff;  // n + 1 prefix sums of primitives / points
+  std::vector<BatchDesc> host_desc;
+  DevBuf desc, offs, lohi, nodes, prims, order, codes, roots, parent, keys, keys_alt, vals, vals_alt, zero;
+  size_t zero_words = 0;
+  cudaError_t allocate();
+  cudaError_t upload_tables(cudaStream_t st);
+  // Borrowed views of scene s's arrays (what a single build would own).
+  void view(uint32_t s, AccelBuffers& a) const;
+  ~BatchStore() { release(); }
+  void release() {
+    desc.release(); offs.release(); lohi.release(); nodes.release(); prims.release(); order.release();
+    codes.release(); roots.release(); parent.release(); keys.release(); keys_alt.release(); vals.release();
+    vals_alt.release(); zero.release();
+  }
+};
+int batch_sort_passes(uint32_t n_scenes);
+// One pass of batched kernels over every scene (no allocation, no host sync).
+BuildResult build_batch(BatchStore& b, int morton_mode, uint32_t* err, cudaStream_t st);
 
 struct QueryTarget {
   const float4* rays = nullptr;

@@ -201,4 +201,15 @@ __device__ __forceinline__ bool spin_until(Pred pred, uint32_t limit) {
   return pred();
 }
 
+// Largest k with off[k] <= x (off has n + 1 non-decreasing entries, off[0] = 0 <= x < off[n]).
+__device__ __forceinline__ uint32_t segment_of(const uint32_t* __restrict__ off, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;  // answer in [lo, hi)
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
 }  // namespace rq

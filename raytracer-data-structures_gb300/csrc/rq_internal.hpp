@@ -10,12 +10,15 @@
 
 namespace rq {
 
-// Grow-only device allocation.
+// Grow-only device allocation.  A borrowed buffer (owned = false) is a slice
+// of memory owned elsewhere: it never grows and is never freed here.
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+  bool owned = true;
   cudaError_t ensure(size_t bytes) {
     if (bytes <= cap && p) return cudaSuccess;
+    if (!owned) return cudaErrorInvalidValue;
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;
@@ -25,9 +28,10 @@ struct DevBuf {
     return e;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p && owned) cudaFree(p);
     p = nullptr;
     cap = 0;
+    owned = true;
   }
   template <typename T>
   T* as() const {
@@ -137,6 +141,28 @@ struct Bvh4View {
 void launch_trace_bvh4(int kind, bool any, const Bvh4View& v, const float4* rays, uint32_t n, float4* hits,
                        uint32_t* occ, uint32_t* err, cudaStream_t s, const uint32_t* perm = nullptr,
                        unsigned long long* counters = nullptr);
+
+// Rays of many BVH structures in one persistent launch (trace_batched.cu).
+// views: device array of n_views structures (nodes = 4-wide nodes when
+// width == 4); roff: device array of n_views + 1 ray offsets; work: one
+// device word (zeroed by the launcher).
+struct BatchedTrace {
+  int kind = kTriangles;
+  bool any = false;
+  int width = 2;
+  const Bvh2View* views = nullptr;
+  const uint32_t* roff = nullptr;
+  uint32_t n_views = 0;
+  const float4* rays = nullptr;
+  uint32_t n = 0;
+  float4* hits = nullptr;
+  uint32_t* occ = nullptr;
+  uint32_t* work = nullptr;
+  uint32_t* err = nullptr;
+};
+// block: 128 or 256 threads; deep: the deeper of the two stack sizes.
+cudaError_t launch_trace_batched(const BatchedTrace& t, int block, int deep, cudaStream_t s);
+int batched_stack_entries(int width, int deep);
 
 struct KdView {
   const int4* nodes;      // {word0, word1, word2, 0}

@@ -1,0 +1,105 @@
+// Persistent, work-stealing traversal of many structures in one launch.
+//
+// Rays of all structures lie back to back; ray_off (n_views + 1 entries)
+// gives each structure's range.  The grid is sized to what the SMs hold at
+// once; each warp takes blocks of 256 consecutive rays from a global counter
+// until none are left, so long and short structures, coherent and incoherent
+// rays share the GPU without a tail per structure.  Each ray finds its
+// structure by binary search over ray_off and walks it with the same FAST
+// walk as a one-structure query (identical results).
+//
+// Launch shapes (block size, traversal stack depth) are template choices that
+// rq_plan_create times on the caller's rays; a stack too shallow for a tree
+// reports RQ_ERROR_STACK_OVERFLOW and the tuner drops that shape.
+#include "trace_device.cuh"
+
+namespace rq {
+namespace {
+
+constexpr uint32_t kGrab = 256;  // rays a warp takes per counter access (8 passes of 32)
+
+template <int KIND, bool ANY, int W, int STACK, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restrict__ views,
+                                                         const uint32_t* __restrict__ roff, uint32_t n_views,
+                                                         const float4* __restrict__ rays, uint32_t n,
+                                                         float4* __restrict__ hits, uint32_t* __restrict__ occ,
+                                                         uint32_t* __restrict__ work, uint32_t* err) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, kGrab);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) return;  // the whole warp leaves together
+#pragma unroll 1
+    for (uint32_t sub = 0; sub < kGrab; sub += 32) {
+      const uint32_t r = base + sub + lane;
+      bool occluded = false;
+      if (r < n) {
+        const Bvh2View v = views[segment_of(roff, n_views, r)];
+        const Ray ray = load_ray(rays, r);
+        Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+        uint32_t visits = 0, tests = 0;
+        if (W == 4) {
+          const Bvh4View v4{v.nodes, v.prims, v.order, v.root, v.n_internal, v.n_slots};
+          occluded = walk_bvh4<KIND, ANY, false, STACK>(v4, ray, c, visits, tests, err);
+        } else {
+          occluded = walk_bvh2<KIND, ANY, false, STACK>(v, ray, c, visits, tests, err);
+        }
+        if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+      }
+      if (ANY) {
+        const uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+        if (lane == 0 && base + sub < n) occ[(base + sub) >> 5] = bits;
+      }
+    }
+  }
+}
+
+template <int KIND, bool ANY, int W, int STACK, int BLOCK>
+cudaError_t launch_shape(const BatchedTrace& t, cudaStream_t s) {
+  auto k = k_trace_batched<KIND, ANY, W, STACK, BLOCK>;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, BLOCK, 0);
+  if (e != cudaSuccess) return e;
+  int sms = 0;
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  const uint64_t want_warps = ((uint64_t)t.n + kGrab - 1) / kGrab;
+  uint64_t blocks = (uint64_t)(per_sm > 0 ? per_sm : 1) * sms;
+  const uint64_t enough = (want_warps * 32 + BLOCK - 1) / BLOCK;  // no more warps than work blocks
+  if (blocks > enough) blocks = enough;
+  if (blocks < 1) blocks = 1;
+  if ((e = cudaMemsetAsync(t.work, 0, 4, s)) != cudaSuccess) return e;
+  count_launch();
+  k<<<(unsigned)blocks, BLOCK, 0, s>>>(t.views, t.roff, t.n_views, t.rays, t.n, t.hits, t.occ, t.work, t.err);
+  return cudaGetLastError();
+}
+
+template <int KIND, bool ANY, int W>
+cudaError_t dispatch_shape(const BatchedTrace& t, int block, int deep, cudaStream_t s) {
+  constexpr int kShallow = W == 4 ? 48 : 32, kDeep = W == 4 ? 96 : 64;
+  if (block == 256) {
+    return deep ? launch_shape<KIND, ANY, W, kDeep, 256>(t, s) : launch_shape<KIND, ANY, W, kShallow, 256>(t, s);
+  }
+  return deep ? launch_shape<KIND, ANY, W, kDeep, 128>(t, s) : launch_shape<KIND, ANY, W, kShallow, 128>(t, s);
+}
+
+template <int KIND, bool ANY>
+cudaError_t dispatch_width(const BatchedTrace& t, int block, int deep, cudaStream_t s) {
+  return t.width == 4 ? dispatch_shape<KIND, ANY, 4>(t, block, deep, s) : dispatch_shape<KIND, ANY, 2>(t, block, deep, s);
+}
+
+}  // namespace
+
+int batched_stack_entries(int width, int deep) { return width == 4 ? (deep ? 96 : 48) : (deep ? 64 : 32); }
+
+cudaError_t launch_trace_batched(const BatchedTrace& t, int block, int deep, cudaStream_t s) {
+  if (t.n == 0) return cudaSuccess;
+  if (block != 128 && block != 256) return cudaErrorInvalidValue;
+  if (t.kind == kTriangles)
+    return t.any ? dispatch_width<kTriangles, true>(t, block, deep, s) : dispatch_width<kTriangles, false>(t, block, deep, s);
+  return t.any ? dispatch_width<kSpheres, true>(t, block, deep, s) : dispatch_width<kSpheres, false>(t, block, deep, s);
+}
+
+}  // namespace rq

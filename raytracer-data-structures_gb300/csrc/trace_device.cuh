@@ -1,0 +1,220 @@
+// Per-ray traversal device code shared by the one-structure kernels
+// (trace.cu) and the persistent many-structure kernel (trace_batched.cu).
+#pragma once
+#include "rq_device.cuh"
+#include "rq_internal.hpp"
+
+namespace rq {
+
+struct Ray {
+  F3 o, d;
+  float tmin, tmax;
+};
+
+__device__ __forceinline__ Ray load_ray(const float4* __restrict__ rays, uint32_t r) {
+  float4 a = __ldg(rays + 2 * (size_t)r), b = __ldg(rays + 2 * (size_t)r + 1);
+  return {{a.x, a.y, a.z}, {b.x, b.y, b.z}, a.w, b.w};
+}
+
+struct Closest {
+  float t;
+  uint32_t prim;
+  float u, v;
+};
+
+// Test the primitives of one leaf.  Returns true when an any-hit query is done.
+template <int KIND, bool ANY, bool REF>
+__device__ __forceinline__ bool test_leaf(const float4* __restrict__ prims,
+                                          const uint32_t* __restrict__ order, uint32_t first,
+                                          int count, const Ray& ray, Closest& c) {
+  for (int k = 0; k < count; ++k) {
+    uint32_t slot = first + (uint32_t)k;
+    if (KIND == kTriangles) {
+      float4 p0 = __ldg(prims + 3 * (size_t)slot), p1 = __ldg(prims + 3 * (size_t)slot + 1),
+             p2 = __ldg(prims + 3 * (size_t)slot + 2);
+      float t, u, v;
+      if (tri_mt(p0, p1, p2, ray.o, ray.d, ray.tmin, ANY ? ray.tmax : c.t, t, u, v)) {
+        if (ANY) return true;
+        c = {t, __float_as_uint(p0.w), u, v};
+      }
+    } else {
+      float4 s = __ldg(prims + slot);
+      if (ANY) {
+        float t0, t1, t;
+        if (REF ? sphere_ref(s, ray.o, ray.d, t0, t1)
+                : sphere_closest(s, ray.o, ray.d, ray.tmin, ray.tmax, false, t))
+          return true;
+      } else {
+        float t;
+        if (sphere_closest(s, ray.o, ray.d, ray.tmin, c.t, REF, t)) c = {t, __ldg(order + slot), 0.f, 0.f};
+      }
+    }
+  }
+  return false;
+}
+
+// Primitive tests one leaf visit performs: every primitive for closest hit;
+// up to and including the first accepted one for any hit (the oracle's count).
+template <int KIND, bool ANY>
+__device__ __forceinline__ uint32_t test_count(const float4* __restrict__ prims, uint32_t first, int count,
+                                               const Ray& ray) {
+  if (!ANY) return (uint32_t)count;
+  Closest dummy = {ray.tmax, kMiss, 0.f, 0.f};
+  for (int k = 0; k < count; ++k)
+    if (test_leaf<KIND, true, false>(prims, nullptr, first + (uint32_t)k, 1, ray, dummy)) return (uint32_t)k + 1;
+  return (uint32_t)count;
+}
+
+// FAST walk of one ray through a BVH2: near child first, far child on a
+// per-thread stack of STACK entries, boxes clipped to [tmin, closest hit].
+// Returns true when an any-hit query found a hit.
+template <int KIND, bool ANY, bool COUNT, int STACK>
+__device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* err) {
+  const SlabRay sr = slab_ray(ray.o, ray.d);
+  float tn;
+  const float* rb = bvh.root;
+  if (!slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
+  int2 stack[STACK];
+  int sp = 0;
+  int cur = bvh.n_internal ? 0 : -1;
+  int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
+  // A valid walk visits every node at most once.
+  const uint32_t max_steps = 2u * (bvh.n_internal + bvh.n_slots) + 8u;
+  uint32_t steps = 0;
+  for (;;) {
+    if (++steps > max_steps) { atomicOr(err, kErrCorrupt); return false; }
+    if (cur >= 0) {
+      const float4* nd = bvh.nodes + 4 * (size_t)cur;
+      float4 a = __ldg(nd), b = __ldg(nd + 1), z = __ldg(nd + 2);
+      int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+      if (COUNT) ++visits;
+      const float tfar = ANY ? ray.tmax : c.t;
+      float tl, tr;
+      bool hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+      bool hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+      if (hl && hr) {
+        int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
+        if (tr < tl) { int2 t = nearE; nearE = farE; farE = t; }
+        if (sp >= STACK) { atomicOr(err, kErrStackOverflow); return false; }
+        stack[sp++] = farE;
+        cur = nearE.x;
+        cnt = nearE.y;
+        continue;
+      }
+      if (hl) { cur = l.x; cnt = l.z; continue; }
+      if (hr) { cur = l.y; cnt = l.w; continue; }
+    } else {
+      if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, (uint32_t)(~cur), cnt, ray);
+      if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) return true;
+    }
+    if (sp == 0) return false;
+    int2 e = stack[--sp];
+    cur = e.x;
+    cnt = e.y;
+  }
+}
+
+// Sum the per-thread visit / test counts of a warp into counters[0..1].
+__device__ __forceinline__ void add_counts(unsigned long long* counters, uint32_t visits, uint32_t tests) {
+  unsigned long long v = visits, t = tests;
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_down_sync(0xffffffffu, v, o);
+    t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(counters, v);
+    atomicAdd(counters + 1, t);
+  }
+}
+
+// ---------------------------------------------------------------- 4-wide
+// FAST traversal of the collapsed 4-wide BVH: one 128-byte node fetch tests
+// up to four child boxes.  The hit children are ordered by a 32-bit key, the
+// order-preserving bits of the entry distance with the low two bits replaced
+// by the slot (unique keys, so a sorting network gives the same order as any
+// sort); the nearest is visited next and the others pushed farthest first.
+// Three entries per level at most: 96 stack entries cover trees 64 binary
+// levels deep, like the binary walk's 64.
+constexpr int kStack4 = 96;
+
+__device__ __forceinline__ uint32_t order_key(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
+  uint32_t lo = min(a, b), hi = max(a, b);
+  a = lo;
+  b = hi;
+}
+
+__device__ __forceinline__ int pick(const int4& v, uint32_t k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
+// FAST walk of one ray through the collapsed 4-wide BVH.  Returns true when
+// an any-hit query found a hit.
+template <int KIND, bool ANY, bool COUNT, int STACK>
+__device__ __forceinline__ bool walk_bvh4(const Bvh4View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* err) {
+  const SlabRay sr = slab_ray(ray.o, ray.d);
+  float tn;
+  const float* rb = bvh.root;
+  if (!slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
+  int2 stack[STACK];
+  int sp = 0;
+  int cur = bvh.n_binary ? 0 : -1;
+  int cnt = bvh.n_binary ? 0 : (int)bvh.n_slots;
+  // A valid walk visits every node and leaf at most once.
+  const uint32_t max_steps = 2u * (bvh.n_binary + bvh.n_slots) + 8u;
+  uint32_t steps = 0;
+  for (;;) {
+    if (++steps > max_steps) { atomicOr(err, kErrCorrupt); return false; }
+    if (cur >= 0) {
+      const float4* nd = bvh.nodes + 8 * (size_t)cur;
+      const float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+      const float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+      const int4 lk = __ldg(reinterpret_cast<const int4*>(nd + 6));
+      const int4 ct = __ldg(reinterpret_cast<const int4*>(nd + 7));
+      if (COUNT) ++visits;
+      const float tfar = ANY ? ray.tmax : c.t;
+      float t0, t1, t2, t3;
+      uint32_t k0 = 0xFFFFFFFFu, k1 = 0xFFFFFFFFu, k2 = 0xFFFFFFFFu, k3 = 0xFFFFFFFFu;
+      if (ct.x >= 0 && slab_fast(sr, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, ray.tmin, tfar, t0))
+        k0 = (order_key(t0) & ~3u) | 0u;
+      if (ct.y >= 0 && slab_fast(sr, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, ray.tmin, tfar, t1))
+        k1 = (order_key(t1) & ~3u) | 1u;
+      if (ct.z >= 0 && slab_fast(sr, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, ray.tmin, tfar, t2))
+        k2 = (order_key(t2) & ~3u) | 2u;
+      if (ct.w >= 0 && slab_fast(sr, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, ray.tmin, tfar, t3))
+        k3 = (order_key(t3) & ~3u) | 3u;
+      // A hit key is at most order_key(+inf) | 3 < 0xFFFFFFFF, so misses sort last.
+      const int m = (k0 != 0xFFFFFFFFu) + (k1 != 0xFFFFFFFFu) + (k2 != 0xFFFFFFFFu) + (k3 != 0xFFFFFFFFu);
+      if (m > 0) {
+        cswap(k0, k1);
+        cswap(k2, k3);
+        cswap(k0, k2);
+        cswap(k1, k3);
+        cswap(k1, k2);
+        if (sp + m - 1 > STACK) { atomicOr(err, kErrStackOverflow); return false; }
+        if (m >= 4) stack[sp++] = make_int2(pick(lk, k3 & 3u), pick(ct, k3 & 3u));
+        if (m >= 3) stack[sp++] = make_int2(pick(lk, k2 & 3u), pick(ct, k2 & 3u));
+        if (m >= 2) stack[sp++] = make_int2(pick(lk, k1 & 3u), pick(ct, k1 & 3u));
+        cur = pick(lk, k0 & 3u);
+        cnt = pick(ct, k0 & 3u);
+        continue;
+      }
+    } else {
+      if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, (uint32_t)(~cur), cnt, ray);
+      if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) return true;
+    }
+    if (sp == 0) return false;
+    int2 e = stack[--sp];
+    cur = e.x;
+    cnt = e.y;
+  }
+}
+
+
+}  // namespace rq

@@ -65,6 +65,31 @@ def make_view(eye, target, up=(0, 0, 1), fov_deg=40.0, light=(0, 0, 10), albedo=
     return v
 
 
+class PlanInfo(C.Structure):
+    _fields_ = [("block_threads", C.c_uint32), ("stack_entries", C.c_uint32), ("graph_kernels", C.c_uint32),
+                ("n_rays", C.c_uint32), ("rebuilds", C.c_uint32), ("shape_ms", C.c_float * 4)]
+
+
+class Plan:
+    """rq_plan_t: a captured [rebuild +] many-structure query, replayed as one CUDA graph."""
+
+    def __init__(self, engine, handle, keep):
+        self.engine, self.handle, self._keep = engine, handle, keep
+
+    def launch(self):
+        self.engine._check(load().rq_plan_launch(self.handle))
+
+    def info(self):
+        inf = PlanInfo()
+        self.engine._check(load().rq_plan_get_info(self.handle, C.byref(inf)))
+        return inf
+
+    def close(self):
+        if self.handle:
+            load().rq_plan_destroy(self.handle)
+            self.handle = None
+
+
 class RqError(RuntimeError):
     def __init__(self, status, message):
         self.status = status
@@ -119,6 +144,13 @@ def load(build_if_missing=True):
         "rq_kernel_launch_count": (C.c_uint64, []),
         "rq_sort_pairs_noalloc": (i32, [vp, vp, u32, u32, vp]),
         "rq_render": (i32, [vp, vp, vp, vp, vp, vp, u32]),
+        "rq_build_batched": (i32, [vp, vp, u32, i32, vp]),
+        "rq_accel_rebuild_batched": (i32, [vp, vp, u32]),
+        "rq_trace_batched": (i32, [vp, vp, u32, vp, vp, i32, vp, u32]),
+        "rq_plan_create": (i32, [vp, vp, u32, i32, vp, vp, i32, vp, vp]),
+        "rq_plan_launch": (i32, [vp]),
+        "rq_plan_get_info": (i32, [vp, vp]),
+        "rq_plan_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -259,6 +291,50 @@ class Engine:
         h = C.c_void_p()
         self._check(load().rq_build(self.ctx, scene.handle, acc_type, C.byref(h)))
         return Accel(self, h, scene, acc_type)
+
+    def build_batched(self, scenes, acc_type):
+        """rq_build_batched: one structure per scene (RQ_LBVH: one pass of batched kernels)."""
+        if isinstance(acc_type, str):
+            acc_type = ACC_NAMES[acc_type]
+        n = len(scenes)
+        hs = (C.c_void_p * n)(*[sc.handle for sc in scenes])
+        out = (C.c_void_p * n)()
+        self._check(load().rq_build_batched(self.ctx, hs, n, acc_type, out))
+        return [Accel(self, C.c_void_p(out[k]), scenes[k], acc_type) for k in range(n)]
+
+    def rebuild_batched(self, accels):
+        hs = (C.c_void_p * len(accels))(*[a.handle.value if isinstance(a.handle, C.c_void_p) else a.handle
+                                           for a in accels])
+        self._check(load().rq_accel_rebuild_batched(self.ctx, hs, len(accels)))
+
+    @staticmethod
+    def _handles(accels):
+        return (C.c_void_p * len(accels))(*[a.handle.value if isinstance(a.handle, C.c_void_p) else a.handle
+                                            for a in accels])
+
+    def trace_batched(self, accels, rays, ray_offsets, any_hit=False, out=None):
+        """rq_trace_batched: rays[ray_offsets[k]:ray_offsets[k+1]] against accels[k]."""
+        offs = np.ascontiguousarray(ray_offsets, np.uint32)
+        n = int(offs[-1])
+        if isinstance(rays, np.ndarray):
+            rays = np.ascontiguousarray(rays, RAY_DTYPE)
+            if out is None:
+                out = np.zeros((n + 31) // 32, np.uint32) if any_hit else np.zeros(n, HIT_DTYPE)
+        pr, fl = _ptr(rays)
+        po, _ = _ptr(out)
+        self._check(load().rq_trace_batched(self.ctx, self._handles(accels), len(accels), pr, offs.ctypes.data,
+                                            int(any_hit), po, fl))
+        return out
+
+    def plan(self, accels, rays, ray_offsets, out, any_hit=False, rebuild=False):
+        """rq_plan_create on device buffers rays / out (torch tensors or pointers)."""
+        offs = np.ascontiguousarray(ray_offsets, np.uint32)
+        pr, _ = _ptr(rays)
+        po, _ = _ptr(out)
+        h = C.c_void_p()
+        self._check(load().rq_plan_create(self.ctx, self._handles(accels), len(accels), int(rebuild), pr,
+                                          offs.ctypes.data, int(any_hit), po, C.byref(h)))
+        return Plan(self, h, (accels, rays, out))
 
     # -- queries
     def trace_closest(self, accel, rays, hits=None):
