@@ -339,6 +339,10 @@ def run_ours(args):
     if not args.skip_render:
         render = run_render_legs(eng, stream, dev, args)
 
+    batched = None
+    if not args.skip_batch:
+        batched = run_batch_leg(eng, stream, dev, args)
+
     e2e = None
     if rank == 0 and not args.skip_e2e:
         e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice)
@@ -371,6 +375,7 @@ def run_ours(args):
                                "frac": round(build_bytes / (build_ms * 1e-3) / 1e9 / peak, 4)},
             "structures": structures,
             "render": render,
+            "batched": batched,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),
         }
         print(json.dumps(out), flush=True)
@@ -438,6 +443,126 @@ def run_render_legs(eng, stream, dev, args):
         out["c3"] = leg(v3, f3, ("LBVH",), 3840, 2160, 4, scenes.C3_VIEW, 3)
     eng.settings = saved
     log(f"[bench] render: {out}")
+    return out
+
+
+def batch_rays(torch, dev, meshes, counts, seed):
+    """Rays of each scene, generated on the device from a seeded generator:
+    origins uniform on the scene's bounding sphere (radius x 1.05), directions
+    towards uniform points inside its box, tmin 0, tmax inf.  Returns a
+    (sum counts) x 32-byte uint8 tensor."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    lo = torch.tensor(np.array([v.min(0) for v, _ in meshes]), dtype=torch.float64, device=dev)
+    hi = torch.tensor(np.array([v.max(0) for v, _ in meshes]), dtype=torch.float64, device=dev)
+    idx = torch.repeat_interleave(torch.arange(len(meshes), device=dev), torch.tensor(counts, device=dev))
+    n = int(idx.numel())
+    l, h = lo[idx], hi[idx]
+    c, R = (l + h) / 2, torch.linalg.norm(h - l, dim=1, keepdim=True) / 2 * 1.05
+    sdir = torch.randn(n, 3, generator=g, device=dev, dtype=torch.float64)
+    org = c + R * sdir / torch.linalg.norm(sdir, dim=1, keepdim=True)
+    tgt = l + torch.rand(n, 3, generator=g, device=dev, dtype=torch.float64) * (h - l)
+    d = tgt - org
+    d = d / torch.linalg.norm(d, dim=1, keepdim=True)
+    out = torch.empty(n, 8, dtype=torch.float32, device=dev)
+    out[:, 0:3] = org.float()
+    out[:, 3] = 0.0
+    out[:, 4:7] = d.float()
+    out[:, 7] = float("inf")
+    return out.view(torch.uint8).reshape(-1)
+
+
+def run_batch_leg(eng, stream, dev, args):
+    """Many scenes at once: 256 terrain meshes with triangle counts
+    log-uniform in [1k, 500k] and ray counts log-uniform in [64k, 2M] (origins
+    on each scene's bounding sphere, directions into its box).  One step =
+    rebuild every structure + closest hit for every ray.  'plain' does it one
+    scene per launch (rq_accel_rebuild + rq_trace_closest per scene); 'batched'
+    replays one plan: the batched LBVH rebuild + one persistent many-structure
+    query, captured as a CUDA graph, launch shape autotuned.  Device buffers,
+    L2 flushed before every timed step."""
+    import torch
+    import rq
+    import scenes
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    rng = np.random.default_rng(SEED + 40)
+    n_sc = 32 if args.small else 256
+    tri_t = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_sc))
+    ray_n = np.exp(rng.uniform(np.log(64e3), np.log(2e6), n_sc)).astype(np.int64)
+    meshes = []
+    for k in range(n_sc):
+        nx = max(2, int(round(np.sqrt(tri_t[k] / 2)))) + 1
+        meshes.append(scenes.wave_heightfield(nx, nx, seed=SEED + 100 + k))
+    n_tri = int(sum(len(f) for _, f in meshes))
+    saved = eng.settings
+    eng.configure(ray_sort=rq.RAY_SORT_NONE)
+    sc = [eng.scene_triangles(v, f) for v, f in meshes]
+    offs = np.zeros(n_sc + 1, np.uint32)
+    offs[1:] = np.cumsum(ray_n)
+    n_rays = int(offs[-1])
+    d_rays = batch_rays(torch, dev, meshes, ray_n.tolist(), SEED + 41)
+    d_hits = torch.empty(n_rays * HIT_BYTES, dtype=torch.uint8, device=dev)
+    log(f"[bench] batch: {n_sc} scenes, {n_tri} tris, {n_rays} rays")
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = ev(), ev()
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(a.elapsed_time(b))
+        return float(np.mean(ts[1:])) if len(ts) > 1 else ts[0]
+
+    # plain: one scene per launch
+    singles = [eng.build(s, rq.LBVH) for s in sc]
+    views = [(d_rays[int(offs[k]) * 32:int(offs[k + 1]) * 32], d_hits[int(offs[k]) * 16:int(offs[k + 1]) * 16])
+             for k in range(n_sc)]
+
+    def plain_step():
+        for k in range(n_sc):
+            singles[k].rebuild()
+            eng.trace_closest(singles[k], views[k][0], views[k][1])
+
+    def plain_build():
+        for k in range(n_sc):
+            singles[k].rebuild()
+
+    plain_ms = timed(plain_step, 4)
+    plain_build_ms = timed(plain_build, 4)
+    ref_hits = d_hits.clone()
+    for a in singles:
+        a.close()
+
+    # batched: one plan = batched rebuild + persistent query, one CUDA graph
+    accs = eng.build_batched(sc, rq.LBVH)
+    plan = eng.plan(accs, d_rays, offs, d_hits, rebuild=True)
+    batched_ms = timed(plan.launch, 6)
+    eng.synchronize()
+    same = bool(torch.equal(d_hits, ref_hits))
+    batched_build_ms = timed(lambda: eng.rebuild_batched(accs), 4)
+    info = plan.info()
+    plan.close()
+    for a in accs:
+        a.close()
+    for s in sc:
+        s.close()
+    eng.settings = saved
+    out = {"scenes": n_sc, "triangles": n_tri, "rays": n_rays,
+           "plain": {"step_ms": round(plain_ms, 3), "build_ms": round(plain_build_ms, 3),
+                     "grays_s": round(n_rays / (plain_ms * 1e-3) / 1e9, 4)},
+           "batched": {"step_ms": round(batched_ms, 3), "build_ms": round(batched_build_ms, 3),
+                       "grays_s": round(n_rays / (batched_ms * 1e-3) / 1e9, 4),
+                       "build_mtri_s": round(n_tri / (batched_build_ms * 1e-3) / 1e6, 1),
+                       "graph_kernels": int(info.graph_kernels),
+                       "shape": {"block": int(info.block_threads), "stack": int(info.stack_entries),
+                                 "tuned_ms": [round(float(x), 3) for x in info.shape_ms]}},
+           "speedup": round(plain_ms / batched_ms, 3), "hits_identical": same}
+    log(f"[bench] batched: {out}")
     return out
 
 
@@ -617,6 +742,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="960x540x4 rays (profiling case)")
     ap.add_argument("--skip-structures", action="store_true", help="skip the BVH / KDTREE comparison")
     ap.add_argument("--skip-render", action="store_true", help="skip the render-step legs")
+    ap.add_argument("--skip-batch", action="store_true", help="skip the many-scene leg")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

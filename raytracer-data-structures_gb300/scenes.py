@@ -105,6 +105,25 @@ def displaced_icosphere(level=6, amplitude=0.15, octaves=3, seed=1, unit_cube=Tr
     return v.astype(np.float32), f.astype(np.uint32)
 
 
+def wave_heightfield(nx, ny, seed=0, size=1.0):
+    """A cheap seeded terrain for many-scene batches: an nx x ny vertex grid
+    over [-size, size]^2, z = a sum of four products of sines with seeded
+    frequencies and phases; 2 (nx - 1)(ny - 1) triangles."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(-size, size, nx, dtype=np.float32)
+    y = np.linspace(-size, size, ny, dtype=np.float32)
+    X, Y = np.meshgrid(x, y, indexing="xy")
+    Z = np.zeros_like(X)
+    for _ in range(4):
+        a, fx, fy, px, py = rng.uniform([0.02, 1, 1, 0, 0], [0.15, 9, 9, 6.3, 6.3])
+        Z += np.float32(a) * np.sin(np.float32(fx) * X + np.float32(px)) * np.cos(np.float32(fy) * Y + np.float32(py))
+    v = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1).astype(np.float32)
+    i = np.arange(nx * ny, dtype=np.uint32).reshape(ny, nx)
+    a, b, c, d = i[:-1, :-1].ravel(), i[:-1, 1:].ravel(), i[1:, :-1].ravel(), i[1:, 1:].ravel()
+    f = np.concatenate([np.stack([a, b, d], 1), np.stack([a, d, c], 1)]).astype(np.uint32)
+    return v, f
+
+
 def c1_mesh(seed=1):
     """The small plain workload's mesh: 81,920-triangle displaced icosphere
     (level 6, 3-octave value noise, amplitude 0.15) scaled into the unit cube
