@@ -394,6 +394,70 @@ typedef struct rq_view_t {
 rq_status_t rq_render(rq_ctx_t ctx, rq_accel_t accel, const rq_view_t* view, uint8_t* pixels, float* rgb,
                       uint64_t* ray_counts, uint32_t flags);
 
+/* ------------------------------------------------------------ serving */
+
+/* A serving loop: render requests against a library of triangle meshes,
+ * served by a worker thread that owns its own context on `device`.
+ *  - Admission: a request must name a registered mesh, and its camera rays
+ *    (width * height * spp) must fit max_batch_rays; requests whose mesh
+ *    cannot fit the HBM budget complete with RQ_ERROR_OUT_OF_MEMORY.
+ *  - Residency: meshes are kept on the host; a request's mesh is uploaded and
+ *    its LBVH built on first use.  Resident scenes and structures stay within
+ *    hbm_budget bytes by evicting the least recently used meshes the batch
+ *    being formed does not need (rebuilt when requested again).
+ *  - Continuous batching (batching = 1): every step takes the waiting
+ *    requests in arrival order up to max_batch_rays camera rays and
+ *    max_batch_requests requests and renders them as one wavefront (camera
+ *    rays, one many-structure closest-hit query, shading, one many-structure
+ *    shadow query, pixels, one download).  batching = 0 renders one request
+ *    per step.
+ *  - A request renders exactly what rq_render renders for the same view with
+ *    bounces = 0, settings.bias = 1e-4 and its width, height, spp and
+ *    background, alone or among others.
+ *  - Latency: from rq_server_submit until the pixels are in host memory.
+ * The reference has no serving path; this is the engine's own. */
+typedef struct rq_server* rq_server_t;
+typedef struct rq_server_config_t {
+  int32_t device;              /* CUDA ordinal */
+  int32_t batching;            /* 1: continuous batching; 0: one request per step */
+  uint64_t hbm_budget;         /* bytes of resident scenes + structures; 0: 80 GB */
+  uint32_t max_batch_rays;     /* camera rays per step; 0: 2^25 (below 2^31) */
+  uint32_t max_batch_requests; /* requests per step; 0: 256 */
+} rq_server_config_t;
+typedef struct rq_request_t {
+  uint32_t mesh_id;
+  uint32_t width, height, spp;
+  rq_view_t view;              /* window and bounces are ignored */
+  float background[3];
+  uint32_t keep_pixels;        /* 1: keep width*height*3 bytes for rq_server_wait */
+} rq_request_t;
+typedef struct rq_server_stats_t {
+  uint64_t submitted, completed, rejected;
+  uint64_t batches, builds, evictions;
+  uint64_t camera_rays, shadow_rays;
+  uint64_t resident_bytes, resident_meshes;
+  double busy_s;               /* worker time spent in steps */
+  double latency_ms_p50, latency_ms_p99, latency_ms_mean, latency_ms_max;
+} rq_server_stats_t;
+/* cfg may be NULL (device 0, batching on, defaults). */
+rq_status_t rq_server_create(const rq_server_config_t* cfg, rq_server_t* out);
+/* Register a mesh (copied; validated: finite vertices, indices < nv). */
+rq_status_t rq_server_add_mesh(rq_server_t s, uint32_t mesh_id, const float* verts, uint32_t nv,
+                               const uint32_t* idx, uint32_t nt);
+rq_status_t rq_server_submit(rq_server_t s, const rq_request_t* req, uint64_t* ticket);
+/* Wait for a request (timeout_s < 0: no limit; RQ_ERROR_TIMEOUT when it runs
+ * out), copy its pixels when it kept them, and forget the ticket.  Returns
+ * the request's status. */
+rq_status_t rq_server_wait(rq_server_t s, uint64_t ticket, uint8_t* pixels, double timeout_s);
+/* Wait until every submitted request has completed. */
+rq_status_t rq_server_drain(rq_server_t s, double timeout_s);
+rq_status_t rq_server_get_stats(rq_server_t s, rq_server_stats_t* out);
+rq_status_t rq_server_reset_stats(rq_server_t s);
+/* Last device-side or CUDA error the worker met (empty when none). */
+const char* rq_server_last_error(rq_server_t s);
+/* Stops the worker after its current step; drain first. */
+rq_status_t rq_server_destroy(rq_server_t s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,106 @@
+// Definitions of the C ABI's opaque handles (contexts, scenes, structures,
+// plans), shared by the translation units that implement the ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "rq_build.hpp"
+#include "rq_internal.hpp"
+
+using namespace rq;
+
+// Host-buffer queries of at least 2 chunks are streamed: chunk k+1 uploads
+// (one copy stream) and chunk k-1 downloads (another) while chunk k is traced.
+// Chunks alternate between two compute lanes (the context's stream and one
+// more, each with its own sort scratch) so that the slow tail of one chunk's
+// traversal overlaps the start of the next.
+constexpr uint32_t kPipeChunk = 1u << 21;  // rays per chunk: 64 MB up, 32 MB (or 256 KB of bits) down
+constexpr int kPipeSlots = 3;
+struct HostPipe {
+  cudaStream_t up = nullptr, down = nullptr, lane2 = nullptr;
+  BuildScratch scratch2;
+  cudaEvent_t start = nullptr, uploaded[kPipeSlots] = {}, traced[kPipeSlots] = {}, downloaded[kPipeSlots] = {};
+  DevBuf rays[kPipeSlots], out[kPipeSlots];
+  bool ready = false;
+  cudaError_t init() {
+    if (ready) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&lane2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    for (int k = 0; k < kPipeSlots && e == cudaSuccess; ++k) {
+      e = cudaEventCreateWithFlags(&uploaded[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&traced[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&downloaded[k], cudaEventDisableTiming);
+    }
+    ready = e == cudaSuccess;
+    return e;
+  }
+  void release() {
+    for (int k = 0; k < kPipeSlots; ++k) {
+      rays[k].release();
+      out[k].release();
+      if (uploaded[k]) cudaEventDestroy(uploaded[k]);
+      if (traced[k]) cudaEventDestroy(traced[k]);
+      if (downloaded[k]) cudaEventDestroy(downloaded[k]);
+      uploaded[k] = traced[k] = downloaded[k] = nullptr;
+    }
+    if (start) cudaEventDestroy(start);
+    if (up) cudaStreamDestroy(up);
+    if (down) cudaStreamDestroy(down);
+    if (lane2) cudaStreamDestroy(lane2);
+    scratch2.release();
+    start = nullptr;
+    up = down = lane2 = nullptr;
+    ready = false;
+  }
+};
+
+struct rq_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  rq_settings_t settings{};
+  std::string last_error;
+  uint32_t* d_err = nullptr;
+  int sm_count = 0;
+  DevBuf stage_in, stage_out, stage_aux;
+  BuildScratch scratch;
+  RenderScratch render;
+  HostPipe pipe;
+  DevBuf batch_table;  // views + ray offsets + work counter of rq_trace_batched
+};
+
+struct rq_plan {
+  rq_ctx_t ctx = nullptr;
+  std::vector<rq_accel_t> accels;
+  std::shared_ptr<BatchStore> store;  // set when the plan rebuilds a batch
+  BatchedTrace trace;
+  DevBuf table;
+  int block = 128, deep = 1;
+  float shape_ms[4] = {-1.f, -1.f, -1.f, -1.f};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;
+};
+
+struct rq_scene {
+  rq_ctx_t ctx = nullptr;
+  int kind = kTriangles;
+  uint32_t n = 0;   // primitives
+  uint32_t nv = 0;  // vertices (triangles)
+  DevBuf verts, idx, sph;
+};
+
+struct rq_accel {
+  rq_ctx_t ctx = nullptr;
+  rq_scene_t scene = nullptr;
+  int type = RQ_NONE;
+  AccelBuffers buf;
+  std::shared_ptr<BatchStore> batch;  // set when buf borrows a batched build's arrays
+  uint32_t batch_index = 0;
+};
+

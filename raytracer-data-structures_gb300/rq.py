@@ -90,6 +90,82 @@ class Plan:
             self.handle = None
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("batching", C.c_int32), ("hbm_budget", C.c_uint64),
+                ("max_batch_rays", C.c_uint32), ("max_batch_requests", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("mesh_id", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("view", View), ("background", C.c_float * 3), ("keep_pixels", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("batches", C.c_uint64), ("builds", C.c_uint64), ("evictions", C.c_uint64),
+                ("camera_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("resident_bytes", C.c_uint64),
+                ("resident_meshes", C.c_uint64), ("busy_s", C.c_double), ("latency_ms_p50", C.c_double),
+                ("latency_ms_p99", C.c_double), ("latency_ms_mean", C.c_double), ("latency_ms_max", C.c_double)]
+
+
+class Server:
+    """rq_server_t: the serving loop (admission, HBM budget with LRU residency,
+    continuous batching, latency statistics) on its own worker thread."""
+
+    def __init__(self, device=0, batching=True, hbm_budget=0, max_batch_rays=0, max_batch_requests=0):
+        lib = load()
+        cfg = ServerConfig(device, int(batching), hbm_budget, max_batch_rays, max_batch_requests)
+        self.handle = C.c_void_p()
+        self._check(lib.rq_server_create(C.byref(cfg), C.byref(self.handle)))
+        self._sizes = {}
+
+    @staticmethod
+    def _check(st):
+        if st != SUCCESS:
+            raise RqError(st, STATUS_NAMES.get(st, str(st)))
+
+    def add_mesh(self, mesh_id, verts, idx):
+        verts = np.ascontiguousarray(verts, np.float32)
+        idx = np.ascontiguousarray(idx, np.uint32)
+        self._check(load().rq_server_add_mesh(self.handle, mesh_id, verts.ctypes.data, verts.size // 3,
+                                              idx.ctypes.data, idx.size // 3))
+
+    def submit(self, mesh_id, view, width, height, spp=1, background=(1.0, 1.0, 1.0), keep_pixels=True):
+        r = Request()
+        r.mesh_id, r.width, r.height, r.spp = mesh_id, width, height, spp
+        r.view = view
+        r.background[:] = background
+        r.keep_pixels = int(keep_pixels)
+        t = C.c_uint64()
+        self._check(load().rq_server_submit(self.handle, C.byref(r), C.byref(t)))
+        self._sizes[t.value] = (height, width)
+        return t.value
+
+    def wait(self, ticket, timeout_s=-1.0, want_pixels=True):
+        """(status, pixels (h, w, 3) or None)."""
+        h, w = self._sizes.pop(ticket, (0, 0))
+        pix = np.zeros((h, w, 3), np.uint8) if want_pixels and h else None
+        st = load().rq_server_wait(self.handle, C.c_uint64(ticket), pix.ctypes.data if pix is not None else None,
+                                   C.c_double(timeout_s))
+        return st, pix
+
+    def drain(self, timeout_s=-1.0):
+        self._check(load().rq_server_drain(self.handle, C.c_double(timeout_s)))
+
+    def stats(self):
+        s = ServerStats()
+        self._check(load().rq_server_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def reset_stats(self):
+        self._check(load().rq_server_reset_stats(self.handle))
+
+    def close(self):
+        if self.handle:
+            load().rq_server_destroy(self.handle)
+            self.handle = None
+
+
 class RqError(RuntimeError):
     def __init__(self, status, message):
         self.status = status
@@ -151,6 +227,15 @@ def load(build_if_missing=True):
         "rq_plan_launch": (i32, [vp]),
         "rq_plan_get_info": (i32, [vp, vp]),
         "rq_plan_destroy": (i32, [vp]),
+        "rq_server_create": (i32, [vp, vp]),
+        "rq_server_add_mesh": (i32, [vp, u32, vp, u32, vp, u32]),
+        "rq_server_submit": (i32, [vp, vp, vp]),
+        "rq_server_wait": (i32, [vp, C.c_uint64, vp, C.c_double]),
+        "rq_server_drain": (i32, [vp, C.c_double]),
+        "rq_server_get_stats": (i32, [vp, vp]),
+        "rq_server_reset_stats": (i32, [vp]),
+        "rq_server_last_error": (C.c_char_p, [vp]),
+        "rq_server_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
