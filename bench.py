@@ -343,6 +343,10 @@ def run_ours(args):
     if not args.skip_batch:
         batched = run_batch_leg(eng, stream, dev, args)
 
+    served = None
+    if not args.skip_serve and ws == 1:
+        served = run_serve_leg(args)
+
     e2e = None
     if rank == 0 and not args.skip_e2e:
         e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice)
@@ -376,6 +380,7 @@ def run_ours(args):
             "structures": structures,
             "render": render,
             "batched": batched,
+            "served": served,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),
         }
         print(json.dumps(out), flush=True)
@@ -566,6 +571,80 @@ def run_batch_leg(eng, stream, dev, args):
     return out
 
 
+def run_serve_leg(args):
+    """The serving loop under load: Poisson arrivals at 400 requests/s for a
+    few seconds; 32 resident terrain meshes of 10k-2M triangles (log-uniform)
+    plus new meshes (5% of requests name a mesh never seen before: upload +
+    LBVH build on demand); resolution uniform over 320x240, 640x480, 1280x720,
+    1920x1080, spp over 1, 2, 4, 8, 16; HBM budget 80 GB with LRU eviction.
+    The same request stream is served with continuous batching and one
+    request per step; latency = submit to pixels in host memory."""
+    import rq
+    import scenes
+
+    rng = np.random.default_rng(SEED + 50)
+    rate, secs = 400.0, (1.0 if args.small else 4.0)
+    n_res, n_new_max = 32, 64
+
+    def mesh(seed):
+        t = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        nx = max(2, int(round(np.sqrt(t / 2)))) + 1
+        return scenes.wave_heightfield(nx, nx, seed=seed)
+
+    lib = {k: mesh(SEED + 200 + k) for k in range(n_res)}
+    fresh = {1000 + k: mesh(SEED + 400 + k) for k in range(n_new_max)}
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * secs * 1.2)))
+    arrivals = arrivals[arrivals < secs]
+    res = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+    sched, new_ids = [], iter(sorted(fresh))
+    for k, t in enumerate(arrivals):
+        mid = next(new_ids, None) if rng.random() < 0.05 else None
+        if mid is None:
+            mid = int(rng.integers(n_res))
+        w, h = res[int(rng.integers(4))]
+        spp = int(rng.choice([1, 2, 4, 8, 16]))
+        az = rng.uniform(0, 6.283)
+        view = rq.make_view(eye=(float(2.2 * np.cos(az)), float(2.2 * np.sin(az)), float(rng.uniform(0.5, 1.5))),
+                            target=(0.0, 0.0, 0.0), up=(0.0, 0.0, 1.0), fov_deg=float(rng.uniform(35, 60)),
+                            light=(1.0, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=int(SEED + k))
+        sched.append((float(t), mid, view, w, h, spp))
+    out = {"requests": len(sched), "rate_per_s": rate, "seconds": secs,
+           "resident_meshes": n_res, "new_mesh_requests": sum(1 for s in sched if s[1] >= 1000),
+           "triangles_resident": int(sum(len(f) for _, f in lib.values()))}
+    for mode, batching in (("batched", True), ("one_per_step", False)):
+        srv = rq.Server(batching=batching, hbm_budget=80 << 30)
+        for mid, (v, f) in list(lib.items()) + list(fresh.items()):
+            srv.add_mesh(mid, v, f)
+        for mid in lib:  # the library starts resident
+            srv.wait(srv.submit(mid, sched[0][2], 32, 32, 1, keep_pixels=False), want_pixels=False)
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        tickets = []
+        for t, mid, view, w, h, spp in sched:
+            lag = t - (time.perf_counter() - t0)
+            if lag > 0:
+                time.sleep(lag)
+            tickets.append(srv.submit(mid, view, w, h, spp, keep_pixels=False))
+        srv.drain()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        rays = int(st.camera_rays + st.shadow_rays)
+        out[mode] = {"completed": int(st.completed), "rejected": int(st.rejected), "steps": int(st.batches),
+                     "builds": int(st.builds), "evictions": int(st.evictions),
+                     "p50_ms": round(st.latency_ms_p50, 3), "p99_ms": round(st.latency_ms_p99, 3),
+                     "mean_ms": round(st.latency_ms_mean, 3), "max_ms": round(st.latency_ms_max, 3),
+                     "wall_s": round(wall, 3), "busy_s": round(st.busy_s, 3), "rays": rays,
+                     "grays_s_wall": round(rays / wall / 1e9, 4), "grays_s_busy": round(rays / max(st.busy_s, 1e-9) / 1e9, 4)}
+        for tk in tickets:
+            srv.wait(tk, want_pixels=False)
+        srv.close()
+        log(f"[bench] serve {mode}: {out[mode]}")
+    b, o = out["batched"], out["one_per_step"]
+    out["busy_rays_ratio"] = round(b["grays_s_busy"] / max(o["grays_s_busy"], 1e-9), 3)
+    out["p99_ratio"] = round(o["p99_ms"] / max(b["p99_ms"], 1e-9), 3)
+    return out
+
+
 def build_bytes_per_tri():
     """Compulsory bytes per triangle of the LBVH build kernels:
     bounds 6 (12 B per vertex, 0.5 vertex per triangle) + Morton 26 (12 B indices,
@@ -743,6 +822,7 @@ def main():
     ap.add_argument("--skip-structures", action="store_true", help="skip the BVH / KDTREE comparison")
     ap.add_argument("--skip-render", action="store_true", help="skip the render-step legs")
     ap.add_argument("--skip-batch", action="store_true", help="skip the many-scene leg")
+    ap.add_argument("--skip-serve", action="store_true", help="skip the serving-loop leg")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")
