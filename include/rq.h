@@ -394,6 +394,35 @@ typedef struct rq_view_t {
 rq_status_t rq_render(rq_ctx_t ctx, rq_accel_t accel, const rq_view_t* view, uint8_t* pixels, float* rgb,
                       uint64_t* ray_counts, uint32_t flags);
 
+/* ------------------------------------------------------------ scene I/O */
+
+/* Wavefront OBJ meshes (host only; no context or GPU needed).  rq_obj_load
+ * reads `v x y z` records and `f` records with the v, v/vt, v/vt/vn or v//vn
+ * corner forms, 1-based or negative (relative to the vertices read so far);
+ * a polygon of k > 3 corners becomes k - 2 triangles around its first
+ * corner; every other record (vn, vt, o, g, s, usemtl, mtllib, #) is
+ * skipped.  A file without `f` records gives nt = 0 (a point cloud: the form
+ * of the reference's models, which its loader, main.cpp:650-718, reads as
+ * `v` records only).  verts (nv * 3 floats) and idx (nt * 3) are allocated by
+ * the library; release them with rq_free.  Malformed records, out-of-range
+ * corners and unreadable files: RQ_ERROR_INVALID_ARGUMENT. */
+rq_status_t rq_obj_load(const char* path, float** verts, uint32_t* nv, uint32_t** idx, uint32_t* nt);
+/* `v` records in the shortest form that reads back to the same float, then
+ * 1-based `f` records. */
+rq_status_t rq_obj_save(const char* path, const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt);
+void rq_free(void* p);
+/* createScene_new's model file (main.cpp:605-643): <dir>/<name>.obj for a
+ * rq_scene_model_t (other values: test.obj), the name matched without regard
+ * to case (the reference asks for "igea.obj"; its file is "Igea.obj").  out
+ * receives the path (cap bytes including the terminating NUL). */
+rq_status_t rq_model_path(const char* dir, int32_t scene_model, char* out, uint32_t cap);
+/* createScene_new's spheres from a model file: each `v` record up to the
+ * first other token becomes a sphere of radius 0.05 at v * 100 + shift, then
+ * y - 10, z - 60 (shift = 20 * clone, for `clones` copies), followed by the
+ * ground sphere of radius 100 (main.cpp:650-718).  spheres: n * 4 floats,
+ * released with rq_free. */
+rq_status_t rq_reference_spheres(const char* path, int32_t clones, float** spheres, uint32_t* n);
+
 /* ------------------------------------------------------------ serving */
 
 /* A serving loop: render requests against a library of triangle meshes,

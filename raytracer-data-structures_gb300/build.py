@@ -1,7 +1,7 @@
 """Build recipe for the engine library (librq.so) — nvcc, sm_103a only.
 
-Each .cu in csrc/ is compiled to an object in parallel, then linked into
-librq.so next to this file.  Used by __graft_entry__.build() and by rq.py when
+Each .cu in csrc/ (nvcc) and each .cpp (the host C++ compiler) is compiled
+to an object in parallel, then linked into librq.so next to this file.  Used by __graft_entry__.build() and by rq.py when
 the library is missing.
 """
 import concurrent.futures as cf
@@ -31,7 +31,7 @@ def nvcc():
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _newest_input():
@@ -49,10 +49,17 @@ def build(force=False, verbose=False):
     cc = nvcc()
     srcs = sources()
 
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc, *ARCH, *NVFLAGS, "-c", src, "-o", obj]
-        if verbose:
+        obj = os.path.join(OUT_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
+        if src.endswith(".cpp"):  # host-only code
+            # no contraction of a*b+c, so x86 and Arm builds round alike
+            cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+                   "-c", src, "-o", obj]
+        else:
+            cmd = [cc, *ARCH, *NVFLAGS, "-c", src, "-o", obj]
+        if verbose and not src.endswith(".cpp"):
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -75,7 +82,8 @@ def build(force=False, verbose=False):
 def build_driver():
     """The C++ host program over the C ABI (host/rq_render_main.cpp)."""
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(HERE, "host"),
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(HERE, "host"),
            os.path.join(HERE, "host", "rq_render_main.cpp"), "-L", HERE, "-lrq", "-Wl,-rpath,$ORIGIN",
            "-o", DRIVER]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -153,29 +153,51 @@ inline Accel build(Context& c, const Scene& s, int dataStructure) { return Accel
 
 // createScene_new's loader (main.cpp:650-718): every `v x y z` line up to the
 // first other token becomes a sphere of radius 0.05 at v*100 + (0,-10,-60)
-// (+20 per clone), then the ground sphere of radius 100 is appended.
+// (+20 per clone), then the ground sphere of radius 100 is appended
+// (rq_reference_spheres).
 inline std::vector<SphereRecord> loadReferenceScene(const std::string& objPath, int clones = 1) {
-  std::vector<SphereRecord> out;
-  for (int clone = 0; clone < clones; ++clone) {
-    float shift = clone * 20.f;
-    std::ifstream f(objPath);
-    if (!f.good()) throw Error(RQ_ERROR_INVALID_ARGUMENT, "cannot open " + objPath);
-    std::string tok;
-    while (f >> tok && tok == "v") {
-      float x, y, z;
-      f >> x >> y >> z;
-      SphereRecord s;
-      s.center[0] = x * 100 + shift;
-      s.center[1] = y * 100 + shift;
-      s.center[2] = z * 100 + shift;
-      s.center[1] += -10;
-      s.center[2] += -60;
-      s.radius = (float)(0.01 * 5);  // the reference multiplies in double, then stores to float
-      out.push_back(s);
-    }
-  }
-  out.push_back(SphereRecord{{0.93591022f, -105.47120094f, -43.2363205f}, 100.f});
+  float* p = nullptr;
+  uint32_t n = 0;
+  rq_status_t st = rq_reference_spheres(objPath.c_str(), clones, &p, &n);
+  if (st != RQ_SUCCESS) throw Error(st, "cannot load " + objPath);
+  std::vector<SphereRecord> out(n);
+  for (uint32_t i = 0; i < n; ++i)
+    out[i] = SphereRecord{{p[4 * i], p[4 * i + 1], p[4 * i + 2]}, p[4 * i + 3]};
+  rq_free(p);
   return out;
+}
+
+// createScene_new's model file for settings.sceneModel under `dir`, the name
+// matched without regard to case (rq_model_path).
+inline std::string modelPath(const std::string& dir, int sceneModel) {
+  char buf[4096];
+  rq_status_t st = rq_model_path(dir.c_str(), sceneModel, buf, sizeof(buf));
+  if (st != RQ_SUCCESS) throw Error(st, "no model file in " + dir);
+  return buf;
+}
+
+// A triangle mesh read from / written to a Wavefront OBJ file (v / f records).
+struct Mesh {
+  std::vector<float> verts;    // nv * 3
+  std::vector<uint32_t> idx;   // nt * 3
+};
+inline Mesh loadObj(const std::string& path) {
+  float* v = nullptr;
+  uint32_t* f = nullptr;
+  uint32_t nv = 0, nt = 0;
+  rq_status_t st = rq_obj_load(path.c_str(), &v, &nv, &f, &nt);
+  if (st != RQ_SUCCESS) throw Error(st, "cannot load " + path);
+  Mesh m;
+  m.verts.assign(v, v + (size_t)nv * 3);
+  m.idx.assign(f, f + (size_t)nt * 3);
+  rq_free(v);
+  rq_free(f);
+  return m;
+}
+inline void saveObj(const std::string& path, const Mesh& m) {
+  rq_status_t st = rq_obj_save(path.c_str(), m.verts.data(), (uint32_t)(m.verts.size() / 3), m.idx.data(),
+                               (uint32_t)(m.idx.size() / 3));
+  if (st != RQ_SUCCESS) throw Error(st, "cannot save " + path);
 }
 
 // Surface colours of those spheres: (0.8, 0.7, 0) per vertex sphere

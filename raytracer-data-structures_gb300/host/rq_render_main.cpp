@@ -2,10 +2,13 @@
 // load the scene the way createScene_new does, build the structure chosen by
 // settings.dataStructure, render the 640x480 image and write it as P6.
 //
-//   rq_render [--model file.obj | --spheres file.xyzr] [--structure BVH|KDTREE|LBVH|NONE]
-//             [--out output.ppm] [--width W] [--height H] [--aa N] [--device D]
-//             [--dump-spheres file.xyzr]
+//   rq_render [--model file.obj | --spheres file.xyzr | --models DIR --scene-model NAME]
+//             [--structure BVH|KDTREE|LBVH|NONE] [--out output.ppm] [--width W]
+//             [--height H] [--aa N] [--device D] [--dump-spheres file.xyzr]
 //
+// Without --model or --spheres the model is settings.sceneModel's file under
+// --models (default "models"), as createScene_new picks it, with the name
+// matched without regard to case.
 // --spheres reads raw little-endian float32 (cx, cy, cz, r) records, the
 // sphere list createScene_new produces.
 #include <chrono>
@@ -38,6 +41,14 @@ int structure_of(const std::string& name) {
   throw rq::Error(RQ_ERROR_INVALID_ARGUMENT, "unknown structure " + name);
 }
 
+// SceneModel names (settings.h:4).
+int scene_model_of(const std::string& name) {
+  const char* names[] = {"IGEA", "ARMADILLO", "BUNNY", "BUNNIES", "TEST", "GRASS", "BUDDHA", "CITY"};
+  for (int k = 0; k < 8; ++k)
+    if (name == names[k]) return k;
+  throw rq::Error(RQ_ERROR_INVALID_ARGUMENT, "unknown scene model " + name);
+}
+
 double seconds_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -45,7 +56,7 @@ double seconds_since(std::chrono::steady_clock::time_point t0) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  std::string model, spheres_path, dump, out = "output.ppm";
+  std::string model, spheres_path, dump, out = "output.ppm", models_dir = "models";
   rq::Settings settings;
   int device = 0;
   for (int i = 1; i < argc; ++i) {
@@ -63,6 +74,8 @@ int main(int argc, char** argv) {
     else if (a == "--aa") settings.aa_samples = (uint32_t)std::stoul(next());
     else if (a == "--device") device = std::stoi(next());
     else if (a == "--dump-spheres") dump = next();  // write the loaded sphere list and stop
+    else if (a == "--models") models_dir = next();
+    else if (a == "--scene-model") settings.sceneModel = scene_model_of(next());
     else {
       std::cerr << "unknown argument " << a << "\n";
       return 2;
@@ -70,8 +83,9 @@ int main(int argc, char** argv) {
   }
   try {
     auto t0 = std::chrono::steady_clock::now();
+    if (spheres_path.empty() && model.empty()) model = rq::modelPath(models_dir, settings.sceneModel);
     std::vector<rq::SphereRecord> spheres =
-        !spheres_path.empty() ? read_spheres(spheres_path) : rq::loadReferenceScene(model.empty() ? "models/bunny.obj" : model);
+        !spheres_path.empty() ? read_spheres(spheres_path) : rq::loadReferenceScene(model);
     std::cout << "Number of spheres: " << spheres.size() << "\n";
     if (!dump.empty()) {
       std::ofstream f(dump, std::ios::binary);

@@ -20,6 +20,8 @@ TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
 RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON = 0, 1
 NODE_WIDTH_2, NODE_WIDTH_4 = 0, 4
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1
+# SceneModel (settings.h:4)
+IGEA, ARMADILLO, BUNNY_MODEL, BUNNIES, TEST, GRASS, BUDDHA, CITY = range(8)
 DEVICE_POINTERS = 0x1
 MISS = 0xFFFFFFFF
 
@@ -227,6 +229,11 @@ def load(build_if_missing=True):
         "rq_plan_launch": (i32, [vp]),
         "rq_plan_get_info": (i32, [vp, vp]),
         "rq_plan_destroy": (i32, [vp]),
+        "rq_obj_load": (i32, [C.c_char_p, vp, vp, vp, vp]),
+        "rq_obj_save": (i32, [C.c_char_p, vp, u32, vp, u32]),
+        "rq_free": (None, [vp]),
+        "rq_model_path": (i32, [C.c_char_p, i32, vp, u32]),
+        "rq_reference_spheres": (i32, [C.c_char_p, i32, vp, vp]),
         "rq_server_create": (i32, [vp, vp]),
         "rq_server_add_mesh": (i32, [vp, u32, vp, u32, vp, u32]),
         "rq_server_submit": (i32, [vp, vp, vp]),
@@ -538,6 +545,53 @@ def sort_pairs_noalloc(keys_ptr, vals_ptr, n, key_bits=32, stream_ptr=None):
     """rq_sort_pairs_noalloc on device buffers (pointers as ints); returns the status.
     Allocates nothing: for callers that cannot allocate device memory mid-run."""
     return int(load().rq_sort_pairs_noalloc(keys_ptr, vals_ptr, n, key_bits, stream_ptr))
+
+
+def _take(ptr, count, dtype, width):
+    """Copy a library-allocated array into numpy and release it."""
+    try:
+        if count == 0:
+            return np.zeros((0, width), dtype)
+        buf = (C.c_char * (count * width * np.dtype(dtype).itemsize)).from_address(ptr.value)
+        return np.frombuffer(bytes(buf), dtype).reshape(count, width).copy()
+    finally:
+        load().rq_free(ptr)
+
+
+def obj_load(path):
+    """rq_obj_load: (verts (nv, 3) float32, idx (nt, 3) uint32)."""
+    pv, pi = C.c_void_p(), C.c_void_p()
+    nv, nt = C.c_uint32(), C.c_uint32()
+    st = load().rq_obj_load(os.fsencode(path), C.byref(pv), C.byref(nv), C.byref(pi), C.byref(nt))
+    if st != SUCCESS:
+        raise RqError(st, f"cannot load {path}")
+    return _take(pv, nv.value, np.float32, 3), _take(pi, nt.value, np.uint32, 3)
+
+
+def obj_save(path, verts, idx):
+    verts = np.ascontiguousarray(verts, np.float32)
+    idx = np.ascontiguousarray(idx, np.uint32)
+    st = load().rq_obj_save(os.fsencode(path), verts.ctypes.data, verts.size // 3, idx.ctypes.data, idx.size // 3)
+    if st != SUCCESS:
+        raise RqError(st, f"cannot save {path}")
+
+
+def model_path(directory, scene_model):
+    """rq_model_path: the model file of a SceneModel value, matched without regard to case."""
+    buf = C.create_string_buffer(4096)
+    st = load().rq_model_path(os.fsencode(directory), scene_model, buf, len(buf))
+    if st != SUCCESS:
+        raise RqError(st, f"no model file for {scene_model} in {directory}")
+    return buf.value.decode()
+
+
+def reference_spheres(path, clones=1):
+    """rq_reference_spheres: createScene_new's spheres (n, 4) from a model file."""
+    ps, n = C.c_void_p(), C.c_uint32()
+    st = load().rq_reference_spheres(os.fsencode(path), clones, C.byref(ps), C.byref(n))
+    if st != SUCCESS:
+        raise RqError(st, f"cannot load {path}")
+    return _take(ps, n.value, np.float32, 4)
 
 
 def kernel_launch_count():

@@ -64,3 +64,17 @@ def test_driver_renders_reference_image(driver, tmp_path, structure):
         assert diff.max() <= 1
     else:
         assert data.size == 15 + 640 * 480 * 3
+
+
+def test_driver_finds_the_model_without_regard_to_case(driver, tmp_path):
+    """createScene_new asks for "igea.obj"; the reference ships "Igea.obj"."""
+    (tmp_path / "Igea.obj").write_text("v 0.1 0.2 0.3\nv -0.25 0.5 0.125\n")
+    out = tmp_path / "igea.xyzr"
+    r = subprocess.run([driver, "--models", str(tmp_path), "--scene-model", "IGEA", "--dump-spheres", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(out, np.float32).reshape(-1, 4)
+    assert got.shape == (3, 4) and got[-1, 3] == 100  # two vertex spheres + the ground
+    r = subprocess.run([driver, "--models", str(tmp_path), "--scene-model", "ARMADILLO", "--dump-spheres", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "no model file" in r.stderr
