@@ -809,6 +809,60 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_case(args):
+    """Profiling driver (no bench line): one query class of the benchmark
+    workload run warmup + steps times, for ncu captures of a single kernel.
+    Cases: primary, secondary, shadow (the LBVH traversal kernels, with
+    --ray-sort 0/1), build (the LBVH rebuild), batched (the many-structure
+    persistent query on the many-scene workload, 32 scenes with --small)."""
+    import torch
+    import rq
+    import scenes
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    eng = rq.Engine(0)
+    eng.set_stream(stream.cuda_stream)
+    if args.case == "batched":
+        rng = np.random.default_rng(SEED + 40)
+        n_sc = 32 if args.small else 256
+        tri_t = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_sc))
+        ray_n = np.exp(rng.uniform(np.log(64e3), np.log(2e6), n_sc)).astype(np.int64)
+        meshes = [scenes.wave_heightfield(max(2, int(round(np.sqrt(t / 2)))) + 1,
+                                          max(2, int(round(np.sqrt(t / 2)))) + 1, seed=SEED + 100 + k)
+                  for k, t in enumerate(tri_t)]
+        sc = [eng.scene_triangles(v, f) for v, f in meshes]
+        accs = eng.build_batched(sc, rq.LBVH)
+        offs = np.zeros(n_sc + 1, np.uint32)
+        offs[1:] = np.cumsum(ray_n)
+        d_rays = batch_rays(torch, dev, meshes, ray_n.tolist(), SEED + 41)
+        d_hits = torch.empty(int(offs[-1]) * HIT_BYTES, dtype=torch.uint8, device=dev)
+        call = lambda: eng.trace_batched(accs, d_rays, offs, out=d_hits)  # noqa: E731
+    else:
+        verts, idx, primary = make_inputs(args.small)
+        scene = eng.scene_triangles(verts, idx)
+        acc = eng.build(scene, rq.LBVH)
+        hits_p = eng.trace_closest(acc, primary)
+        rays = {"primary": primary, "build": primary,
+                "secondary": scenes.cosine_rays(verts, idx, primary, hits_p, seed=SEED + 2),
+                "shadow": scenes.shadow_rays(verts, idx, primary, hits_p, LIGHT)}[args.case]
+        d_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8)).to(dev)
+        d_out = torch.empty(len(rays) * HIT_BYTES, dtype=torch.uint8, device=dev)
+        eng.configure(ray_sort=args.ray_sort)
+        if args.case == "build":
+            call = acc.rebuild
+        elif args.case == "shadow":
+            call = lambda: eng.trace_any(acc, d_rays, d_out)  # noqa: E731
+        else:
+            call = lambda: eng.trace_closest(acc, d_rays, d_out)  # noqa: E731
+    for _ in range(args.warmup + args.steps):
+        call()
+    eng.synchronize()
+    log(f"[bench] case {args.case}: {args.warmup + args.steps} launches done")
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -823,7 +877,13 @@ def main():
     ap.add_argument("--skip-render", action="store_true", help="skip the render-step legs")
     ap.add_argument("--skip-batch", action="store_true", help="skip the many-scene leg")
     ap.add_argument("--skip-serve", action="store_true", help="skip the serving-loop leg")
+    ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "batched"],
+                    help="profiling driver: run one query class, print no bench line")
+    ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")
         args.warmup = 3
