@@ -79,8 +79,17 @@ typedef struct rq_settings_t {
   int32_t kd_max_depth;       /* <= 0: round(8 + 1.3 log2 N) as the reference (accelerators.h:958) */
   int32_t ray_sort;           /* rq_ray_sort_t: reorder large FAST batches for coherence */
   int32_t node_width;         /* rq_node_width_t: BVH node fan-out for FAST queries (RQ_BVH, RQ_LBVH) */
-  int32_t reserved[3];
+  int32_t scheduling;         /* rq_scheduling_t: how FAST binary-BVH queries map rays to threads */
+  int32_t reserved[2];
 } rq_settings_t;
+
+/* How FAST queries on binary BVH structures map rays to GPU threads.  Speed
+ * only: every ray walks the same nodes in the same order either way. */
+typedef enum rq_scheduling_t {
+  RQ_SCHEDULING_THREAD_PER_RAY = 0, /* one thread per ray */
+  RQ_SCHEDULING_LANE_REFILL = 1,    /* persistent warps refill finished lanes with new rays */
+  RQ_SCHEDULING_SPECULATIVE = 2     /* while-while walk that postpones leaves until the warp has one each */
+} rq_scheduling_t;
 
 /* Node fan-out of BVH structures (RQ_BVH, RQ_LBVH), fixed when the structure
  * is built.  RQ_NODE_WIDTH_4 adds a collapsed 4-wide copy of the binary tree
@@ -105,7 +114,10 @@ typedef enum rq_ray_sort_t {
 typedef enum rq_traversal_t {
   /* Reciprocal-direction slab test clipped to [tmin, closest hit], widened by
    * 1 + 2*gamma(3) so no box is lost to rounding; near child first; hits
-   * limited to (tmin, tmax). */
+   * limited to (tmin, tmax).  BVH and brute-force closest hit is the smallest
+   * t and, among primitives hit at exactly that t, the smallest primitive id:
+   * a result independent of the order of the walk (node width, scheduling,
+   * ray reordering). */
   RQ_TRAVERSAL_FAST = 0,
   /* The reference's semantics: division slab test with no clipping
    * (accelerators.h:588-626), boxIntersect's pre-order candidate walk

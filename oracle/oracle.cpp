@@ -131,6 +131,17 @@ inline bool test_prim(int kind, int mode, const float* prims, uint32_t id, V3 o,
   return t > tmin && t < best;
 }
 
+// FAST closest-hit acceptance: a smaller t, or the same t with a smaller
+// primitive id, so that the chosen hit does not depend on the order in which
+// a walk meets the primitives (tree shape, node width, scheduling).  Hits
+// stay inside (tmin, tmax).
+inline bool closest_fast(int kind, const float* prims, uint32_t id, V3 o, V3 d, float tmin, const orc_hit_t& h,
+                         float& t, float& u, float& v) {
+  const float bound = h.prim == kMiss ? h.t : std::nextafter(h.t, INFINITY);
+  if (!test_prim(kind, ORC_MODE_FAST, prims, id, o, d, tmin, bound, t, u, v)) return false;
+  return t < h.t || id < h.prim;
+}
+
 // Any-hit acceptance.  REFERENCE spheres: kdtreeIntersect returns on any
 // successful sphere test (accelerators.h:1020,1030).
 inline bool test_prim_any(int kind, int mode, const float* prims, uint32_t id, V3 o, V3 d,
@@ -299,7 +310,9 @@ void trace_one_bvh2(int kind, int mode, int query, const float* nodes, uint32_t 
           }
         } else {
           float t, u, v;
-          if (test_prim(kind, mode, prims, id, o, d, ray.tmin, best, t, u, v)) {
+          const bool take = mode == ORC_MODE_FAST ? closest_fast(kind, prims, id, o, d, ray.tmin, hit, t, u, v)
+                                                  : test_prim(kind, mode, prims, id, o, d, ray.tmin, best, t, u, v);
+          if (take) {
             best = t;
             hit.t = t;
             hit.prim = id;
@@ -1135,7 +1148,7 @@ int orc_trace_bvh4(int kind, int query, const float* nodes32, uint32_t n4, const
               }
             } else {
               float t, u, v;
-              if (test_prim(kind, ORC_MODE_FAST, prims, id, o, d, ray.tmin, best, t, u, v)) {
+              if (closest_fast(kind, prims, id, o, d, ray.tmin, h, t, u, v)) {
                 best = t;
                 h = {t, id, u, v};
               }

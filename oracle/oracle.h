@@ -79,6 +79,9 @@ int orc_build_kd(const float* aabb6, uint32_t n, int32_t max_depth, int32_t* nod
                  uint32_t* n_idx, float* root_bounds6);
 
 /* ---- ray queries ---- */
+/* FAST closest hit: the smallest t in (tmin, tmax) and, among primitives hit
+ * at exactly that t, the smallest primitive id (independent of traversal
+ * order).  REFERENCE: the reference's first closest in candidate order. */
 /* prims: triangles = 9 floats per primitive id (v0, e1 = v1-v0, e2 = v2-v0);
  * spheres = 4 floats per primitive id (centre, radius).
  * counters (may be NULL): [0] += internal nodes visited, [1] += primitive tests. */

@@ -174,28 +174,43 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
 BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers& a, const rq_settings_t& cfg,
                                 bool any, const QueryTarget& q, BuildScratch& sc, uint32_t* err, cudaStream_t st) {
   const bool bvh2 = type == RQ_LBVH || type == RQ_BVH;
-  if (!bvh2 || cfg.traversal != RQ_TRAVERSAL_FAST || cfg.ray_sort != RQ_RAY_SORT_OCTANT_MORTON ||
-      q.n < kRaySortMin) {
+  const bool fast = bvh2 && cfg.traversal == RQ_TRAVERSAL_FAST;
+  const bool sorted = fast && cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON && q.n >= kRaySortMin;
+  const bool refill = fast && cfg.scheduling == RQ_SCHEDULING_LANE_REFILL && a.node_width != 4;
+  const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && a.node_width != 4;
+  if (!sorted && !refill && !spec) {
     launch_query(type, s, a, cfg.traversal, any, q, err, st);
     RQ_B(cudaGetLastError(), "trace launch");
     return {};
   }
-  // Coherence order: sort (octant | origin Morton, index) pairs, then trace
-  // through the permutation; results keep the caller's order.
-  RQ_B(sc.keys.ensure((size_t)q.n * 4), "ray sort scratch");
-  RQ_B(sc.vals.ensure((size_t)q.n * 4), "ray sort scratch");
-  uint32_t* keys = sc.keys.as<uint32_t>();
-  uint32_t* perm = sc.vals.as<uint32_t>();
-  launch_ray_keys(q.rays, q.n, a.root.as<const float>(), keys, perm, st);
-  BuildResult r = sort_pairs(keys, perm, q.n, 4, true, sc, err, st);
-  if (!r.ok()) return r;
-  if (a.node_width == 4) {
-    launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
-  } else {
-    Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
-               a.root.as<const float>(), a.n_nodes, a.n_slots};
-    launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm);
+  const uint32_t* perm = nullptr;
+  if (sorted) {
+    // Coherence order: sort (octant | origin Morton, index) pairs, then trace
+    // through the permutation; results keep the caller's order.
+    RQ_B(sc.keys.ensure((size_t)q.n * 4), "ray sort scratch");
+    RQ_B(sc.vals.ensure((size_t)q.n * 4), "ray sort scratch");
+    uint32_t* keys = sc.keys.as<uint32_t>();
+    uint32_t* p = sc.vals.as<uint32_t>();
+    launch_ray_keys(q.rays, q.n, a.root.as<const float>(), keys, p, st);
+    BuildResult r = sort_pairs(keys, p, q.n, 4, true, sc, err, st);
+    if (!r.ok()) return r;
+    perm = p;
   }
+  Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+             a.root.as<const float>(), a.n_nodes, a.n_slots};
+  if (spec) {
+    launch_trace_bvh2_spec(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, perm, st);
+    RQ_B(cudaGetLastError(), "trace launch");
+    return {};
+  }
+  if (refill) {
+    RQ_B(sc.work.ensure(256), "traversal work counter");
+    RQ_B(launch_trace_bvh2_refill(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, perm, sc.work.as<uint32_t>(), st),
+         "trace launch");
+    return {};
+  }
+  if (a.node_width == 4) launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
+  else launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm);
   RQ_B(cudaGetLastError(), "trace launch");
   return {};
 }

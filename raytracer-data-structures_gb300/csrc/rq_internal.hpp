@@ -116,6 +116,14 @@ struct Bvh2View {
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
                        uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
                        const uint32_t* perm = nullptr);
+// FAST traversal by persistent warps that refill finished lanes (one work
+// word, zeroed by the launcher); same results as launch_trace_bvh2.
+cudaError_t launch_trace_bvh2_refill(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n,
+                                     float4* hits, uint32_t* occ, uint32_t* err, const uint32_t* perm,
+                                     uint32_t* work, cudaStream_t s);
+// FAST traversal with speculative leaf postponement (while-while); same results.
+void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
+                            uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s);
 // Coherence sort keys: direction octant (3 bits) + 27-bit Morton code of the
 // origin in the root box; vals = identity.
 void launch_ray_keys(const float4* rays, uint32_t n, const float* root, uint32_t* keys, uint32_t* vals,

@@ -23,19 +23,26 @@ struct Closest {
 };
 
 // Test the primitives of one leaf.  Returns true when an any-hit query is done.
+// FAST closest hit (REF = false) keeps the smallest t and, among primitives
+// hit at exactly that t, the smallest primitive id, so the result does not
+// depend on the order in which a walk meets the primitives.  REF keeps the
+// reference's first closest (strict <, castRay main.cpp:343-358).
 template <int KIND, bool ANY, bool REF>
 __device__ __forceinline__ bool test_leaf(const float4* __restrict__ prims,
                                           const uint32_t* __restrict__ order, uint32_t first,
                                           int count, const Ray& ray, Closest& c) {
   for (int k = 0; k < count; ++k) {
     uint32_t slot = first + (uint32_t)k;
+    // closest hit: accept t <= c.t once something is hit (ties go to the smaller id)
+    const float bound = (ANY || REF || c.prim == kMiss) ? c.t : nextafterf(c.t, __int_as_float(0x7F800000));
     if (KIND == kTriangles) {
       float4 p0 = __ldg(prims + 3 * (size_t)slot), p1 = __ldg(prims + 3 * (size_t)slot + 1),
              p2 = __ldg(prims + 3 * (size_t)slot + 2);
       float t, u, v;
-      if (tri_mt(p0, p1, p2, ray.o, ray.d, ray.tmin, ANY ? ray.tmax : c.t, t, u, v)) {
+      if (tri_mt(p0, p1, p2, ray.o, ray.d, ray.tmin, ANY ? ray.tmax : bound, t, u, v)) {
         if (ANY) return true;
-        c = {t, __float_as_uint(p0.w), u, v};
+        const uint32_t id = __float_as_uint(p0.w);
+        if (REF || t < c.t || id < c.prim) c = {t, id, u, v};
       }
     } else {
       float4 s = __ldg(prims + slot);
@@ -46,7 +53,10 @@ __device__ __forceinline__ bool test_leaf(const float4* __restrict__ prims,
           return true;
       } else {
         float t;
-        if (sphere_closest(s, ray.o, ray.d, ray.tmin, c.t, REF, t)) c = {t, __ldg(order + slot), 0.f, 0.f};
+        if (sphere_closest(s, ray.o, ray.d, ray.tmin, bound, REF, t)) {
+          const uint32_t id = __ldg(order + slot);
+          if (REF || t < c.t || id < c.prim) c = {t, id, 0.f, 0.f};
+        }
       }
     }
   }

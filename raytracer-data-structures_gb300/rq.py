@@ -19,6 +19,7 @@ ACC_NAMES = {"BVH": BVH, "KDTREE": KDTREE, "UNIFORM_GRID": UNIFORM_GRID, "LBVH":
 TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
 RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON = 0, 1
 NODE_WIDTH_2, NODE_WIDTH_4 = 0, 4
+SCHEDULING_THREAD_PER_RAY, SCHEDULING_LANE_REFILL, SCHEDULING_SPECULATIVE = 0, 1, 2
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1
 # SceneModel (settings.h:4)
 IGEA, ARMADILLO, BUNNY_MODEL, BUNNIES, TEST, GRASS, BUDDHA, CITY = range(8)
@@ -39,7 +40,7 @@ class Settings(C.Structure):
                 ("backgroundColor", C.c_float * 3), ("bias", C.c_float), ("aa_samples", C.c_uint32),
                 ("dataStructure", C.c_int32), ("sceneModel", C.c_int32), ("traversal", C.c_int32),
                 ("morton", C.c_int32), ("kd_max_depth", C.c_int32), ("ray_sort", C.c_int32),
-                ("node_width", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("node_width", C.c_int32), ("scheduling", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class AccelInfo(C.Structure):

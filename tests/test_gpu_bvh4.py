@@ -3,8 +3,9 @@ engine's collapse equals the oracle's collapse of the engine's own binary
 tree bit for bit, and FAST closest / any-hit queries through it equal the
 oracle's 4-wide walk bit for bit (hits, occlusion bits, node-visit and
 primitive-test counts).  The 4-wide walk visits children in a different order
-from the binary walk, so against the binary results t must agree exactly and
-ids may differ only where two primitives are hit at the same t."""
+from the binary walk; FAST closest hit keeps the smallest t and, on exact
+ties, the smallest primitive id, so the results equal the binary walk's bit
+for bit too."""
 import numpy as np
 import pytest
 
@@ -55,8 +56,7 @@ def test_bvh4_triangles_match_oracle(engine, oracle, rqm, acc_name):
     rays = scenes.incoherent_rays(lo, hi, 50_000, seed=42)
     h4 = _check_queries(engine, oracle, oracle.TRIANGLES, acc, b, nodes4, prims, rays)
     h2 = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, b, prims, rays)
-    assert np.array_equal(h4["t"], h2["t"])
-    assert (h4["prim"] == h2["prim"]).mean() > 0.999
+    assert np.array_equal(_u32(h4), _u32(h2))
 
 
 @pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])

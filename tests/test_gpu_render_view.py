@@ -72,8 +72,8 @@ def test_c1_icosphere_render_matches_oracle(engine, oracle, rqm, acc_name):
 @pytest.mark.parametrize("acc_name", ["LBVH", "BVH", "KDTREE"])
 def test_c1_crop_none_vs_structures(engine, oracle, rqm, acc_name):
     """C1's 64x48 crop rendered by brute force (NONE) and by each structure:
-    each equals its oracle; closest-hit distances agree between NONE and the
-    structure, so pixels differ at most where two triangles tie in t."""
+    each equals its oracle; BVH structures equal NONE pixel for pixel (the
+    same closest-hit rule), the KD walk at most at grazing hits."""
     v, f = scenes.c1_mesh()
     engine.configure(width=640, height=480, aa_samples=1)
     s = engine.scene_triangles(v, f)
@@ -85,7 +85,10 @@ def test_c1_crop_none_vs_structures(engine, oracle, rqm, acc_name):
     pa, ra, _ = _check(engine, oracle, rqm, acc, oracle.TRIANGLES, prims, ICO_VIEW, window, verts=v, idx=f)
     full, _, _ = engine.render(acc, rqm.make_view(**ICO_VIEW))
     assert np.array_equal(full[200:248, 300:364], pa)  # the window is a crop of the full render
-    assert (np.abs(pn.astype(int) - pa.astype(int)).max(axis=2) <= 1).mean() > 0.99
+    if acc_name == "KDTREE":  # the KD walk clips at split planes and keeps its own tie order
+        assert (np.abs(pn.astype(int) - pa.astype(int)).max(axis=2) <= 1).mean() > 0.99
+    else:  # BVH walks pick the same hit as brute force (smallest t, then smallest id)
+        assert np.array_equal(pn, pa)
 
 
 def test_c3_style_mirror_bounces_and_spp(engine, oracle, rqm):

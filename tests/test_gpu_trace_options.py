@@ -1,6 +1,8 @@
 """Engine options that change speed, never results: ray reordering for
 coherence (settings.ray_sort) must give bit-identical hits and occlusion bits,
 in the caller's order, for closest and any-hit queries."""
+import os
+
 import numpy as np
 import pytest
 
@@ -63,3 +65,44 @@ def test_streamed_host_queries_equal_device_queries(engine, rqm):
     engine.configure(ray_sort=rqm.RAY_SORT_OCTANT_MORTON)
     engine.trace_closest(acc, hr, hh)
     assert np.array_equal(hh.view(np.uint32).ravel(), want_h)
+
+
+@pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])
+@pytest.mark.parametrize("ray_sort", [0, 1])
+@pytest.mark.parametrize("sched", ["LANE_REFILL", "SPECULATIVE"])
+def test_scheduling_is_result_neutral(engine, oracle, rqm, acc_name, ray_sort, sched):
+    """Persistent warps that refill finished lanes, and the speculative
+    while-while walk (settings.scheduling), give bit-identical hits and
+    occlusion bits, with and without ray reordering, for triangles and
+    spheres, equal to the oracle's plain walk."""
+    mode = getattr(rqm, "SCHEDULING_" + sched)
+    v, f = scenes.heightfield(301, 150, seed=17)
+    s = engine.scene_triangles(v, f)
+    acc = engine.build(s, acc_name)
+    primary = scenes.pinhole_rays(320, 180, 2, eye=(0, -0.6, 1.1), target=(0, 0, 0), seed=18)
+    h0 = engine.trace_closest(acc, primary)
+    sec = scenes.cosine_rays(v, f, primary, h0, seed=19)
+    ref_c = engine.trace_closest(acc, sec)
+    ref_a = engine.trace_any(acc, sec)
+    engine.configure(scheduling=mode, ray_sort=ray_sort)
+    assert np.array_equal(engine.trace_closest(acc, sec).view(np.uint32), ref_c.view(np.uint32))
+    assert np.array_equal(engine.trace_any(acc, sec), ref_a)
+    for n in (1, 31, 33, 1000):  # partial warps and tiny batches
+        assert np.array_equal(engine.trace_closest(acc, sec[:n]).view(np.uint32), ref_c[:n].view(np.uint32))
+        want = rqm.unpack_bits(ref_a, len(sec))[:n]
+        assert np.array_equal(rqm.unpack_bits(engine.trace_any(acc, sec[:n]), n), want)
+    nodes, order, _, root, _ = engine.export_bvh2(acc)
+    prims, _, _ = oracle.tri_prims(v, f)
+    want = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, oracle.Bvh2(nodes, len(nodes), root, order),
+                             prims, sec)
+    assert np.array_equal(ref_c.view(np.uint32), want.view(np.uint32))
+    # spheres
+    sph = np.load(os.path.join(os.path.dirname(__file__), "golden", "synth_c.npz"))["spheres"]
+    engine.configure(scheduling=rqm.SCHEDULING_THREAD_PER_RAY)
+    ss = engine.build(engine.scene_spheres(sph), acc_name)
+    c = sph[:, :3]
+    rays = scenes.incoherent_rays(c.min(0) - 2, c.max(0) + 2, 70_000, seed=20)
+    base_c, base_a = engine.trace_closest(ss, rays), engine.trace_any(ss, rays)
+    engine.configure(scheduling=mode)
+    assert np.array_equal(engine.trace_closest(ss, rays).view(np.uint32), base_c.view(np.uint32))
+    assert np.array_equal(engine.trace_any(ss, rays), base_a)

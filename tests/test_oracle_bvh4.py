@@ -68,10 +68,9 @@ def test_bvh4_queries_equal_binary_and_brute_force(oracle, tree):
     h2 = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, b, prims, rays)
     h4 = oracle.trace_bvh4(oracle.TRIANGLES, oracle.CLOSEST, n4, b, prims, rays)
     hn = oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, prims, rays)
-    assert np.array_equal(h4["t"], h2["t"])
-    assert np.array_equal(h4["t"], hn["t"])
-    same = h4["prim"] == h2["prim"]
-    assert same.mean() > 0.999  # ids may differ only on exact-t ties (shared edges)
+    # smallest t, ties to the smallest id: independent of the walk
+    assert np.array_equal(h4.view(np.uint32), h2.view(np.uint32))
+    assert np.array_equal(h4.view(np.uint32), hn.view(np.uint32))
     a4 = oracle.trace_bvh4(oracle.TRIANGLES, oracle.ANY, n4, b, prims, rays)
     a2 = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.ANY, b, prims, rays)
     assert np.array_equal(a4, a2)

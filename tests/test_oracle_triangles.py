@@ -20,11 +20,8 @@ def test_lbvh_closest_equals_brute_force(oracle):
     rays = scenes.incoherent_rays(lo, hi, 4000, seed=3)
     hb = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, bvh, prims, rays)
     hn = oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, prims, rays)
-    assert np.array_equal(hb["prim"] == oracle.MISS, hn["prim"] == oracle.MISS)
-    same = hb["prim"] == hn["prim"]
-    # where ids differ the two triangles are hit at exactly the same t (a shared edge)
-    assert np.array_equal(hb["t"][~same], hn["t"][~same])
-    assert np.array_equal(hb["t"], hn["t"])
+    # FAST closest hit: smallest t, ties to the smallest id, whatever the walk
+    assert np.array_equal(hb.view(np.uint32), hn.view(np.uint32))
     ab = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.ANY, bvh, prims, rays)
     an = oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.ANY, prims, rays)
     assert np.array_equal(ab, an)
@@ -38,7 +35,7 @@ def test_median_and_kd_agree_with_brute_force(oracle):
     hn = oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, prims, rays)
     m = oracle.build_median(aabb, cen)
     hm = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, m, prims, rays)
-    assert np.array_equal(hm["t"], hn["t"])
+    assert np.array_equal(hm.view(np.uint32), hn.view(np.uint32))
     kd = oracle.build_kd(aabb)
     hk = oracle.trace_kd(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, kd, prims, rays)
     # KD traversal clips at split planes: allow the rare grazing difference
