@@ -210,20 +210,30 @@ def run_ours(args):
             return lambda: eng.trace_closest(a, d_sec, d_hits_s)
         return lambda: eng.trace_any(a, d_sh, d_bits)
 
+    # Every (ray order, scheduling) pair per ray class; scheduling variants
+    # walk binary nodes only.
+    sort_names = {rq.RAY_SORT_NONE: "none", rq.RAY_SORT_OCTANT_MORTON: "octant_morton",
+                  rq.RAY_SORT_ORIGIN_DIRECTION: "origin_direction", rq.RAY_SORT_DIRECTION_ORIGIN: "direction_origin",
+                  rq.RAY_SORT_OCTANT_MORTON12: "octant_morton12"}
+    sched_names = {rq.SCHEDULING_THREAD_PER_RAY: "thread_per_ray", rq.SCHEDULING_LANE_REFILL: "lane_refill",
+                   rq.SCHEDULING_SPECULATIVE: "speculative"}
     tuning = {}
     best = None
     for width in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4):
-        eng.configure(node_width=width, ray_sort=rq.RAY_SORT_NONE)
+        eng.configure(node_width=width, ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
         cand = eng.build(scene, rq.LBVH)
         choice, total = {}, timed(cand.rebuild)
+        scheds = list(sched_names) if width == rq.NODE_WIDTH_2 else [rq.SCHEDULING_THREAD_PER_RAY]
         for name in ("primary", "secondary", "shadow"):
             opts = {}
-            for opt in (rq.RAY_SORT_NONE, rq.RAY_SORT_OCTANT_MORTON):
-                eng.configure(ray_sort=opt)
-                opts[opt] = timed(class_call(cand, name))
+            for srt in sort_names:
+                for sch in scheds:
+                    eng.configure(ray_sort=srt, scheduling=sch)
+                    opts[(srt, sch)] = timed(class_call(cand, name))
             choice[name] = min(opts, key=opts.get)
             total += opts[choice[name]]
-        tuning[f"width{max(width, 2)}"] = {"est_step_ms": round(total, 4), "ray_sort": choice}
+        tuning[f"width{max(width, 2)}"] = {"est_step_ms": round(total, 4),
+                                           "choice": {k: [sort_names[v[0]], sched_names[v[1]]] for k, v in choice.items()}}
         if best is None or total < best[0]:
             if best is not None:
                 best[1].close()
@@ -232,7 +242,7 @@ def run_ours(args):
             cand.close()
     acc.close()
     _, acc, node_width, sort_choice = best
-    eng.configure(node_width=node_width)
+    eng.configure(node_width=node_width, ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
     node_bytes = 128 if node_width == rq.NODE_WIDTH_4 else NODE_BYTES
     log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}")
 
@@ -243,7 +253,7 @@ def run_ours(args):
         counts[name] = (int(cnt[0]), int(cnt[1]))
 
     def trace_class(name, marks=None):
-        eng.configure(ray_sort=sort_choice[name])
+        eng.configure(ray_sort=sort_choice[name][0], scheduling=sort_choice[name][1])
         class_call(acc, name)()
 
     def step(marks=None):
@@ -321,7 +331,7 @@ def run_ours(args):
                 other.rebuild()
                 m[1].record(stream)
                 for cls in ("primary", "secondary", "shadow"):
-                    eng.configure(ray_sort=sort_choice[cls])
+                    eng.configure(ray_sort=sort_choice[cls][0], scheduling=sort_choice[cls][1])
                     class_call(other, cls)()
                 m[2].record(stream)
                 torch.cuda.synchronize(dev)
@@ -364,7 +374,9 @@ def run_ours(args):
                        "secondary_rays": n_s, "shadow_rays": n_sh, "seed": SEED,
                        "l2": "flushed before every timed step (256 MB write); rays exceed L2",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                       "node_width": max(node_width, 2), "ray_sort": sort_choice, "tuning": tuning},
+                       "node_width": max(node_width, 2),
+                       "ray_sort": {k: sort_names[v[0]] for k, v in sort_choice.items()},
+                       "scheduling": {k: sched_names[v[1]] for k, v in sort_choice.items()}, "tuning": tuning},
             "lbvh_build_mtri_s": round(n_tri / (build_ms * 1e-3) / 1e6, 2),
             "closest_grays_s": round((n_p + n_s) / ((prim_ms + sec_ms) * 1e-3) / 1e9, 4),
             "any_grays_s": round(n_sh / (sh_ms * 1e-3) / 1e9, 4),
@@ -406,7 +418,8 @@ def run_render_legs(eng, stream, dev, args):
     out = {}
 
     def leg(verts, idx, structures, width, height, spp, view_kw, frames):
-        eng.configure(width=width, height=height, aa_samples=spp, ray_sort=rq.RAY_SORT_NONE)
+        eng.configure(width=width, height=height, aa_samples=spp, ray_sort=rq.RAY_SORT_NONE,
+                      scheduling=rq.SCHEDULING_THREAD_PER_RAY)
         dv = torch.from_numpy(verts).to(dev)
         di = torch.from_numpy(idx.view(np.int32)).to(dev)
         scene = eng.scene_triangles(dv, di)
@@ -502,7 +515,7 @@ def run_batch_leg(eng, stream, dev, args):
         meshes.append(scenes.wave_heightfield(nx, nx, seed=SEED + 100 + k))
     n_tri = int(sum(len(f) for _, f in meshes))
     saved = eng.settings
-    eng.configure(ray_sort=rq.RAY_SORT_NONE)
+    eng.configure(ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
     sc = [eng.scene_triangles(v, f) for v, f in meshes]
     offs = np.zeros(n_sc + 1, np.uint32)
     offs[1:] = np.cumsum(ray_n)
@@ -679,11 +692,11 @@ def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_
     def step():
         scene.update(hv, hi)
         acc.rebuild()
-        eng.configure(ray_sort=sort_choice["primary"])
+        eng.configure(ray_sort=sort_choice["primary"][0], scheduling=sort_choice["primary"][1])
         eng.trace_closest(acc, hp, out_p)
-        eng.configure(ray_sort=sort_choice["secondary"])
+        eng.configure(ray_sort=sort_choice["secondary"][0], scheduling=sort_choice["secondary"][1])
         eng.trace_closest(acc, hs, out_s)
-        eng.configure(ray_sort=sort_choice["shadow"])
+        eng.configure(ray_sort=sort_choice["shadow"][0], scheduling=sort_choice["shadow"][1])
         eng.trace_any(acc, hsh, out_b)
 
     for _ in range(max(1, args.warmup)):

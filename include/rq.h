@@ -107,7 +107,10 @@ typedef enum rq_node_width_t {
  * change; only the speed does. */
 typedef enum rq_ray_sort_t {
   RQ_RAY_SORT_NONE = 0,
-  RQ_RAY_SORT_OCTANT_MORTON = 1 /* direction octant, then 27-bit Morton code of the origin */
+  RQ_RAY_SORT_OCTANT_MORTON = 1,    /* direction octant, then 27-bit Morton code of the origin */
+  RQ_RAY_SORT_ORIGIN_DIRECTION = 2, /* octant, 15-bit origin Morton code, 12-bit direction (|dx|, |dy|) */
+  RQ_RAY_SORT_DIRECTION_ORIGIN = 3, /* octant, 12-bit direction, 15-bit origin Morton code */
+  RQ_RAY_SORT_OCTANT_MORTON12 = 4   /* octant, 12-bit origin Morton code: a 15-bit key, half the sort passes */
 } rq_ray_sort_t;
 
 /* How rays meet boxes and primitives. */

@@ -175,7 +175,7 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
                                 bool any, const QueryTarget& q, BuildScratch& sc, uint32_t* err, cudaStream_t st) {
   const bool bvh2 = type == RQ_LBVH || type == RQ_BVH;
   const bool fast = bvh2 && cfg.traversal == RQ_TRAVERSAL_FAST;
-  const bool sorted = fast && cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON && q.n >= kRaySortMin;
+  const bool sorted = fast && cfg.ray_sort != RQ_RAY_SORT_NONE && q.n >= kRaySortMin;
   const bool refill = fast && cfg.scheduling == RQ_SCHEDULING_LANE_REFILL && a.node_width != 4;
   const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && a.node_width != 4;
   if (!sorted && !refill && !spec) {
@@ -191,8 +191,9 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
     RQ_B(sc.vals.ensure((size_t)q.n * 4), "ray sort scratch");
     uint32_t* keys = sc.keys.as<uint32_t>();
     uint32_t* p = sc.vals.as<uint32_t>();
-    launch_ray_keys(q.rays, q.n, a.root.as<const float>(), keys, p, st);
-    BuildResult r = sort_pairs(keys, p, q.n, 4, true, sc, err, st);
+    launch_ray_keys(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, keys, p, st);
+    const int passes = cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON12 ? 2 : 4;
+    BuildResult r = sort_pairs(keys, p, q.n, passes, true, sc, err, st);
     if (!r.ok()) return r;
     perm = p;
   }

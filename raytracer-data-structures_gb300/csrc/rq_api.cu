@@ -186,6 +186,8 @@ rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.morton must be SCENE_BOUNDS or REFERENCE");
   if (s->node_width != RQ_NODE_WIDTH_2 && s->node_width != 2 && s->node_width != RQ_NODE_WIDTH_4)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.node_width must be 2 or 4");
+  if (s->ray_sort < RQ_RAY_SORT_NONE || s->ray_sort > RQ_RAY_SORT_OCTANT_MORTON12)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.ray_sort out of range");
   if (s->scheduling < RQ_SCHEDULING_THREAD_PER_RAY || s->scheduling > RQ_SCHEDULING_SPECULATIVE)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.scheduling must be THREAD_PER_RAY, LANE_REFILL or SPECULATIVE");
   ctx->settings = *s;

@@ -124,9 +124,8 @@ cudaError_t launch_trace_bvh2_refill(int kind, bool any, const Bvh2View& v, cons
 // FAST traversal with speculative leaf postponement (while-while); same results.
 void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
                             uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s);
-// Coherence sort keys: direction octant (3 bits) + 27-bit Morton code of the
-// origin in the root box; vals = identity.
-void launch_ray_keys(const float4* rays, uint32_t n, const float* root, uint32_t* keys, uint32_t* vals,
+// Coherence sort keys (mode: rq_ray_sort_t other than NONE, 30 bits); vals = identity.
+void launch_ray_keys(const float4* rays, uint32_t n, const float* root, int mode, uint32_t* keys, uint32_t* vals,
                      cudaStream_t s);
 // FAST traversal that also sums internal-node visits and primitive tests
 // into counters[0..1] (the inputs of the traversal byte model).

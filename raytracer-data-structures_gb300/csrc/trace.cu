@@ -544,39 +544,61 @@ void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4*
   }
 }
 
-// Sort key of a ray for coherent tracing: the direction octant in the top
-// three bits, then a 27-bit Morton code of the origin inside the scene box.
+// Sort keys of rays for coherent tracing (30 bits, direction octant on top):
+//   RQ_RAY_SORT_OCTANT_MORTON    octant | 27-bit Morton code of the origin
+//   RQ_RAY_SORT_ORIGIN_DIRECTION octant | 15-bit origin Morton | 12-bit direction
+//   RQ_RAY_SORT_DIRECTION_ORIGIN octant | 12-bit direction | 15-bit origin Morton
+//   RQ_RAY_SORT_OCTANT_MORTON12  octant | 12-bit origin Morton (15 bits: a 2-pass sort)
+// The origin is quantised in the root box; the direction by |dx|, |dy| of the
+// unit direction, 6 bits each (|dz| follows within the octant).
+__device__ __forceinline__ uint32_t spread_bits(uint32_t v) {  // 10 bits -> every third bit
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
 __global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ rays, uint32_t n,
-                                                  const float* __restrict__ root, uint32_t* __restrict__ keys,
-                                                  uint32_t* __restrict__ vals) {
+                                                  const float* __restrict__ root, int mode,
+                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
   const float o[3] = {a.x, a.y, a.z};
+  const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4 : 5;
+  const float cells = (float)(1u << obits);
   uint32_t q[3];
   for (int k = 0; k < 3; ++k) {
     float lo = root[k], ext = root[3 + k] - root[k];
     float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
-    u = fminf(fmaxf(u * 512.f, 0.f), 511.f);
+    u = fminf(fmaxf(u * cells, 0.f), cells - 1.f);
     q[k] = (uint32_t)u;
   }
-  auto spread = [](uint32_t v) {  // 9 bits -> every third bit
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
-  };
+  const uint32_t morton = (spread_bits(q[0]) << 2) | (spread_bits(q[1]) << 1) | spread_bits(q[2]);
   const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
-  keys[i] = (oct << 27) | (spread(q[0]) << 2) | (spread(q[1]) << 1) | spread(q[2]);
+  uint32_t key;
+  if (mode == RQ_RAY_SORT_OCTANT_MORTON) {
+    key = (oct << 27) | morton;
+  } else if (mode == RQ_RAY_SORT_OCTANT_MORTON12) {
+    key = (oct << 12) | morton;
+  } else {
+    const float len = sqrtf(b.x * b.x + b.y * b.y + b.z * b.z);
+    const float inv = len > 0.f ? 1.0f / len : 0.f;
+    const uint32_t dx = (uint32_t)fminf(fabsf(b.x) * inv * 64.f, 63.f);
+    const uint32_t dy = (uint32_t)fminf(fabsf(b.y) * inv * 64.f, 63.f);
+    const uint32_t dir = (dx << 6) | dy;
+    key = mode == RQ_RAY_SORT_ORIGIN_DIRECTION ? (oct << 27) | (morton << 12) | dir : (oct << 27) | (dir << 15) | morton;
+  }
+  keys[i] = key;
   vals[i] = i;
 }
 
-void launch_ray_keys(const float4* rays, uint32_t n, const float* root, uint32_t* keys, uint32_t* vals,
+void launch_ray_keys(const float4* rays, uint32_t n, const float* root, int mode, uint32_t* keys, uint32_t* vals,
                      cudaStream_t s) {
   if (n == 0) return;
   count_launch();
-  k_ray_keys<<<(n + 255) / 256, 256, 0, s>>>(rays, n, root, keys, vals);
+  k_ray_keys<<<(n + 255) / 256, 256, 0, s>>>(rays, n, root, mode, keys, vals);
 }
 
 void launch_trace_brute(int kind, int traversal, bool any, const float4* prims, uint32_t n_prims,

@@ -17,7 +17,8 @@ LIB_PATH = os.path.join(HERE, "librq.so")
 BVH, KDTREE, UNIFORM_GRID, LBVH, NONE = 0, 1, 2, 3, 4
 ACC_NAMES = {"BVH": BVH, "KDTREE": KDTREE, "UNIFORM_GRID": UNIFORM_GRID, "LBVH": LBVH, "NONE": NONE}
 TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
-RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON = 0, 1
+RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON, RAY_SORT_ORIGIN_DIRECTION, RAY_SORT_DIRECTION_ORIGIN, RAY_SORT_OCTANT_MORTON12 = \
+    0, 1, 2, 3, 4
 NODE_WIDTH_2, NODE_WIDTH_4 = 0, 4
 SCHEDULING_THREAD_PER_RAY, SCHEDULING_LANE_REFILL, SCHEDULING_SPECULATIVE = 0, 1, 2
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1

@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])
-def test_ray_sort_is_result_neutral(engine, oracle, rqm, acc_name):
+@pytest.mark.parametrize("key", ["OCTANT_MORTON", "ORIGIN_DIRECTION", "DIRECTION_ORIGIN", "OCTANT_MORTON12"])
+def test_ray_sort_is_result_neutral(engine, oracle, rqm, acc_name, key):
     v, f = scenes.heightfield(301, 150, seed=12)
     s = engine.scene_triangles(v, f)
     acc = engine.build(s, acc_name)
@@ -22,7 +23,7 @@ def test_ray_sort_is_result_neutral(engine, oracle, rqm, acc_name):
     assert len(sec) >= 65536  # above the reordering threshold
     ref_c = engine.trace_closest(acc, sec)
     ref_a = engine.trace_any(acc, sec)
-    engine.configure(ray_sort=rqm.RAY_SORT_OCTANT_MORTON)
+    engine.configure(ray_sort=getattr(rqm, "RAY_SORT_" + key))
     got_c = engine.trace_closest(acc, sec)
     got_a = engine.trace_any(acc, sec)
     assert np.array_equal(got_c.view(np.uint32), ref_c.view(np.uint32))
