@@ -153,9 +153,11 @@ void launch_validate(const float* verts, uint32_t nv, const uint32_t* idx, uint3
 // Working arrays of rq_render (grow-only, per context).
 struct RenderScratch {
   DevBuf rays, shadow, hits, cw, pend, bits, out, counters;
+  DevBuf list_a, list_b, list_s, list_n;  // live-sample lists of the compacting render
   void release() {
     rays.release(); shadow.release(); hits.release(); cw.release(); pend.release(); bits.release();
     out.release(); counters.release();
+    list_a.release(); list_b.release(); list_s.release(); list_n.release();
   }
 };
 // Wavefront render of `view` into device buffers pixels (3 B per pixel) and

@@ -118,17 +118,19 @@ __device__ __forceinline__ V3 surface_normal(const SceneView& sc, uint32_t prim,
 
 // One depth of shading for sample r: background on a miss, else Lambert +
 // ambient with a shadow ray and (below the last depth) a mirror ray into
-// rays[r].  Sets emit_shadow / emit_mirror for the ray counters.
-template <int KIND>
+// rays[r].  Sets emit_shadow / emit_mirror for the ray counters.  LISTS: the
+// caller drives later queries from lists of the emitting samples, so
+// samples that emit nothing get no dead-ray markers and no zero light term.
+template <int KIND, bool LISTS = false>
 __device__ __forceinline__ void shade_sample(const ViewDev& v, const SceneView& sc, uint64_t r, bool last,
                                              float4* __restrict__ rays, const float4* __restrict__ hits,
                                              float4* __restrict__ shadow, float4* __restrict__ cw,
                                              float4* __restrict__ pend, bool& emit_shadow, bool& emit_mirror) {
   emit_shadow = emit_mirror = false;
   const float4 r0 = rays[2 * r], r1 = rays[2 * r + 1];
-  pend[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!LISTS) pend[r] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!(r0.w <= r1.w)) {  // finished sample
-    store_dead(shadow, r);
+    if (!LISTS) store_dead(shadow, r);
     return;
   }
   const float4 h = __ldg(hits + r);
@@ -139,8 +141,10 @@ __device__ __forceinline__ void shade_sample(const ViewDev& v, const SceneView& 
     c.y = c.y + w * v.bg.y;
     c.z = c.z + w * v.bg.z;
     cw[r] = make_float4(c.x, c.y, c.z, 0.f);
-    store_dead(rays, r);
-    store_dead(shadow, r);
+    if (!LISTS) {
+      store_dead(rays, r);
+      store_dead(shadow, r);
+    }
     return;
   }
   const V3 o = {r0.x, r0.y, r0.z}, d = {r1.x, r1.y, r1.z};
@@ -161,7 +165,7 @@ __device__ __forceinline__ void shade_sample(const ViewDev& v, const SceneView& 
     pend[r] = make_float4(fa.x * ndl, fa.y * ndl, fa.z * ndl, 0.f);
     store_ray(shadow, r, po, 0.f, ld, dist);
     emit_shadow = true;
-  } else {
+  } else if (!LISTS) {
     store_dead(shadow, r);
   }
   const float wn = w * v.mirror;
@@ -169,7 +173,7 @@ __device__ __forceinline__ void shade_sample(const ViewDev& v, const SceneView& 
     const V3 rd = v3sub(d, v3mul(n, 2.0f * v3dot(d, n)));
     store_ray(rays, r, po, 0.f, rd, __int_as_float(0x7F800000));
     emit_mirror = true;
-  } else {
+  } else if (!LISTS) {
     store_dead(rays, r);
   }
   cw[r] = make_float4(c.x, c.y, c.z, emit_mirror ? wn : 0.f);
