@@ -11,7 +11,8 @@ and L2 is additionally flushed (256 MB write) before every timed step.
 
   value  = rays traced per second over the whole step (build included), Grays/s
   e2e    = the same through the C ABI with pinned host buffers: mesh upload,
-           rebuild, ray upload and hit/bit download inside the timed region
+           rebuild, and one rq_trace_queries call for the three ray classes
+           (ray upload and hit/bit download inside the timed region)
   roofline: the step's dominant kernel against measured HBM bandwidth, with
            algorithmic bytes from the engine's traversal counters
   cpu_baseline: the CPU oracle (the reference's algorithms: median BVH build,
@@ -690,14 +691,12 @@ def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_
     tb, out_b = pinned(np.zeros((len(shadow) + 31) // 32, np.uint32)); keep.append(tb)
 
     def step():
+        # one call for the three queries: copies and traversals overlap across them
         scene.update(hv, hi)
         acc.rebuild()
-        eng.configure(ray_sort=sort_choice["primary"][0], scheduling=sort_choice["primary"][1])
-        eng.trace_closest(acc, hp, out_p)
-        eng.configure(ray_sort=sort_choice["secondary"][0], scheduling=sort_choice["secondary"][1])
-        eng.trace_closest(acc, hs, out_s)
-        eng.configure(ray_sort=sort_choice["shadow"][0], scheduling=sort_choice["shadow"][1])
-        eng.trace_any(acc, hsh, out_b)
+        eng.trace_queries(acc, [(hp, False, out_p, sort_choice["primary"][0], sort_choice["primary"][1]),
+                                (hs, False, out_s, sort_choice["secondary"][0], sort_choice["secondary"][1]),
+                                (hsh, True, out_b, sort_choice["shadow"][0], sort_choice["shadow"][1])])
 
     for _ in range(max(1, args.warmup)):
         step()

@@ -275,6 +275,24 @@ rq_status_t rq_trace_closest(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* ray
 rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n,
                          uint32_t* occluded_bits, uint32_t flags);
 
+/* One host-buffer query of rq_trace_queries. */
+typedef struct rq_query_t {
+  const rq_ray_t* rays;   /* host */
+  uint32_t n;
+  int32_t any;            /* 0: closest hits (rq_hit_t per ray) into out; 1: occlusion bits */
+  void* out;              /* host */
+  int32_t ray_sort;       /* rq_ray_sort_t for this query; -1: the context's setting */
+  int32_t scheduling;     /* rq_scheduling_t for this query; -1: the context's setting */
+} rq_query_t;
+/* Several host-buffer queries on one structure in one call, with copies
+ * and traversals overlapped across queries: the first query streams chunk
+ * by chunk, later ones upload whole while earlier ones trace (each then
+ * traced as one batch) and download while later ones trace.  Results equal
+ * rq_trace_closest / rq_trace_any per query; returns when every result is in
+ * host memory.  Device memory: each query after the first keeps a buffer of
+ * its rays and results (grow-only, per context). */
+rq_status_t rq_trace_queries(rq_ctx_t ctx, rq_accel_t accel, const rq_query_t* queries, uint32_t n_queries);
+
 /* The FAST closest/any query of rq_trace_closest / rq_trace_any that also
  * sums, over all rays, the internal nodes visited (counters[0]) and the
  * primitives tested (counters[1]): the inputs of the traversal byte model.

@@ -573,7 +573,7 @@ rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t a, int32_t* nodes, int32
 // the context's stream, download on pipe.down, with kPipeSlots device slots
 // in rotation (a slot is re-filled only after its previous download).
 static rq_status_t trace_streamed_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n,
-                                          void* out, bool any) {
+                                          void* out, bool any, const rq_settings_t& cfg, bool join_downloads = true) {
   HostPipe& p = ctx->pipe;
   RQ_TRY_CUDA(ctx, p.init());
   const size_t out_chunk = any ? kPipeChunk / 8 : (size_t)kPipeChunk * 16;
@@ -617,7 +617,7 @@ static rq_status_t trace_streamed_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_r
     q.n = m;
     q.hits = any ? nullptr : p.out[sl].as<float4>();
     q.occ = any ? p.out[sl].as<uint32_t>() : nullptr;
-    BuildResult br = launch_query_sorted(a->type, sv, a->buf, ctx->settings, any, q, lane_scratch, ctx->d_err, lane);
+    BuildResult br = launch_query_sorted(a->type, sv, a->buf, cfg, any, q, lane_scratch, ctx->d_err, lane);
     if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
     if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
     RQ_TRY_CUDA(ctx, cudaEventRecord(p.traced[sl], lane));
@@ -632,15 +632,21 @@ static rq_status_t trace_streamed_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_r
     }
     RQ_TRY_CUDA(ctx, cudaEventRecord(p.downloaded[sl], p.down));
   }
-  // the context's stream is ordered after the last download
-  RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, p.down));
-  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, p.start, 0));
+  if (join_downloads) {
+    // the context's stream is ordered after the last download
+    RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, p.down));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, p.start, 0));
+  } else {
+    // only after the other lane's traversals (later work reuses the lanes)
+    RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, p.lane2));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, p.start, 0));
+  }
   return RQ_SUCCESS;
 }
 
 static rq_status_t trace_streamed(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, void* out,
                                   bool any) {
-  rq_status_t st = trace_streamed_enqueue(ctx, a, rays, n, out, any);
+  rq_status_t st = trace_streamed_enqueue(ctx, a, rays, n, out, any, ctx->settings);
   if (st != RQ_SUCCESS) {
     // nothing may still read or write the caller's buffers after an error
     if (ctx->pipe.up) cudaStreamSynchronize(ctx->pipe.up);
@@ -692,6 +698,92 @@ rq_status_t rq_trace_closest(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, u
 rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n,
                          uint32_t* occluded_bits, uint32_t flags) {
   return trace(ctx, a, rays, n, occluded_bits, flags, true);
+}
+
+// Several host-buffer queries in one call: the first streams chunk by chunk,
+// the others upload whole (on the upload stream, behind the first's chunks)
+// while earlier queries trace, trace as full batches on the context's stream
+// and download while later ones trace.
+static rq_status_t trace_queries_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_query_t* qs, uint32_t nq) {
+  HostPipe& p = ctx->pipe;
+  RQ_TRY_CUDA(ctx, p.init());
+  const SceneView sv = scene_view(a->scene);
+  auto cfg_of = [&](const rq_query_t& q) {
+    rq_settings_t c = ctx->settings;
+    if (q.ray_sort >= 0) c.ray_sort = q.ray_sort;
+    if (q.scheduling >= 0) c.scheduling = q.scheduling;
+    return c;
+  };
+  uint32_t first = 0;
+  if (qs[0].n >= 2 * kPipeChunk) {
+    RQ_TRY(trace_streamed_enqueue(ctx, a, qs[0].rays, qs[0].n, qs[0].out, qs[0].any != 0, cfg_of(qs[0]), false));
+    first = 1;
+  } else {
+    RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, p.start, 0));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.down, p.start, 0));
+  }
+  if (p.q_rays.size() < nq) {
+    p.q_rays.resize(nq);
+    p.q_out.resize(nq);
+  }
+  while (p.q_events.size() < 2 * (size_t)nq) {
+    cudaEvent_t e;
+    RQ_TRY_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    p.q_events.push_back(e);
+  }
+  for (uint32_t k = first; k < nq; ++k) {
+    const rq_query_t& q = qs[k];
+    if (q.n == 0) continue;
+    const size_t out_bytes = q.any ? (size_t)((q.n + 31) / 32) * 4 : (size_t)q.n * 16;
+    RQ_TRY_CUDA(ctx, p.q_rays[k].ensure((size_t)q.n * 32));
+    RQ_TRY_CUDA(ctx, p.q_out[k].ensure(out_bytes));
+  }
+  for (uint32_t k = first; k < nq; ++k) {
+    const rq_query_t& q = qs[k];
+    if (q.n == 0) continue;
+    cudaEvent_t up = p.q_events[2 * k], done = p.q_events[2 * k + 1];
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(p.q_rays[k].p, q.rays, (size_t)q.n * 32, cudaMemcpyHostToDevice, p.up));
+    RQ_TRY_CUDA(ctx, cudaEventRecord(up, p.up));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, up, 0));
+    QueryTarget t;
+    t.rays = p.q_rays[k].as<const float4>();
+    t.n = q.n;
+    t.hits = q.any ? nullptr : p.q_out[k].as<float4>();
+    t.occ = q.any ? p.q_out[k].as<uint32_t>() : nullptr;
+    BuildResult br = launch_query_sorted(a->type, sv, a->buf, cfg_of(q), q.any != 0, t, ctx->scratch, ctx->d_err,
+                                         ctx->stream);
+    if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+    if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
+    RQ_TRY_CUDA(ctx, cudaEventRecord(done, ctx->stream));
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.down, done, 0));
+    const size_t out_bytes = q.any ? (size_t)((q.n + 31) / 32) * 4 : (size_t)q.n * 16;
+    RQ_TRY_CUDA(ctx, cudaMemcpyAsync(q.out, p.q_out[k].p, out_bytes, cudaMemcpyDeviceToHost, p.down));
+  }
+  RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, p.down));
+  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, p.start, 0));
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_trace_queries(rq_ctx_t ctx, rq_accel_t a, const rq_query_t* queries, uint32_t n_queries) {
+  RQ_TRY(bind(ctx));
+  if (!a || (n_queries && !queries)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel or query list");
+  if (n_queries == 0) return RQ_SUCCESS;
+  for (uint32_t k = 0; k < n_queries; ++k) {
+    const rq_query_t& q = queries[k];
+    if (q.n && (!q.rays || !q.out)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
+    if (q.ray_sort > RQ_RAY_SORT_OCTANT_MORTON12 || q.scheduling > RQ_SCHEDULING_SPECULATIVE)
+      return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "query ray_sort or scheduling out of range");
+  }
+  rq_status_t st = trace_queries_enqueue(ctx, a, queries, n_queries);
+  if (st != RQ_SUCCESS) {
+    if (ctx->pipe.up) cudaStreamSynchronize(ctx->pipe.up);
+    if (ctx->pipe.lane2) cudaStreamSynchronize(ctx->pipe.lane2);
+    if (ctx->pipe.down) cudaStreamSynchronize(ctx->pipe.down);
+    cudaStreamSynchronize(ctx->stream);
+    return st;
+  }
+  return collect_device_errors(ctx);
 }
 
 // Device tables of a many-structure query: one Bvh2View per structure (the

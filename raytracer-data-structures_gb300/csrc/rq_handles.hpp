@@ -24,6 +24,8 @@ struct HostPipe {
   BuildScratch scratch2;
   cudaEvent_t start = nullptr, uploaded[kPipeSlots] = {}, traced[kPipeSlots] = {}, downloaded[kPipeSlots] = {};
   DevBuf rays[kPipeSlots], out[kPipeSlots];
+  std::vector<DevBuf> q_rays, q_out;   // whole-query buffers of rq_trace_queries
+  std::vector<cudaEvent_t> q_events;   // uploaded / traced per query
   bool ready = false;
   cudaError_t init() {
     if (ready) return cudaSuccess;
@@ -53,6 +55,12 @@ struct HostPipe {
     if (down) cudaStreamDestroy(down);
     if (lane2) cudaStreamDestroy(lane2);
     scratch2.release();
+    for (auto& b : q_rays) b.release();
+    for (auto& b : q_out) b.release();
+    for (cudaEvent_t e : q_events) cudaEventDestroy(e);
+    q_rays.clear();
+    q_out.clear();
+    q_events.clear();
     start = nullptr;
     up = down = lane2 = nullptr;
     ready = false;

@@ -69,6 +69,11 @@ def make_view(eye, target, up=(0, 0, 1), fov_deg=40.0, light=(0, 0, 10), albedo=
     return v
 
 
+class Query(C.Structure):
+    _fields_ = [("rays", C.c_void_p), ("n", C.c_uint32), ("any", C.c_int32), ("out", C.c_void_p),
+                ("ray_sort", C.c_int32), ("scheduling", C.c_int32)]
+
+
 class PlanInfo(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("stack_entries", C.c_uint32), ("graph_kernels", C.c_uint32),
                 ("n_rays", C.c_uint32), ("rebuilds", C.c_uint32), ("shape_ms", C.c_float * 4)]
@@ -227,6 +232,7 @@ def load(build_if_missing=True):
         "rq_build_batched": (i32, [vp, vp, u32, i32, vp]),
         "rq_accel_rebuild_batched": (i32, [vp, vp, u32]),
         "rq_trace_batched": (i32, [vp, vp, u32, vp, vp, i32, vp, u32]),
+        "rq_trace_queries": (i32, [vp, vp, vp, u32]),
         "rq_plan_create": (i32, [vp, vp, u32, i32, vp, vp, i32, vp, vp]),
         "rq_plan_launch": (i32, [vp]),
         "rq_plan_get_info": (i32, [vp, vp]),
@@ -454,6 +460,22 @@ class Engine:
         pb, _ = _ptr(bits)
         self._check(load().rq_trace_any(self.ctx, accel.handle, pr, n, pb, fl))
         return bits
+
+    def trace_queries(self, accel, queries):
+        """rq_trace_queries over host arrays: queries = [(rays, any_hit, out or None,
+        ray_sort or -1, scheduling or -1), ...]; returns the outputs."""
+        qs = (Query * len(queries))()
+        outs, keep = [], []
+        for k, (rays, any_hit, out, srt, sch) in enumerate(queries):
+            rays = np.ascontiguousarray(rays, RAY_DTYPE)
+            n = len(rays)
+            if out is None:
+                out = np.zeros((n + 31) // 32, np.uint32) if any_hit else np.zeros(n, HIT_DTYPE)
+            keep.append(rays)
+            outs.append(out)
+            qs[k] = Query(rays.ctypes.data, n, int(any_hit), out.ctypes.data, srt, sch)
+        self._check(load().rq_trace_queries(self.ctx, accel.handle, qs, len(queries)))
+        return outs
 
     def trace_counters(self, accel, rays, any_hit=False):
         """FAST query plus (internal nodes visited, primitives tested) summed over the rays."""

@@ -107,3 +107,26 @@ def test_scheduling_is_result_neutral(engine, oracle, rqm, acc_name, ray_sort, s
     engine.configure(scheduling=mode)
     assert np.array_equal(engine.trace_closest(ss, rays).view(np.uint32), base_c.view(np.uint32))
     assert np.array_equal(engine.trace_any(ss, rays), base_a)
+
+
+def test_trace_queries_equal_single_queries(engine, rqm):
+    """rq_trace_queries (copies and traversals overlapped across queries, the
+    first streamed in chunks) returns exactly the results of one call per
+    query, with per-query ray order and scheduling."""
+    v, f = scenes.heightfield(301, 150, seed=21)
+    acc = engine.build(engine.scene_triangles(v, f), "LBVH")
+    primary = scenes.pinhole_rays(1250, 1000, 4, eye=(0, -0.6, 1.1), target=(0, 0, 0), seed=22)  # 5M: streamed
+    h0 = engine.trace_closest(acc, primary)
+    sec = scenes.cosine_rays(v, f, primary[:700_000], h0[:700_000], seed=23)
+    sh = scenes.shadow_rays(v, f, primary[:300_000], h0[:300_000], (1.5, -1.0, 3.0))
+    want = [h0, engine.trace_closest(acc, sec), engine.trace_any(acc, sh), engine.trace_closest(acc, primary[:10])]
+    got = engine.trace_queries(acc, [(primary, False, None, -1, -1),
+                                     (sec, False, None, rqm.RAY_SORT_OCTANT_MORTON12, -1),
+                                     (sh, True, None, -1, rqm.SCHEDULING_SPECULATIVE),
+                                     (primary[:10], False, None, -1, -1)])
+    for g, w in zip(got, want):
+        assert np.array_equal(np.ascontiguousarray(g).view(np.uint32), np.ascontiguousarray(w).view(np.uint32))
+    # a short first query takes the whole-buffer path too
+    got = engine.trace_queries(acc, [(sec, False, None, -1, -1), (sh, True, None, -1, -1)])
+    assert np.array_equal(got[0].view(np.uint32), want[1].view(np.uint32))
+    assert np.array_equal(got[1], want[2])
