@@ -54,6 +54,24 @@ def dist_env():
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def replica_step_ms(mean_ms, ws, device):
+    """Step time of an N-replica job: the max over ranks of each rank's mean
+    step time (the job ends with its slowest replica).  One process per GPU;
+    no collective touches the data path, only this timing reduction."""
+    if ws <= 1:
+        return float(mean_ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(mean_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_value(ws, rays_per_rank, step_ms):
+    """Whole-job rays per second (Grays/s) when every rank traces its own full workload."""
+    return ws * rays_per_rank / (step_ms * 1e-3) / 1e9
+
+
 def make_inputs(small=False):
     import scenes
     verts, idx = scenes.heightfield(1001, 500, amplitude=0.3, octaves=5, seed=SEED % 1000)
@@ -289,12 +307,8 @@ def run_ours(args):
             phase[k] = [marks[i].elapsed_time(marks[i + 1]) for i in range(4)]
     eng.synchronize()
     launches = rq.kernel_launch_count() - launches0
-    mean_ms = float(step_ms.mean())
-    if ws > 1:
-        t = torch.tensor([mean_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        mean_ms = float(t.item())
-    value = ws * total_rays / (mean_ms * 1e-3) / 1e9
+    mean_ms = replica_step_ms(float(step_ms.mean()), ws, dev)
+    value = weak_value(ws, total_rays, mean_ms)
     ph = phase.mean(0)
     build_ms, prim_ms, sec_ms, sh_ms = ph
 
