@@ -236,34 +236,39 @@ def run_ours(args):
                   rq.RAY_SORT_OCTANT_MORTON12: "octant_morton12"}
     sched_names = {rq.SCHEDULING_THREAD_PER_RAY: "thread_per_ray", rq.SCHEDULING_LANE_REFILL: "lane_refill",
                    rq.SCHEDULING_SPECULATIVE: "speculative"}
+    morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
     tuning = {}
     best = None
     for width in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4):
-        eng.configure(node_width=width, ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
-        cand = eng.build(scene, rq.LBVH)
-        choice, total = {}, timed(cand.rebuild)
-        scheds = list(sched_names) if width == rq.NODE_WIDTH_2 else [rq.SCHEDULING_THREAD_PER_RAY]
-        for name in ("primary", "secondary", "shadow"):
-            opts = {}
-            for srt in sort_names:
-                for sch in scheds:
-                    eng.configure(ray_sort=srt, scheduling=sch)
-                    opts[(srt, sch)] = timed(class_call(cand, name))
-            choice[name] = min(opts, key=opts.get)
-            total += opts[choice[name]]
-        tuning[f"width{max(width, 2)}"] = {"est_step_ms": round(total, 4),
-                                           "choice": {k: [sort_names[v[0]], sched_names[v[1]]] for k, v in choice.items()}}
-        if best is None or total < best[0]:
-            if best is not None:
-                best[1].close()
-            best = (total, cand, width, choice)
-        else:
-            cand.close()
+        for morton in morton_names:
+            eng.configure(node_width=width, morton=morton, ray_sort=rq.RAY_SORT_NONE,
+                          scheduling=rq.SCHEDULING_THREAD_PER_RAY)
+            cand = eng.build(scene, rq.LBVH)
+            choice, total = {}, timed(cand.rebuild)
+            scheds = list(sched_names) if width == rq.NODE_WIDTH_2 else [rq.SCHEDULING_THREAD_PER_RAY]
+            for name in ("primary", "secondary", "shadow"):
+                opts = {}
+                for srt in sort_names:
+                    for sch in scheds:
+                        eng.configure(ray_sort=srt, scheduling=sch)
+                        opts[(srt, sch)] = timed(class_call(cand, name))
+                choice[name] = min(opts, key=opts.get)
+                total += opts[choice[name]]
+            tuning[f"width{max(width, 2)}_{morton_names[morton]}"] = {
+                "est_step_ms": round(total, 4),
+                "choice": {k: [sort_names[v[0]], sched_names[v[1]]] for k, v in choice.items()}}
+            if best is None or total < best[0]:
+                if best is not None:
+                    best[1].close()
+                best = (total, cand, (width, morton), choice)
+            else:
+                cand.close()
     acc.close()
-    _, acc, node_width, sort_choice = best
-    eng.configure(node_width=node_width, ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
+    _, acc, (node_width, morton_mode), sort_choice = best
+    eng.configure(node_width=node_width, morton=morton_mode, ray_sort=rq.RAY_SORT_NONE,
+                  scheduling=rq.SCHEDULING_THREAD_PER_RAY)
     node_bytes = 128 if node_width == rq.NODE_WIDTH_4 else NODE_BYTES
-    log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}")
+    log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}, morton {morton_names[morton_mode]}")
 
     # Traversal work of each query on these exact rays (the byte model's inputs).
     counts = {}
@@ -389,7 +394,7 @@ def run_ours(args):
                        "secondary_rays": n_s, "shadow_rays": n_sh, "seed": SEED,
                        "l2": "flushed before every timed step (256 MB write); rays exceed L2",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                       "node_width": max(node_width, 2),
+                       "node_width": max(node_width, 2), "morton": morton_names[morton_mode],
                        "ray_sort": {k: sort_names[v[0]] for k, v in sort_choice.items()},
                        "scheduling": {k: sched_names[v[1]] for k, v in sort_choice.items()}, "tuning": tuning},
             "lbvh_build_mtri_s": round(n_tri / (build_ms * 1e-3) / 1e6, 2),

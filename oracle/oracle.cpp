@@ -710,6 +710,18 @@ void orc_morton_centroids(const float* cen, uint32_t n, const float* lo, const f
   }
 }
 
+// The engine's cube normalisation: every axis divided by the largest extent
+// E = max(hi - lo) of the scene box.
+void orc_morton_centroids_cube(const float* cen, uint32_t n, const float* lo, const float* hi,
+                               uint32_t* codes) {
+  const float e = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+  for (uint32_t i = 0; i < n; ++i) {
+    float q[3];
+    for (int k = 0; k < 3; ++k) q[k] = e > 0 ? (cen[3 * (size_t)i + k] - lo[k]) / e : 0.0f;
+    codes[i] = orc_morton3d(q[0], q[1], q[2]);
+  }
+}
+
 void orc_tri_prims(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt,
                    float* prims9, float* aabb6, float* centroid3) {
   (void)nv;

@@ -48,6 +48,9 @@ uint32_t orc_morton3d(float x, float y, float z);
 void orc_morton_spheres_ref(const float* sph, uint32_t n, uint32_t* codes);
 void orc_morton_centroids(const float* centroids, uint32_t n, const float* lo, const float* hi,
                           uint32_t* codes);
+/* The engine's cube normalisation (one scale, the largest extent). */
+void orc_morton_centroids_cube(const float* centroids, uint32_t n, const float* lo, const float* hi,
+                               uint32_t* codes);
 
 /* ---- primitive preparation (engine definitions) ---- */
 void orc_tri_prims(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt,

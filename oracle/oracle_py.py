@@ -76,12 +76,14 @@ def morton_spheres_ref(sph):
     return out
 
 
-def morton_centroids(cen, lo, hi):
+def morton_centroids(cen, lo, hi, cube=False):
+    """cube=True: the engine's RQ_MORTON_SCENE_CUBE (one scale, the largest extent)."""
     cen = _c(cen, np.float32)
     lo = _c(lo, np.float32)
     hi = _c(hi, np.float32)
     out = np.zeros(len(cen), np.uint32)
-    lib().orc_morton_centroids(_p(cen), C.c_uint32(len(cen)), _p(lo), _p(hi), _p(out))
+    f = lib().orc_morton_centroids_cube if cube else lib().orc_morton_centroids
+    f(_p(cen), C.c_uint32(len(cen)), _p(lo), _p(hi), _p(out))
     return out
 
 

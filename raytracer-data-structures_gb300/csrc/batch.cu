@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_morton(const BatchDesc* __re
   if (kind == kTriangles) {
     float lo[3], ext[3];
     bounds_from(lohi + 6 * s, lo, ext);
+    if (mode == RQ_MORTON_SCENE_CUBE) cube_extent(ext);
     code = code_scene(tri_centroid(desc[s].verts, desc[s].idx, i), lo, ext);
   } else {
     const float4 c = __ldg(desc[s].sph + i);
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_morton(const BatchDesc* __re
     } else {
       float lo[3], ext[3];
       bounds_from(lohi + 6 * s, lo, ext);
+      if (mode == RQ_MORTON_SCENE_CUBE) cube_extent(ext);
       code = code_scene({c.x, c.y, c.z}, lo, ext);
     }
   }

@@ -76,9 +76,9 @@ BuildResult morton_codes(const SceneView& s, int mode, uint32_t* codes, uint32_t
   if (s.kind == kTriangles) {
     launch_init_bounds(lohi, st);
     launch_point_bounds(s.verts, s.nv, 3, lohi, st);
-    launch_morton_tris(s.verts, s.idx, s.n, lohi, codes, vals, hist, st);
+    launch_morton_tris(s.verts, s.idx, s.n, mode, lohi, codes, vals, hist, st);
   } else {
-    if (mode == RQ_MORTON_SCENE_BOUNDS) {
+    if (mode != RQ_MORTON_REFERENCE) {
       launch_init_bounds(lohi, st);
       launch_point_bounds(reinterpret_cast<const float*>(s.sph), s.n, 4, lohi, st);
     }

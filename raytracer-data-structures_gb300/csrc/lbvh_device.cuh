@@ -17,6 +17,14 @@ __device__ __forceinline__ void bounds_from(const int32_t* lohi, float* lo, floa
   }
 }
 
+// Cube normalisation (RQ_MORTON_SCENE_CUBE): every axis scaled by the
+// largest extent of the scene box, so the curve splits space evenly on flat
+// or elongated scenes.
+__device__ __forceinline__ void cube_extent(float* ext) {
+  const float e = fmaxf(fmaxf(ext[0], ext[1]), ext[2]);
+  ext[0] = ext[1] = ext[2] = e;
+}
+
 // (c - lo) / ext per axis, 0 where the extent is 0.
 __device__ __forceinline__ uint32_t code_scene(F3 c, const float* lo, const float* ext) {
   float q0 = ext[0] > 0.f ? __fdiv_rn(__fsub_rn(c.x, lo[0]), ext[0]) : 0.f;

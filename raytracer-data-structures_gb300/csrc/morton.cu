@@ -67,14 +67,17 @@ __device__ __forceinline__ void hist_flush(SharedHist& sh, uint32_t* hist) {
 // Centroid ((v0 + v1) + v2) / 3 per axis, then scene-box normalisation.
 __global__ void __launch_bounds__(kThreads) k_morton_tris(const float* __restrict__ verts,
                                                           const uint32_t* __restrict__ idx,
-                                                          uint32_t nt, const int32_t* __restrict__ lohi,
+                                                          uint32_t nt, int mode, const int32_t* __restrict__ lohi,
                                                           uint32_t* __restrict__ keys,
                                                           uint32_t* __restrict__ vals,
                                                           uint32_t* __restrict__ hist) {
   __shared__ SharedHist sh;
   __shared__ float s_lo[3], s_ext[3];
   if (hist) hist_zero(sh);
-  if (threadIdx.x == 0) bounds_from(lohi, s_lo, s_ext);
+  if (threadIdx.x == 0) {
+    bounds_from(lohi, s_lo, s_ext);
+    if (mode == RQ_MORTON_SCENE_CUBE) cube_extent(s_ext);
+  }
   __syncthreads();
   float lo[3] = {s_lo[0], s_lo[1], s_lo[2]}, ext[3] = {s_ext[0], s_ext[1], s_ext[2]};
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
@@ -97,7 +100,10 @@ __global__ void __launch_bounds__(kThreads) k_morton_spheres(const float4* __res
   __shared__ SharedHist sh;
   __shared__ float s_lo[3], s_ext[3];
   if (hist) hist_zero(sh);
-  if (threadIdx.x == 0 && mode == RQ_MORTON_SCENE_BOUNDS) bounds_from(lohi, s_lo, s_ext);
+  if (threadIdx.x == 0 && mode != RQ_MORTON_REFERENCE) {
+    bounds_from(lohi, s_lo, s_ext);
+    if (mode == RQ_MORTON_SCENE_CUBE) cube_extent(s_ext);
+  }
   __syncthreads();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 s = __ldg(sph + i);
@@ -138,11 +144,11 @@ void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t*
   k_point_bounds<<<grid_for(n) > 1024 ? 1024 : grid_for(n), kThreads, 0, s>>>(pts, n, stride, lohi);
 }
 
-void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, const int32_t* lohi,
+void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, int mode, const int32_t* lohi,
                         uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s) {
   if (nt == 0) return;
   count_launch();
-  k_morton_tris<<<grid_for(nt), kThreads, 0, s>>>(verts, idx, nt, lohi, keys, vals, hist);
+  k_morton_tris<<<grid_for(nt), kThreads, 0, s>>>(verts, idx, nt, mode, lohi, keys, vals, hist);
 }
 
 void launch_morton_spheres(const float4* sph, uint32_t n, int mode, const int32_t* lohi,

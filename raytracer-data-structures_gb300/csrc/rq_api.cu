@@ -182,8 +182,8 @@ rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
   if (!ctx || !s) return RQ_ERROR_INVALID_ARGUMENT;
   if (s->traversal != RQ_TRAVERSAL_FAST && s->traversal != RQ_TRAVERSAL_REFERENCE)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.traversal must be FAST or REFERENCE");
-  if (s->morton != RQ_MORTON_SCENE_BOUNDS && s->morton != RQ_MORTON_REFERENCE)
-    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.morton must be SCENE_BOUNDS or REFERENCE");
+  if (s->morton != RQ_MORTON_SCENE_BOUNDS && s->morton != RQ_MORTON_REFERENCE && s->morton != RQ_MORTON_SCENE_CUBE)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.morton must be SCENE_BOUNDS, REFERENCE or SCENE_CUBE");
   if (s->node_width != RQ_NODE_WIDTH_2 && s->node_width != 2 && s->node_width != RQ_NODE_WIDTH_4)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.node_width must be 2 or 4");
   if (s->ray_sort < RQ_RAY_SORT_NONE || s->ray_sort > RQ_RAY_SORT_OCTANT_MORTON12)

@@ -73,9 +73,9 @@ void launch_onesweep64(uint64_t* keys, uint32_t* vals, uint32_t n, int passes, u
 void launch_init_bounds(int32_t* lohi, cudaStream_t s);
 void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t* lohi,
                          cudaStream_t s);
-// mode: RQ_MORTON_SCENE_BOUNDS (uses lohi) or RQ_MORTON_REFERENCE.  hist may
-// be null; otherwise the 4-pass digit histogram is accumulated into it.
-void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, const int32_t* lohi,
+// mode: rq_morton_t (SCENE_BOUNDS and SCENE_CUBE use lohi).  hist may be
+// null; otherwise the 4-pass digit histogram is accumulated into it.
+void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, int mode, const int32_t* lohi,
                         uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s);
 void launch_morton_spheres(const float4* sph, uint32_t n, int mode, const int32_t* lohi,
                            uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s);

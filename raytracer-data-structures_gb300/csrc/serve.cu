@@ -412,7 +412,12 @@ rq_status_t rq_server_create(const rq_server_config_t* cfg, rq_server_t* out) {
   if (s->cfg.max_batch_rays == 0) s->cfg.max_batch_rays = 1u << 25;
   if (s->cfg.max_batch_requests == 0) s->cfg.max_batch_requests = 256;
   if (s->cfg.max_batch_rays >= (1u << 31)) return RQ_ERROR_INVALID_ARGUMENT;
-  rq_status_t st = rq_create(nullptr, s->cfg.device, &s->ctx);
+  // the server's own context: cube Morton normalisation (tighter LBVHs on
+  // flat scenes; results do not depend on the tree)
+  rq_settings_t settings;
+  rq_settings_default(&settings);
+  settings.morton = RQ_MORTON_SCENE_CUBE;
+  rq_status_t st = rq_create(&settings, s->cfg.device, &s->ctx);
   if (st != RQ_SUCCESS) return st;
   rq_server* raw = s.get();
   s->worker = std::thread([raw] { raw->run(); });

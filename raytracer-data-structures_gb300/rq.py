@@ -21,7 +21,7 @@ RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON, RAY_SORT_ORIGIN_DIRECTION, RAY_SORT_DIREC
     0, 1, 2, 3, 4
 NODE_WIDTH_2, NODE_WIDTH_4 = 0, 4
 SCHEDULING_THREAD_PER_RAY, SCHEDULING_LANE_REFILL, SCHEDULING_SPECULATIVE = 0, 1, 2
-MORTON_SCENE_BOUNDS, MORTON_REFERENCE = 0, 1
+MORTON_SCENE_BOUNDS, MORTON_REFERENCE, MORTON_SCENE_CUBE = 0, 1, 2
 # SceneModel (settings.h:4)
 IGEA, ARMADILLO, BUNNY_MODEL, BUNNIES, TEST, GRASS, BUDDHA, CITY = range(8)
 DEVICE_POINTERS = 0x1

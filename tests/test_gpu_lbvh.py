@@ -272,3 +272,40 @@ def test_rejected_host_update_keeps_the_scene(engine, oracle, rqm):
     assert e.value.status == 1
     acc.rebuild()
     assert np.array_equal(engine.trace_closest(acc, rays).view(np.uint32), before.view(np.uint32))
+
+
+def test_cube_morton_normalisation(engine, oracle, rqm):
+    """RQ_MORTON_SCENE_CUBE: codes and LBVH equal the oracle's cube
+    normalisation bit for bit, batched builds equal single builds, and FAST
+    query results equal the per-axis tree's (the closest-hit rule)."""
+    v, f = scenes.heightfield(301, 150, seed=31)
+    s = engine.scene_triangles(v, f)
+    flat = engine.build(s, "LBVH")
+    engine.configure(morton=rqm.MORTON_SCENE_CUBE)
+    prims, aabb, cen = oracle.tri_prims(v, f)
+    lo, hi = oracle.bounds3(v)
+    want_codes = oracle.morton_centroids(cen, lo, hi, cube=True)
+    assert np.array_equal(engine.morton_codes(s), want_codes)
+    assert not np.array_equal(want_codes, oracle.morton_centroids(cen, lo, hi))
+    acc = engine.build(s, "LBVH")
+    nodes, order, codes, root, _ = engine.export_bvh2(acc)
+    ref = oracle.build_lbvh(want_codes, aabb)
+    assert np.array_equal(codes, ref.sorted_codes) and np.array_equal(order, ref.order)
+    assert np.array_equal(nodes.view(np.uint32), ref.nodes.view(np.uint32))
+    rays = scenes.pinhole_rays(200, 120, 2, eye=(0, -0.6, 1.1), target=(0, 0, 0), seed=32)
+    hits = engine.trace_closest(acc, rays)
+    assert np.array_equal(hits.view(np.uint32), engine.trace_closest(flat, rays).view(np.uint32))
+    assert np.array_equal(engine.trace_any(acc, rays), engine.trace_any(flat, rays))
+    want = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, ref, prims, rays)
+    assert np.array_equal(hits.view(np.uint32), want.view(np.uint32))
+    # batched, with a sphere batch too
+    batch = engine.build_batched([s], "LBVH")
+    for g, w in zip(engine.export_bvh2(batch[0])[:3], (nodes, order, codes)):
+        assert np.array_equal(np.asarray(g).view(np.uint32), np.asarray(w).view(np.uint32))
+    sph = golden("synth_c")["spheres"]
+    ss = engine.scene_spheres(sph)
+    sa = engine.build(ss, "LBVH")
+    slo, shi = oracle.bounds3(sph[:, :3])
+    assert np.array_equal(engine.morton_codes(ss), oracle.morton_centroids(sph[:, :3], slo, shi, cube=True))
+    sb = engine.build_batched([ss], "LBVH")[0]
+    assert np.array_equal(engine.export_bvh2(sb)[0].view(np.uint32), engine.export_bvh2(sa)[0].view(np.uint32))
