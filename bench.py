@@ -239,8 +239,11 @@ def run_ours(args):
     morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
     tuning = {}
     best = None
-    for width in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4):
-        for morton in morton_names:
+    candidates = [(w, m) for w in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4) for m in morton_names]
+    if args.no_tune:  # the live tuner's choice on a GB300, for profiling the same kernel mix
+        candidates = [(rq.NODE_WIDTH_2, rq.MORTON_SCENE_CUBE)]
+    for width, morton in candidates:
+        if True:
             eng.configure(node_width=width, morton=morton, ray_sort=rq.RAY_SORT_NONE,
                           scheduling=rq.SCHEDULING_THREAD_PER_RAY)
             cand = eng.build(scene, rq.LBVH)
@@ -248,10 +251,14 @@ def run_ours(args):
             scheds = list(sched_names) if width == rq.NODE_WIDTH_2 else [rq.SCHEDULING_THREAD_PER_RAY]
             for name in ("primary", "secondary", "shadow"):
                 opts = {}
-                for srt in sort_names:
-                    for sch in scheds:
-                        eng.configure(ray_sort=srt, scheduling=sch)
-                        opts[(srt, sch)] = timed(class_call(cand, name))
+                if args.no_tune:
+                    fixed = rq.RAY_SORT_OCTANT_MORTON12 if name == "secondary" else rq.RAY_SORT_NONE
+                    pairs = [(fixed, rq.SCHEDULING_THREAD_PER_RAY)]
+                else:
+                    pairs = [(srt, sch) for srt in sort_names for sch in scheds]
+                for srt, sch in pairs:
+                    eng.configure(ray_sort=srt, scheduling=sch)
+                    opts[(srt, sch)] = timed(class_call(cand, name))
                 choice[name] = min(opts, key=opts.get)
                 total += opts[choice[name]]
             tuning[f"width{max(width, 2)}_{morton_names[morton]}"] = {
@@ -855,6 +862,7 @@ def run_case(args):
     torch.cuda.set_stream(stream)
     eng = rq.Engine(0)
     eng.set_stream(stream.cuda_stream)
+    eng.configure(morton=rq.MORTON_SCENE_CUBE)  # the tuner's build choice (see --no-tune)
     if args.case == "batched":
         rng = np.random.default_rng(SEED + 40)
         n_sc = 32 if args.small else 256
@@ -911,6 +919,9 @@ def main():
     ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "batched"],
                     help="profiling driver: run one query class, print no bench line")
     ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner and use its GB300 choice (binary nodes, cube Morton codes, "
+                         "15-bit ray order for secondary rays): profiling the measured kernel mix")
     args = ap.parse_args()
     if args.case:
         run_case(args)
