@@ -281,6 +281,18 @@ rq_status_t rq_trace_closest(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* ray
 rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n,
                          uint32_t* occluded_bits, uint32_t flags);
 
+/* boxIntersect (accelerators.h:668-690) for a batch of rays: for each ray,
+ * the ids of the primitives of every leaf the reference's walk reaches
+ * (division slab test without clipping, left subtree before right), the list
+ * castRay's candidate loop (main.cpp:335-358) then tests.  counts: n entries;
+ * *total: their sum; ids (may be NULL: counts only): the lists concatenated
+ * in ray order, ids_cap entries available (RQ_ERROR_INVALID_ARGUMENT when
+ * fewer than *total, or when *total is 2^32 or more: split the rays; counts
+ * and total are still written).  BVH
+ * structures (RQ_BVH, RQ_LBVH); RQ_DEVICE_POINTERS for device buffers. */
+rq_status_t rq_trace_candidates(rq_ctx_t ctx, rq_accel_t accel, const rq_ray_t* rays, uint32_t n, uint32_t* counts,
+                                uint32_t* ids, uint64_t ids_cap, uint64_t* total, uint32_t flags);
+
 /* One host-buffer query of rq_trace_queries. */
 typedef struct rq_query_t {
   const rq_ray_t* rays;   /* host */

@@ -992,6 +992,47 @@ int orc_build_kd(const float* aabb6, uint32_t n, int32_t max_depth, int32_t* nod
   return 0;
 }
 
+// boxIntersect (accelerators.h:668-690): every primitive id of every leaf
+// that the reference's pre-order walk with the division slab test reaches.
+uint64_t orc_candidates_bvh2(const float* nodes, uint32_t n_internal, const float* rb, uint32_t n_prims,
+                             const uint32_t* order, const orc_ray_t* rays, uint32_t nrays, uint32_t* counts,
+                             uint32_t* ids, uint64_t cap) {
+  uint64_t total = 0;
+  for (uint32_t r = 0; r < nrays; ++r) {
+    const V3 o = v3(rays[r].org), d = v3(rays[r].dir);
+    uint32_t c = 0;
+    float a, b;
+    if (box_ref(o, d, rb, rb + 3, a, b)) {
+      std::vector<Entry> stack;
+      Entry cur = n_internal == 0 ? Entry{~0, (int32_t)n_prims} : Entry{0, 0};
+      for (;;) {
+        if (cur.node >= 0) {
+          const float* n = nodes + 16 * (size_t)cur.node;
+          int32_t ch[4];
+          std::memcpy(ch, n + 12, sizeof(ch));
+          float lo[3] = {n[0], n[2], n[8]}, hi[3] = {n[1], n[3], n[9]};
+          float lo2[3] = {n[4], n[6], n[10]}, hi2[3] = {n[5], n[7], n[11]};
+          const bool hl = box_ref(o, d, lo, hi, a, b);
+          const bool hr = box_ref(o, d, lo2, hi2, a, b);
+          if (hr) stack.push_back({ch[1], ch[3]});
+          if (hl) { cur = {ch[0], ch[2]}; continue; }
+        } else {
+          for (int32_t k = 0; k < cur.count; ++k) {
+            if (ids && total + c < cap) ids[total + c] = order[(uint32_t)(~cur.node) + (uint32_t)k];
+            ++c;
+          }
+        }
+        if (stack.empty()) break;
+        cur = stack.back();
+        stack.pop_back();
+      }
+    }
+    counts[r] = c;
+    total += c;
+  }
+  return total;
+}
+
 int orc_trace_bvh2(int kind, int mode, int query, const float* nodes16, uint32_t n_internal,
                    const float* root_bounds6, uint32_t n_prims, const uint32_t* order,
                    const float* prims, const orc_ray_t* rays, uint32_t nrays, orc_hit_t* hits,

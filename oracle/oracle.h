@@ -92,6 +92,12 @@ int orc_trace_bvh2(int kind, int mode, int query, const float* nodes16, uint32_t
                    const float* root_bounds6, uint32_t n_prims, const uint32_t* order,
                    const float* prims, const orc_ray_t* rays, uint32_t nrays, orc_hit_t* hits,
                    uint8_t* occluded, uint64_t* counters, int nthreads);
+/* boxIntersect's candidate lists (accelerators.h:668-690): counts[r] per ray,
+ * the ids concatenated in ray order into ids (up to cap entries; may be
+ * NULL).  Returns the total. */
+uint64_t orc_candidates_bvh2(const float* nodes16, uint32_t n_internal, const float* root_bounds6, uint32_t n_prims,
+                             const uint32_t* order, const orc_ray_t* rays, uint32_t nrays, uint32_t* counts,
+                             uint32_t* ids, uint64_t cap);
 int orc_trace_kd(int kind, int mode, int query, const int32_t* nodes3, uint32_t n_nodes,
                  const int32_t* prim_idx, const float* root_bounds6, const float* prims,
                  const orc_ray_t* rays, uint32_t nrays, orc_hit_t* hits, uint8_t* occluded,

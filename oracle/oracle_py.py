@@ -243,6 +243,21 @@ def trace_bvh2(kind, mode, query, bvh, prims, rays, nthreads=0, counters=None):
     return hits if query == CLOSEST else occ
 
 
+def candidates_bvh2(bvh, rays):
+    """boxIntersect's candidate lists: (counts per ray, ids concatenated)."""
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    counts = np.zeros(len(rays), np.uint32)
+    L = lib()
+    L.orc_candidates_bvh2.restype = C.c_uint64
+    args = [_p(_c(bvh.nodes, np.float32) if bvh.n_internal else np.zeros((1, 16), np.float32)),
+            C.c_uint32(bvh.n_internal), _p(_c(bvh.root_bounds, np.float32)), C.c_uint32(len(bvh.order)),
+            _p(_c(bvh.order, np.uint32)), _p(rays), C.c_uint32(len(rays)), _p(counts)]
+    total = L.orc_candidates_bvh2(*args, None, C.c_uint64(0))
+    ids = np.zeros(max(int(total), 1), np.uint32)
+    L.orc_candidates_bvh2(*args, _p(ids), C.c_uint64(total))
+    return counts, ids[:int(total)]
+
+
 def collapse_bvh4(bvh):
     """Collapsed 4-wide BVH of a Bvh2: (nodes as (n4, 32) float32, n4)."""
     n = max(bvh.n_internal, 1)

@@ -700,6 +700,57 @@ rq_status_t rq_trace_any(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint3
   return trace(ctx, a, rays, n, occluded_bits, flags, true);
 }
 
+rq_status_t rq_trace_candidates(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint32_t n, uint32_t* counts,
+                                uint32_t* ids, uint64_t ids_cap, uint64_t* total, uint32_t flags) {
+  RQ_TRY(bind(ctx));
+  if (!a || !counts || !total) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel, counts or total");
+  if (a->type != RQ_BVH && a->type != RQ_LBVH)
+    return fail(ctx, RQ_ERROR_UNSUPPORTED, "candidate lists exist for BVH structures (RQ_BVH, RQ_LBVH)");
+  *total = 0;
+  if (n == 0) return RQ_SUCCESS;
+  if (!rays) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null rays");
+  const bool dev = flags & RQ_DEVICE_POINTERS;
+  const float4* d_rays = nullptr;
+  RQ_TRY(to_device(ctx, ctx->stage_in, reinterpret_cast<const float4*>(rays), (size_t)n * 32, flags, &d_rays));
+  BuildScratch& sc = ctx->scratch;
+  uint32_t* d_counts = counts;
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, sc.m4.ensure((size_t)n * 4));
+    d_counts = sc.m4.as<uint32_t>();
+  }
+  RQ_TRY_CUDA(ctx, sc.m5.ensure((size_t)n * 4));
+  RQ_TRY_CUDA(ctx, sc.m6.ensure(scan_tmp_words(n) * 4 + 16));
+  const AccelBuffers& b = a->buf;
+  const Bvh2View v{b.nodes.as<const float4>(), b.prims.as<const float4>(), b.order.as<const uint32_t>(),
+                   b.root.as<const float>(), b.n_nodes, b.n_slots};
+  // m6 words: [0] 32-bit scan total, [2..3] 64-bit count total, [4..] scan temporaries
+  uint32_t* d_total = sc.m6.as<uint32_t>();
+  unsigned long long* d_total64 = reinterpret_cast<unsigned long long*>(d_total + 2);
+  RQ_TRY_CUDA(ctx, cudaMemsetAsync(d_total64, 0, 8, ctx->stream));
+  launch_candidates(v, d_rays, n, d_counts, nullptr, nullptr, d_total64, ctx->d_err, ctx->stream);
+  RQ_TRY(check_launch(ctx, "candidate count launch"));
+  uint32_t* offs = sc.m5.as<uint32_t>();
+  launch_scan_excl(d_counts, offs, n, d_total + 4, d_total, ctx->stream);
+  unsigned long long t = 0;
+  RQ_TRY_CUDA(ctx, cudaMemcpyAsync(&t, d_total64, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dev) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  RQ_TRY(collect_device_errors(ctx));
+  *total = t;
+  if (!ids) return RQ_SUCCESS;
+  if (t > 0xFFFFFFFFull)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "more than 2^32-1 candidates in one call: split the rays");
+  if (ids_cap < t) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "ids buffer smaller than the total count");
+  uint32_t* d_ids = ids;
+  if (!dev) {
+    RQ_TRY_CUDA(ctx, ctx->stage_out.ensure((size_t)t * 4 + 4));
+    d_ids = ctx->stage_out.as<uint32_t>();
+  }
+  launch_candidates(v, d_rays, n, d_counts, offs, d_ids, nullptr, ctx->d_err, ctx->stream);
+  RQ_TRY(check_launch(ctx, "candidate fill launch"));
+  if (!dev && t) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(ids, d_ids, (size_t)t * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  return collect_device_errors(ctx);
+}
+
 // Several host-buffer queries in one call: the first streams chunk by chunk,
 // the others upload whole (on the upload stream, behind the first's chunks)
 // while earlier queries trace, trace as full batches on the context's stream

@@ -116,6 +116,12 @@ struct Bvh2View {
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
                        uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
                        const uint32_t* perm = nullptr);
+// boxIntersect's candidate lists: ids == null counts per ray into counts;
+// otherwise writes each ray's ids at offs[r] (and checks the counts).
+// Count pass (ids null): counts[r] and *total (64-bit sum, zeroed by the
+// caller).  Fill pass: ids at offs[r], at most counts[r] per ray.
+void launch_candidates(const Bvh2View& v, const float4* rays, uint32_t n, uint32_t* counts, const uint32_t* offs,
+                       uint32_t* ids, unsigned long long* total, uint32_t* err, cudaStream_t s);
 // FAST traversal by persistent warps that refill finished lanes (one work
 // word, zeroed by the launcher); same results as launch_trace_bvh2.
 cudaError_t launch_trace_bvh2_refill(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n,

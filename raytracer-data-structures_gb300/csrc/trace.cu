@@ -390,6 +390,64 @@ __global__ void __launch_bounds__(kThreads) k_trace_ref(Bvh2View bvh, const floa
   }
 }
 
+// boxIntersect (accelerators.h:668-690): the ids of the primitives in every
+// leaf the reference's walk reaches (division slab test, no clipping,
+// pre-order: left subtree before right), per ray.  FILL = false counts them;
+// FILL = true writes them at offs[r] (the exclusive prefix of the counts).
+template <bool FILL>
+__global__ void __launch_bounds__(kThreads) k_candidates(Bvh2View bvh, const float4* __restrict__ rays, uint32_t n,
+                                                         uint32_t* __restrict__ counts,
+                                                         const uint32_t* __restrict__ offs,
+                                                         uint32_t* __restrict__ ids,
+                                                         unsigned long long* __restrict__ total, uint32_t* err) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const Ray ray = load_ray(rays, r);
+  uint32_t cnt_out = 0;
+  const uint32_t base = FILL ? __ldg(offs + r) : 0u;
+  const uint32_t cap = FILL ? __ldg(counts + r) : 0u;
+  float a0, a1;
+  const float* rb = bvh.root;
+  if (box_ref(ray.o, ray.d, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], a0, a1)) {
+    int2 stack[kStackSize];
+    int sp = 0;
+    int cur = bvh.n_internal ? 0 : -1;
+    int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
+    const uint32_t max_steps = 2u * (bvh.n_internal + bvh.n_slots) + 8u;
+    uint32_t steps = 0;
+    for (;;) {
+      if (++steps > max_steps) { atomicOr(err, kErrCorrupt); break; }
+      if (cur >= 0) {
+        const float4* nd = bvh.nodes + 4 * (size_t)cur;
+        float4 a = __ldg(nd), b = __ldg(nd + 1), z = __ldg(nd + 2);
+        int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+        bool hl = box_ref(ray.o, ray.d, a.x, a.y, a.z, a.w, z.x, z.y, a0, a1);
+        bool hr = box_ref(ray.o, ray.d, b.x, b.y, b.z, b.w, z.z, z.w, a0, a1);
+        if (hr) {
+          if (sp >= kStackSize) { atomicOr(err, kErrStackOverflow); break; }
+          stack[sp++] = make_int2(l.y, l.w);
+        }
+        if (hl) { cur = l.x; cnt = l.z; continue; }
+      } else {
+        for (int k = 0; k < cnt; ++k) {
+          if (FILL && cnt_out < cap) ids[(size_t)base + cnt_out] = __ldg(bvh.order + (uint32_t)(~cur) + (uint32_t)k);
+          ++cnt_out;
+        }
+      }
+      if (sp == 0) break;
+      int2 e = stack[--sp];
+      cur = e.x;
+      cnt = e.y;
+    }
+  }
+  if (!FILL) {
+    counts[r] = cnt_out;
+    atomicAdd(total, (unsigned long long)cnt_out);  // 64-bit: the 32-bit offsets must not wrap
+  } else if (cnt_out != cap) {
+    atomicOr(err, kErrCorrupt);  // the fill walk repeats the count walk
+  }
+}
+
 // NONE: every primitive in id order (main.cpp:373-387), staged through
 // shared memory in tiles shared by the block's rays.
 constexpr int kBruteTile = 256;
@@ -542,6 +600,15 @@ void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4*
     if (any) k_trace_spec<kSpheres, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
     else k_trace_spec<kSpheres, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
   }
+}
+
+void launch_candidates(const Bvh2View& v, const float4* rays, uint32_t n, uint32_t* counts, const uint32_t* offs,
+                       uint32_t* ids, unsigned long long* total, uint32_t* err, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  const uint32_t g = (n + kThreads - 1) / kThreads;
+  if (ids) k_candidates<true><<<g, kThreads, 0, s>>>(v, rays, n, counts, offs, ids, nullptr, err);
+  else k_candidates<false><<<g, kThreads, 0, s>>>(v, rays, n, counts, nullptr, nullptr, total, err);
 }
 
 // Sort keys of rays for coherent tracing (30 bits, direction octant on top):

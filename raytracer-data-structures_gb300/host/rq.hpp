@@ -6,6 +6,7 @@
 //   AccType  BVH, KDTREE, UNIFORM_GRID, LBVH, NONE      accelerators.h:21
 //   build(ctx, scene, settings.dataStructure) the switch in main() (main.cpp:791-843)
 //   constructBVHNew / constructLBVHTree / constructKDTreeNew   accelerators.h:246,570,951
+//   boxIntersect -> boxIntersect / candidates (candidate ids, accelerators.h:668)
 //   boxIntersect + castRay's closest selection -> closestHits  (accelerators.h:668, main.cpp:330-358)
 //   kdtreeIntersect -> anyHits                                  (accelerators.h:997)
 //   render + write_into_file -> render / write_ppm              (main.cpp:541-566, 516-528)
@@ -125,9 +126,32 @@ class Accel {
     for (size_t r = 0; r < rays.size(); ++r) out[r] = (bits[r >> 5] >> (r & 31)) & 1u;
     return out;
   }
+  // boxIntersect (accelerators.h:668-690) for a batch: each ray's candidate
+  // primitive ids in the reference's pre-order, concatenated; counts per ray.
+  void candidates(const std::vector<rq_ray_t>& rays, std::vector<uint32_t>& counts,
+                  std::vector<uint32_t>& ids) const {
+    counts.assign(rays.size(), 0);
+    ids.clear();
+    if (rays.empty()) return;
+    uint64_t total = 0;
+    check(rq_trace_candidates(c_->get(), h_, rays.data(), (uint32_t)rays.size(), counts.data(), nullptr, 0, &total, 0),
+          c_->get());
+    ids.resize(total);
+    check(rq_trace_candidates(c_->get(), h_, rays.data(), (uint32_t)rays.size(), counts.data(), ids.data(), total,
+                              &total, 0),
+          c_->get());
+  }
+  // The reference's signature: append the candidate ids of one ray to boxes
+  // (one device round trip per call: batch with candidates() where possible).
+  void boxIntersect(const float pos[3], const float dir[3], std::vector<int>& boxes) const {
+    std::vector<rq_ray_t> r(1, rq_ray_t{{pos[0], pos[1], pos[2]}, 0.f, {dir[0], dir[1], dir[2]}, __builtin_inff()});
+    std::vector<uint32_t> counts, ids;
+    candidates(r, counts, ids);
+    for (uint32_t id : ids) boxes.push_back((int)id);
+  }
   // One ray at a time, the shape of the reference's per-ray calls (each is a
   // device round trip: batch with closestHits/anyHits where possible).
-  bool boxIntersect(const float pos[3], const float dir[3], rq_hit_t& hit) const {
+  bool closestHit(const float pos[3], const float dir[3], rq_hit_t& hit) const {
     rq_ray_t r = {{pos[0], pos[1], pos[2]}, 0.f, {dir[0], dir[1], dir[2]}, __builtin_inff()};
     check(rq_trace_closest(c_->get(), h_, &r, 1, &hit, 0), c_->get());
     return hit.prim != RQ_MISS;

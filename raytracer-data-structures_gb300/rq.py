@@ -233,6 +233,7 @@ def load(build_if_missing=True):
         "rq_accel_rebuild_batched": (i32, [vp, vp, u32]),
         "rq_trace_batched": (i32, [vp, vp, u32, vp, vp, i32, vp, u32]),
         "rq_trace_queries": (i32, [vp, vp, vp, u32]),
+        "rq_trace_candidates": (i32, [vp, vp, vp, u32, vp, vp, C.c_uint64, vp, u32]),
         "rq_plan_create": (i32, [vp, vp, u32, i32, vp, vp, i32, vp, vp]),
         "rq_plan_launch": (i32, [vp]),
         "rq_plan_get_info": (i32, [vp, vp]),
@@ -460,6 +461,19 @@ class Engine:
         pb, _ = _ptr(bits)
         self._check(load().rq_trace_any(self.ctx, accel.handle, pr, n, pb, fl))
         return bits
+
+    def trace_candidates(self, accel, rays):
+        """rq_trace_candidates (boxIntersect's candidate lists): (counts per ray, ids)."""
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        n = len(rays)
+        counts = np.zeros(n, np.uint32)
+        total = C.c_uint64(0)
+        self._check(load().rq_trace_candidates(self.ctx, accel.handle, rays.ctypes.data, n, counts.ctypes.data,
+                                               None, 0, C.byref(total), 0))
+        ids = np.zeros(max(total.value, 1), np.uint32)
+        self._check(load().rq_trace_candidates(self.ctx, accel.handle, rays.ctypes.data, n, counts.ctypes.data,
+                                               ids.ctypes.data, total.value, C.byref(total), 0))
+        return counts, ids[:total.value]
 
     def trace_queries(self, accel, queries):
         """rq_trace_queries over host arrays: queries = [(rays, any_hit, out or None,

@@ -149,3 +149,23 @@ def test_synthetic_per_ray_results(oracle, scene):
     hn = oracle.trace_brute(oracle.SPHERES, oracle.REFERENCE, oracle.CLOSEST, sph, rays)
     assert np.array_equal(hn["prim"].astype(np.int32), g["none_id"])
     assert np.array_equal(np.where(hn["prim"] == oracle.MISS, np.float32(np.inf), hn["t"]), g["none_t"])
+
+
+def test_candidate_lists_match_reference_counts(oracle, bunny):
+    # castRay (main.cpp:330-358) tests every candidate boxIntersect returns,
+    # so the reference's sphere-test count over the 640x480 image is the sum
+    # of the candidate-list lengths; its closest hits are the first strictly
+    # nearer sphere along each list.
+    sph = bunny["spheres"]
+    aabb, cen = oracle.sphere_prims(sph)
+    rays = oracle.camera_rays_ref(640, 480, 1, oracle.jitter_mt19937(640 * 480 * 2))
+    m = oracle.build_median(aabb, cen, compat=True)
+    counts, ids = oracle.candidates_bvh2(m, rays)
+    assert int(counts.sum()) == len(ids) == int(bunny["bvh_sphere_tests"])
+    offs = np.concatenate([[0], np.cumsum(counts.astype(np.int64))])
+    sel = bunny["crop_index"][::8]
+    for r in sel:
+        lst = ids[offs[r]:offs[r + 1]]
+        h = oracle.trace_brute(oracle.SPHERES, oracle.REFERENCE, oracle.CLOSEST, sph[lst], rays[r:r + 1])
+        got = -1 if h["prim"][0] == oracle.MISS else int(lst[h["prim"][0]])
+        assert got == int(bunny["crop_bvh_id"][list(bunny["crop_index"]).index(r)])
