@@ -48,8 +48,9 @@ void launch_validate(const float* verts, uint32_t nv, const uint32_t* idx, uint3
 }
 
 // Zero region layout: [hist 1024][counters 16][status words][refit flags]
+// [hist 1024][counters 16][look-back status][refit flags n - 1][top count 4]
 static size_t zero_words(uint32_t n, int passes) {
-  return 1024 + 16 + sort_status_words(n, passes) + (n > 1 ? n - 1 : 0);
+  return 1024 + 16 + sort_status_words(n, passes) + (n > 1 ? n - 1 : 0) + 4;
 }
 
 BuildResult sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, bool compute_hist,
@@ -76,7 +77,8 @@ BuildResult morton_codes(const SceneView& s, int mode, uint32_t* codes, uint32_t
   if (s.kind == kTriangles) {
     launch_init_bounds(lohi, st);
     launch_point_bounds(s.verts, s.nv, 3, lohi, st);
-    launch_morton_tris(s.verts, s.idx, s.n, mode, lohi, codes, vals, hist, st);
+    if (!s.verts4 || !s.idx4) return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "triangle scene without packed copies");
+    launch_morton_tris(s.verts4, s.idx4, s.n, mode, lohi, codes, vals, hist, st);
   } else {
     if (mode != RQ_MORTON_REFERENCE) {
       launch_init_bounds(lohi, st);
@@ -101,6 +103,7 @@ static BuildResult build_lbvh(const SceneView& s, const rq_settings_t& cfg, Acce
   RQ_B(sc.vals_alt.ensure((size_t)n * 4), "sort scratch");
   RQ_B(sc.zero.ensure(zero_words(n, kSortPasses) * 4), "build scratch");
   RQ_B(sc.parent.ensure((size_t)(2 * (uint64_t)n) * 4), "parent links");
+  RQ_B(sc.mark.ensure(refit_mark_words(n) * 4), "refit marks");
   uint32_t* z = sc.zero.as<uint32_t>();
   RQ_B(cudaMemsetAsync(z, 0, zero_words(n, kSortPasses) * 4, st), "memset");
   uint32_t* codes = a.codes.as<uint32_t>();
@@ -109,10 +112,13 @@ static BuildResult build_lbvh(const SceneView& s, const rq_settings_t& cfg, Acce
   if (!r.ok()) return r;
   r = sort_pairs(codes, order, n, kSortPasses, false, sc, err, st);
   if (!r.ok()) return r;
-  launch_karras(codes, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(), st);
   uint32_t* flags = z + 1040 + sort_status_words(n, kSortPasses);
-  launch_refit(s.kind, s.verts, s.idx, s.sph, order, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(),
-               flags, a.prims.as<float4>(), a.root.as<float>(), err, st);
+  uint32_t* mk = sc.mark.as<uint32_t>();
+  const RefitTop top{mk, mk + n, mk + refit_treelet_offset(n), flags + (n > 1 ? n - 1 : 0)};
+  launch_karras(codes, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(), top, st);
+  RQ_B(launch_refit(s.kind, s.verts4, s.idx4, s.sph, order, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(),
+                    top, flags, a.prims.as<float4>(), a.root.as<float>(), err, st),
+       "LBVH refit launch");
   RQ_B(cudaGetLastError(), "LBVH launch");
   a.n_nodes = n > 1 ? n - 1 : 0;
   a.n_slots = n;

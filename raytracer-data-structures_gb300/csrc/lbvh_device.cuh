@@ -47,6 +47,19 @@ __device__ __forceinline__ F3 tri_centroid(const float* __restrict__ verts, cons
   return cen;
 }
 
+// The same from the packed copies (one 16-byte load per triangle and per
+// vertex instead of twelve scattered 4-byte loads).
+__device__ __forceinline__ F3 tri_centroid(const float4* __restrict__ verts4, const uint4* __restrict__ idx4,
+                                           uint32_t i) {
+  const uint4 t = __ldg(idx4 + i);
+  const float4 a = __ldg(verts4 + t.x), b = __ldg(verts4 + t.y), c = __ldg(verts4 + t.z);
+  F3 cen;
+  cen.x = __fdiv_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), 3.0f);
+  cen.y = __fdiv_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), 3.0f);
+  cen.z = __fdiv_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), 3.0f);
+  return cen;
+}
+
 // Karras 2012 prefix length between sorted codes i and j (index tiebreak).
 __device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ k, int64_t n, int64_t i, int64_t j,
                                             uint32_t ki) {
@@ -56,11 +69,11 @@ __device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ k, int6
   return 32 + __clz((uint32_t)i ^ (uint32_t)j);
 }
 
-// Children of internal node i (0 <= i < n - 1) of the radix tree over n
-// sorted codes, given the neighbour deltas; returns (left, right) with leaves
-// encoded as ~slot.
-__device__ __forceinline__ int2 karras_children(const uint32_t* __restrict__ codes, int64_t N, int64_t i,
-                                                uint32_t ki, int dprev, int dnext) {
+// Internal node i (0 <= i < n - 1) of the radix tree over n sorted codes,
+// given the neighbour deltas: (left, right, first leaf, last leaf), children
+// encoded as ~slot for leaves.
+__device__ __forceinline__ int4 karras_node(const uint32_t* __restrict__ codes, int64_t N, int64_t i,
+                                           uint32_t ki, int dprev, int dnext) {
   int d = (dnext - dprev) > 0 ? 1 : -1;
   int dmin = d > 0 ? dprev : dnext;
   int64_t lmax = 2;
@@ -79,7 +92,37 @@ __device__ __forceinline__ int2 karras_children(const uint32_t* __restrict__ cod
   int64_t lo = i < j ? i : j, hi = i < j ? j : i;
   int32_t lc = (lo == gamma) ? ~(int32_t)gamma : (int32_t)gamma;
   int32_t rc = (hi == gamma + 1) ? ~(int32_t)(gamma + 1) : (int32_t)(gamma + 1);
-  return make_int2(lc, rc);
+  return make_int4(lc, rc, (int32_t)lo, (int32_t)hi);
+}
+
+// (left, right) of internal node i; leaves encoded as ~slot.
+__device__ __forceinline__ int2 karras_children(const uint32_t* __restrict__ codes, int64_t N, int64_t i,
+                                                uint32_t ki, int dprev, int dnext) {
+  const int4 c = karras_node(codes, N, i, ki, dprev, dnext);
+  return make_int2(c.x, c.y);
+}
+
+// Refit decomposition of an LBVH: treelets are the maximal subtrees of at
+// most kTreeletSpan leaves (each a contiguous slot range), refitted one per
+// block in shared memory; the nodes above them (top nodes, more than
+// kTreeletSpan leaves: about 2n / kTreeletSpan of them) are refitted by one
+// block when there are at most kRefitTopCap, else by device-scope climbing.
+constexpr uint32_t kTreeletSpan = 2048;
+constexpr uint32_t kTreeletThreads = 1024;
+constexpr uint32_t kRefitTopCap = 2048;
+constexpr uint32_t kRefitTopThreads = 1024;
+constexpr uint32_t kTopMark = 0x80000000u;
+constexpr uint32_t kSlotMask = 0x7FFFFFFFu;
+constexpr uint32_t kTreeletRight = 0x80000000u;  // treelet record: the subtree is a right child
+
+// Atomic add with acquire-release semantics at device scope: the adding
+// thread's earlier stores are visible to a thread whose own add observes
+// this one, and that thread's later loads see them (one round trip instead
+// of fence + add + fence).
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
 }
 
 struct Box6 {
@@ -91,35 +134,56 @@ __device__ __forceinline__ void write_child(float4* nodes, uint32_t node, uint32
   reinterpret_cast<float2*>(nodes + 4 * (size_t)node + 2)[side] = make_float2(b.lo[2], b.hi[2]);
 }
 
-// Gather primitive `p` into payload slot `slot` (3 float4 per triangle:
-// (v0, id), (v1 - v0, 0), (v2 - v0, 0); 1 float4 per sphere) and return its box.
+// Payload of triangle p in slot `slot` (3 float4: (v0, id), (v1 - v0, 0),
+// (v2 - v0, 0)) and its box.
+__device__ __forceinline__ Box6 emit_tri(F3 a, F3 c1, F3 c2, uint32_t p, float4* __restrict__ prims,
+                                         uint32_t slot) {
+  Box6 b;
+  F3 e1 = sub_rn(c1, a), e2 = sub_rn(c2, a);
+  float4* q = prims + 3 * (size_t)slot;
+  q[0] = make_float4(a.x, a.y, a.z, __uint_as_float(p));
+  q[1] = make_float4(e1.x, e1.y, e1.z, 0.f);
+  q[2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+  b.lo[0] = fminf(fminf(a.x, c1.x), c2.x); b.hi[0] = fmaxf(fmaxf(a.x, c1.x), c2.x);
+  b.lo[1] = fminf(fminf(a.y, c1.y), c2.y); b.hi[1] = fmaxf(fmaxf(a.y, c1.y), c2.y);
+  b.lo[2] = fminf(fminf(a.z, c1.z), c2.z); b.hi[2] = fmaxf(fmaxf(a.z, c1.z), c2.z);
+  return b;
+}
+
+// Sphere p into slot `slot` (1 float4) and its box: centre -/+ radius
+// (main.cpp:686-688).
+__device__ __forceinline__ Box6 emit_sphere(const float4* __restrict__ sph, uint32_t p, float4* __restrict__ prims,
+                                            uint32_t slot) {
+  Box6 b;
+  float4 s = __ldg(sph + p);
+  prims[slot] = s;
+  b.lo[0] = __fsub_rn(s.x, s.w); b.lo[1] = __fsub_rn(s.y, s.w); b.lo[2] = __fsub_rn(s.z, s.w);
+  b.hi[0] = __fadd_rn(s.x, s.w); b.hi[1] = __fadd_rn(s.y, s.w); b.hi[2] = __fadd_rn(s.z, s.w);
+  return b;
+}
+
+// Gather primitive `p` into payload slot `slot` and return its box.
 __device__ __forceinline__ Box6 emit_prim(int kind, const float* __restrict__ verts,
                                           const uint32_t* __restrict__ idx,
                                           const float4* __restrict__ sph, uint32_t p,
                                           float4* __restrict__ prims, uint32_t slot) {
-  Box6 b;
-  if (kind == kTriangles) {
-    uint32_t i0 = __ldg(idx + 3 * (size_t)p), i1 = __ldg(idx + 3 * (size_t)p + 1),
-             i2 = __ldg(idx + 3 * (size_t)p + 2);
-    F3 a = {__ldg(verts + 3 * (size_t)i0), __ldg(verts + 3 * (size_t)i0 + 1), __ldg(verts + 3 * (size_t)i0 + 2)};
-    F3 c1 = {__ldg(verts + 3 * (size_t)i1), __ldg(verts + 3 * (size_t)i1 + 1), __ldg(verts + 3 * (size_t)i1 + 2)};
-    F3 c2 = {__ldg(verts + 3 * (size_t)i2), __ldg(verts + 3 * (size_t)i2 + 1), __ldg(verts + 3 * (size_t)i2 + 2)};
-    F3 e1 = sub_rn(c1, a), e2 = sub_rn(c2, a);
-    float4* q = prims + 3 * (size_t)slot;
-    q[0] = make_float4(a.x, a.y, a.z, __uint_as_float(p));
-    q[1] = make_float4(e1.x, e1.y, e1.z, 0.f);
-    q[2] = make_float4(e2.x, e2.y, e2.z, 0.f);
-    b.lo[0] = fminf(fminf(a.x, c1.x), c2.x); b.hi[0] = fmaxf(fmaxf(a.x, c1.x), c2.x);
-    b.lo[1] = fminf(fminf(a.y, c1.y), c2.y); b.hi[1] = fmaxf(fmaxf(a.y, c1.y), c2.y);
-    b.lo[2] = fminf(fminf(a.z, c1.z), c2.z); b.hi[2] = fmaxf(fmaxf(a.z, c1.z), c2.z);
-  } else {
-    float4 s = __ldg(sph + p);
-    prims[slot] = s;
-    // centre -/+ radius, main.cpp:686-688
-    b.lo[0] = __fsub_rn(s.x, s.w); b.lo[1] = __fsub_rn(s.y, s.w); b.lo[2] = __fsub_rn(s.z, s.w);
-    b.hi[0] = __fadd_rn(s.x, s.w); b.hi[1] = __fadd_rn(s.y, s.w); b.hi[2] = __fadd_rn(s.z, s.w);
-  }
-  return b;
+  if (kind != kTriangles) return emit_sphere(sph, p, prims, slot);
+  uint32_t i0 = __ldg(idx + 3 * (size_t)p), i1 = __ldg(idx + 3 * (size_t)p + 1), i2 = __ldg(idx + 3 * (size_t)p + 2);
+  F3 a = {__ldg(verts + 3 * (size_t)i0), __ldg(verts + 3 * (size_t)i0 + 1), __ldg(verts + 3 * (size_t)i0 + 2)};
+  F3 c1 = {__ldg(verts + 3 * (size_t)i1), __ldg(verts + 3 * (size_t)i1 + 1), __ldg(verts + 3 * (size_t)i1 + 2)};
+  F3 c2 = {__ldg(verts + 3 * (size_t)i2), __ldg(verts + 3 * (size_t)i2 + 1), __ldg(verts + 3 * (size_t)i2 + 2)};
+  return emit_tri(a, c1, c2, p, prims, slot);
+}
+
+// The same from the packed copies.
+__device__ __forceinline__ Box6 emit_prim(int kind, const float4* __restrict__ verts4,
+                                          const uint4* __restrict__ idx4,
+                                          const float4* __restrict__ sph, uint32_t p,
+                                          float4* __restrict__ prims, uint32_t slot) {
+  if (kind != kTriangles) return emit_sphere(sph, p, prims, slot);
+  const uint4 t = __ldg(idx4 + p);
+  const float4 a = __ldg(verts4 + t.x), c1 = __ldg(verts4 + t.y), c2 = __ldg(verts4 + t.z);
+  return emit_tri({a.x, a.y, a.z}, {c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}, p, prims, slot);
 }
 
 // Bottom-up refit from leaf slot j: write the leaf box into its parent, then
@@ -138,10 +202,9 @@ __device__ __forceinline__ void refit_climb(uint32_t n, uint32_t j, Box6 b, floa
   for (int level = 0;; ++level) {
     if (level >= 128) { atomicOr(err, kErrCorrupt); return; }  // Karras trees are at most 64 deep
     uint32_t node = pw >> 1, side = pw & 1u;
+    const uint32_t up = node ? __ldg(parent + node) : 0u;  // read-only here: fetch beside the add
     write_child(nodes, node, side, b);
-    __threadfence();
-    if (atomicAdd(flags + node, 1u) == 0u) return;  // the sibling's thread finishes this node
-    __threadfence();
+    if (atomic_add_acq_rel(flags + node, 1u) == 0u) return;  // the sibling's thread finishes this node
     float4 a = __ldcg(nodes + 4 * (size_t)node);
     float4 c = __ldcg(nodes + 4 * (size_t)node + 1);
     float4 z = __ldcg(nodes + 4 * (size_t)node + 2);
@@ -152,7 +215,7 @@ __device__ __forceinline__ void refit_climb(uint32_t n, uint32_t j, Box6 b, floa
       for (int k = 0; k < 3; ++k) { root_out[k] = b.lo[k]; root_out[3 + k] = b.hi[k]; }
       return;
     }
-    pw = __ldg(parent + node);
+    pw = up;
   }
 }
 

@@ -64,9 +64,23 @@ __device__ __forceinline__ void hist_flush(SharedHist& sh, uint32_t* hist) {
   }
 }
 
+// 16-byte copies of the vertices and triangles (w = 0).
+__global__ void __launch_bounds__(kThreads) k_pack_tris(const float* __restrict__ verts, uint32_t nv,
+                                                        const uint32_t* __restrict__ idx, uint32_t nt,
+                                                        float4* __restrict__ verts4, uint4* __restrict__ idx4) {
+  const uint32_t m = nv > nt ? nv : nt;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    if (i < nv)
+      verts4[i] = make_float4(__ldg(verts + 3 * (size_t)i), __ldg(verts + 3 * (size_t)i + 1),
+                              __ldg(verts + 3 * (size_t)i + 2), 0.f);
+    if (idx4 && i < nt)
+      idx4[i] = make_uint4(__ldg(idx + 3 * (size_t)i), __ldg(idx + 3 * (size_t)i + 1), __ldg(idx + 3 * (size_t)i + 2), 0u);
+  }
+}
+
 // Centroid ((v0 + v1) + v2) / 3 per axis, then scene-box normalisation.
-__global__ void __launch_bounds__(kThreads) k_morton_tris(const float* __restrict__ verts,
-                                                          const uint32_t* __restrict__ idx,
+__global__ void __launch_bounds__(kThreads) k_morton_tris(const float4* __restrict__ verts,
+                                                          const uint4* __restrict__ idx,
                                                           uint32_t nt, int mode, const int32_t* __restrict__ lohi,
                                                           uint32_t* __restrict__ keys,
                                                           uint32_t* __restrict__ vals,
@@ -144,7 +158,15 @@ void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t*
   k_point_bounds<<<grid_for(n) > 1024 ? 1024 : grid_for(n), kThreads, 0, s>>>(pts, n, stride, lohi);
 }
 
-void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, int mode, const int32_t* lohi,
+void launch_pack_tris(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, float4* verts4,
+                      uint4* idx4, cudaStream_t s) {
+  const uint32_t m = nv > nt ? nv : nt;
+  if (m == 0) return;
+  count_launch();
+  k_pack_tris<<<grid_for(m), kThreads, 0, s>>>(verts, nv, idx, idx4 ? nt : 0, verts4, idx4);
+}
+
+void launch_morton_tris(const float4* verts, const uint4* idx, uint32_t nt, int mode, const int32_t* lohi,
                         uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s) {
   if (nt == 0) return;
   count_launch();

@@ -229,22 +229,29 @@ rq_status_t rq_scene_create_triangles(rq_ctx_t ctx, const float* verts, uint32_t
   if (e == cudaSuccess) e = s->idx.ensure((size_t)nt * 12);
   if (e == cudaSuccess) e = cudaMemcpyAsync(s->verts.p, verts, (size_t)nv * 12, k, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(s->idx.p, idx, (size_t)nt * 12, k, ctx->stream);
+  if (e == cudaSuccess) e = s->verts4.ensure((size_t)nv * 16);
+  if (e == cudaSuccess) e = s->idx4.ensure((size_t)nt * 16);
   if (e == cudaSuccess) {  // finite vertices, indices < nv: checked on the device
     launch_validate(s->verts.as<float>(), nv, s->idx.as<uint32_t>(), nt, nullptr, 0, ctx->d_err, ctx->stream);
+    launch_pack_tris(s->verts.as<float>(), nv, s->idx.as<uint32_t>(), nt, s->verts4.as<float4>(),
+                     s->idx4.as<uint4>(), ctx->stream);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  if (e != cudaSuccess) {
+  auto drop = [&]() {
     s->verts.release();
     s->idx.release();
+    s->verts4.release();
+    s->idx4.release();
     delete s;
+  };
+  if (e != cudaSuccess) {
+    drop();
     return cuda_fail(ctx, e, "scene upload");
   }
   rq_status_t st = collect_device_errors(ctx);
   if (st != RQ_SUCCESS) {
-    s->verts.release();
-    s->idx.release();
-    delete s;
+    drop();
     return st;
   }
   *out = s;
@@ -301,6 +308,9 @@ rq_status_t rq_scene_update(rq_ctx_t ctx, rq_scene_t s, const float* data, const
     if (idx_bytes) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(s->idx.p, idx, idx_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     launch_validate(tri ? s->verts.as<float>() : nullptr, tri ? s->nv : 0, idx_bytes ? s->idx.as<uint32_t>() : nullptr,
                     idx_bytes ? s->n : 0, tri ? nullptr : s->sph.as<float4>(), tri ? 0 : s->n, ctx->d_err, ctx->stream);
+    if (tri)
+      launch_pack_tris(s->verts.as<float>(), s->nv, s->idx.as<uint32_t>(), s->n, s->verts4.as<float4>(),
+                       idx_bytes ? s->idx4.as<uint4>() : nullptr, ctx->stream);
     RQ_TRY(check_launch(ctx, "validate launch"));
     return RQ_SUCCESS;  // device-side validation result arrives with rq_synchronize
   }
@@ -319,6 +329,11 @@ rq_status_t rq_scene_update(rq_ctx_t ctx, rq_scene_t s, const float* data, const
   RQ_TRY(collect_device_errors(ctx));
   RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dst, st, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   if (idx_bytes) RQ_TRY_CUDA(ctx, cudaMemcpyAsync(s->idx.p, st + off, idx_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (tri) {
+    launch_pack_tris(s->verts.as<float>(), s->nv, s->idx.as<uint32_t>(), s->n, s->verts4.as<float4>(),
+                     idx_bytes ? s->idx4.as<uint4>() : nullptr, ctx->stream);
+    RQ_TRY(check_launch(ctx, "pack launch"));
+  }
   return RQ_SUCCESS;
 }
 
@@ -329,6 +344,8 @@ rq_status_t rq_scene_destroy(rq_scene_t s) {
   s->verts.release();
   s->idx.release();
   s->sph.release();
+  s->verts4.release();
+  s->idx4.release();
   delete s;
   return RQ_SUCCESS;
 }
@@ -343,6 +360,8 @@ static SceneView scene_view(rq_scene_t s) {
   v.verts = s->verts.as<const float>();
   v.idx = s->idx.as<const uint32_t>();
   v.sph = s->sph.as<const float4>();
+  v.verts4 = s->verts4.as<const float4>();
+  v.idx4 = s->idx4.as<const uint4>();
   return v;
 }
 

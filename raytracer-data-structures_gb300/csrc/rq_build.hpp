@@ -14,6 +14,8 @@ struct SceneView {
   const float* verts = nullptr;
   const uint32_t* idx = nullptr;
   const float4* sph = nullptr;
+  const float4* verts4 = nullptr;  // 16-byte copies of verts and idx (triangle scenes)
+  const uint4* idx4 = nullptr;
 };
 
 // Device memory held by one acceleration structure.
@@ -47,6 +49,7 @@ struct BuildScratch {
   DevBuf keys_alt, vals_alt;  // radix sort ping-pong
   DevBuf zero;                // [hist 1024][counters 16][look-back status][refit flags]: zeroed per build
   DevBuf parent;              // Karras parent links
+  DevBuf mark;                // refit top nodes: per-node marks, then the top list
   DevBuf lohi;                // ordered-int scene box
   DevBuf keys, vals;          // generic sort input
   DevBuf m0, m1, m2, m3, m4, m5, m6, m7;  // median / KD working arrays
@@ -54,7 +57,7 @@ struct BuildScratch {
   DevBuf work;                // work counter of lane-refill traversal
   void release() {
     work.release();
-    keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); lohi.release();
+    keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); mark.release(); lohi.release();
     keys.release(); vals.release();
     m0.release(); m1.release(); m2.release(); m3.release(); m4.release(); m5.release(); m6.release(); m7.release();
     kd_refs.release();

@@ -101,6 +101,7 @@ struct rq_scene {
   uint32_t n = 0;   // primitives
   uint32_t nv = 0;  // vertices (triangles)
   DevBuf verts, idx, sph;
+  DevBuf verts4, idx4;  // 16-byte copies of verts and idx for the LBVH build's gathers
 };
 
 struct rq_accel {

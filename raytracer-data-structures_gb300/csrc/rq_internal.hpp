@@ -75,19 +75,38 @@ void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t*
                          cudaStream_t s);
 // mode: rq_morton_t (SCENE_BOUNDS and SCENE_CUBE use lohi).  hist may be
 // null; otherwise the 4-pass digit histogram is accumulated into it.
-void launch_morton_tris(const float* verts, const uint32_t* idx, uint32_t nt, int mode, const int32_t* lohi,
+// 16-byte copies of a triangle scene (vertices as float4, triangles as uint4,
+// w = 0) for the gathers of the LBVH build; idx4 may be null (vertices only).
+void launch_pack_tris(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, float4* verts4,
+                      uint4* idx4, cudaStream_t s);
+void launch_morton_tris(const float4* verts, const uint4* idx, uint32_t nt, int mode, const int32_t* lohi,
                         uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s);
 void launch_morton_spheres(const float4* sph, uint32_t n, int mode, const int32_t* lohi,
                            uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s);
 
 // ---------------------------------------------------------------- LBVH
+// Refit decomposition written by launch_karras: mark[n - 1] (per internal
+// node), top[2048] (top node list), treelets[2n] (uint2 records) and two
+// counters (top nodes, treelets) zeroed before launch_karras.
+constexpr uint32_t kRefitTopCapHost = 2048;  // top list capacity (kRefitTopCap on the device)
+struct RefitTop {
+  uint32_t* mark;
+  uint32_t* top;
+  uint32_t* treelets;
+  uint32_t* count;  // [0] top nodes, [1] treelets
+};
+inline size_t refit_treelet_offset(uint32_t n) { return ((size_t)n + kRefitTopCapHost + 1) & ~(size_t)1; }  // 8-byte aligned
+inline size_t refit_mark_words(uint32_t n) { return refit_treelet_offset(n) + 2 * (size_t)n; }
 void launch_karras(const uint32_t* sorted_codes, uint32_t n, float4* nodes, uint32_t* parent,
-                   cudaStream_t s);
-// Gathers each slot's primitive into the slot-ordered payload, writes leaf
-// boxes into the parents and climbs to the root; root_out gets 6 floats.
-void launch_refit(int kind, const float* verts, const uint32_t* idx, const float4* sph,
-                  const uint32_t* order, uint32_t n, float4* nodes, const uint32_t* parent,
-                  uint32_t* flags, float4* prims, float* root_out, uint32_t* err, cudaStream_t s);
+                   const RefitTop& top, cudaStream_t s);
+// Gathers each slot's primitive into the slot-ordered payload and computes
+// every node box: treelets in shared memory, one block each, then the top
+// nodes in one block (or by device-scope climbing when they exceed its
+// capacity); root_out gets 6 floats.
+cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const float4* sph,
+                         const uint32_t* order, uint32_t n, float4* nodes, const uint32_t* parent,
+                         const RefitTop& top, uint32_t* flags, float4* prims, float* root_out, uint32_t* err,
+                         cudaStream_t s);
 // Payload in primitive-id order (KD and brute force) plus per-primitive boxes.
 void launch_prims_by_id(int kind, const float* verts, const uint32_t* idx, const float4* sph,
                         uint32_t n, float4* prims, float* aabb6, cudaStream_t s);

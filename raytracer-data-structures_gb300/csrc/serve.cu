@@ -253,6 +253,8 @@ void rq_server::serve(std::vector<Pending*>& batch) {
     q.sc.verts = sc->verts.as<const float>();
     q.sc.idx = sc->idx.as<const uint32_t>();
     q.sc.sph = nullptr;
+    q.sc.verts4 = sc->verts4.as<const float4>();
+    q.sc.idx4 = sc->idx4.as<const uint4>();
     sreq.push_back(q);
     const AccelBuffers& b = mesh[k]->accel->buf;
     views.push_back({b.nodes.as<const float4>(), b.prims.as<const float4>(), b.order.as<const uint32_t>(),

@@ -162,6 +162,23 @@ def heightfield(nx=1001, ny=500, amplitude=0.3, octaves=5, seed=2):
     return verts, f
 
 
+def chain_clusters(grid=16, group=32, levels=30):
+    """Sphere centres (float32, (grid*grid*levels*group, 3)): grid x grid
+    cells, each holding `levels` groups of `group` coincident points at
+    offsets of 1/2, 1/4, ... of the cell along x, y, z in turn.  Each cell's
+    Morton tree is a caterpillar that peels one group per bit level, so the
+    LBVH has far more large nodes than a balanced tree of the same size."""
+    pts = []
+    cell = 1.0 / grid
+    for cx in range(grid):
+        for cy in range(grid):
+            for k in range(levels):
+                p = np.array([cx * cell, cy * cell, 0.0])
+                p[k % 3] += cell * 2.0 ** -(k // 3 + 1)
+                pts.append(np.repeat(p[None], group, 0))
+    return np.concatenate(pts).astype(np.float32)
+
+
 def merged_icospheres(count=150, target_tris=10_000_000, seed=3, levels=(5, 6, 7)):
     """Many displaced icospheres merged into one mesh; subdivision levels are
     drawn by seed so the total lands near target_tris (the count is recorded

@@ -91,6 +91,46 @@ def test_lbvh_heightfield_bit_exact(engine, oracle, rqm):
     _check_lbvh_against_oracle(engine, oracle, acc, aabb, oracle.morton_centroids(cen, lo, hi))
 
 
+def test_lbvh_full_size_heightfield_bit_exact(engine, oracle, rqm):
+    """The 998,000-triangle terrain of the throughput workload with cube
+    Morton codes: about 670 treelets and 670 top nodes (the top block); a
+    rebuild reproduces the tree."""
+    v, f = scenes.heightfield(1001, 500, seed=2)
+    engine.configure(morton=rqm.MORTON_SCENE_CUBE)
+    s = engine.scene_triangles(v, f)
+    acc = engine.build(s, rqm.LBVH)
+    _, aabb, cen = oracle.tri_prims(v, f)
+    lo, hi = oracle.bounds3(v)
+    codes = oracle.morton_centroids(cen, lo, hi, cube=True)
+    first = _check_lbvh_against_oracle(engine, oracle, acc, aabb, codes)[0]
+    acc.rebuild()
+    assert np.array_equal(engine.export_bvh2(acc)[0].view(np.int32), first.view(np.int32))
+
+
+def test_lbvh_more_top_nodes_than_the_top_block(engine, oracle, rqm):
+    """6M uniform points: about 4,100 nodes of more than 2048 leaves, more
+    than the top block holds, so the treelet roots climb to the root with
+    device-scope arrival counts."""
+    pts = np.random.default_rng(7).random((6_000_000, 3), dtype=np.float32)
+    sph = np.concatenate([pts, np.full((len(pts), 1), 1e-4, np.float32)], 1)
+    acc = engine.build(engine.scene_spheres(sph), rqm.LBVH)
+    aabb, _ = oracle.sphere_prims(sph)
+    _check_lbvh_against_oracle(engine, oracle, acc, aabb, oracle.morton_centroids(pts, pts.min(0), pts.max(0)))
+
+
+@pytest.mark.parametrize("group,levels", [(32, 30), (64, 20)])
+def test_lbvh_caterpillar_trees_bit_exact(engine, oracle, rqm, group, levels):
+    """Caterpillar clusters (each cell's tree peels one group per bit level):
+    deep, unbalanced treelets."""
+    pts = scenes.chain_clusters(16, group, levels)
+    sph = np.concatenate([pts, np.full((len(pts), 1), 1e-3, np.float32)], 1)
+    s = engine.scene_spheres(sph)
+    acc = engine.build(s, rqm.LBVH)
+    aabb, _ = oracle.sphere_prims(sph)
+    lo, hi = oracle.bounds3(pts)
+    _check_lbvh_against_oracle(engine, oracle, acc, aabb, oracle.morton_centroids(pts, lo, hi))
+
+
 def test_lbvh_single_and_two_primitives(engine, oracle, rqm):
     for sph in (np.array([[1, 2, 3, 0.5]], np.float32), np.array([[0, 0, -5, 1], [0, 0, -5, 1]], np.float32)):
         s = engine.scene_spheres(sph)
