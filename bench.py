@@ -344,6 +344,12 @@ def run_ours(args):
                                            * (RAY_BYTES + HIT_BYTES)) / (kern[dom] * 1e-3) / 1e9) / peak, 4)
                 if dom != "build" else None}
 
+    # The same step through the C ABI with host buffers, right after the
+    # device-resident step (before the other legs leave memory and heat behind).
+    e2e = None
+    if rank == 0 and not args.skip_e2e:
+        e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice)
+
     # The same rays through the other builders of the dataStructure switch.
     structures = {"LBVH": {"build_ms": round(build_ms, 4), "trace_ms": round(prim_ms + sec_ms + sh_ms, 4),
                            "grays_s": round(total_rays / ((prim_ms + sec_ms + sh_ms) * 1e-3) / 1e9, 4)}}
@@ -383,10 +389,6 @@ def run_ours(args):
     served = None
     if not args.skip_serve and ws == 1:
         served = run_serve_leg(args)
-
-    e2e = None
-    if rank == 0 and not args.skip_e2e:
-        e2e = run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:

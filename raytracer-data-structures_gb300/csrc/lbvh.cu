@@ -439,21 +439,16 @@ cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   static std::atomic<uint64_t> attr_set{0};  // devices whose kernels allow their shared memory
-  static std::atomic<int> sm_count[64];
   const uint64_t bit = 1ull << (dev & 63);
   if (!(attr_set.load() & bit)) {
-    int sms = 0;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_refit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RefitShared));
+    e = cudaFuncSetAttribute(k_refit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RefitShared));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_refit_top, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TopShared));
     if (e != cudaSuccess) return e;
-    sm_count[dev & 63].store(sms > 0 ? sms : 1);
     attr_set.fetch_or(bit);
   }
-  // Persistent: two treelet blocks per SM loop over the treelet list.
-  const uint32_t blocks = n == 1 ? 1u : 2u * (uint32_t)sm_count[dev & 63].load();
+  // Persistent: two treelet blocks per SM take treelets from a queue.
+  const uint32_t blocks = n == 1 ? 1u : 2u * (uint32_t)device_sm_count();
   count_launch();
   k_refit<<<blocks, kTreeletThreads, sizeof(RefitShared), s>>>(kind, verts, idx, sph, order, n, nodes, parent,
                                                                t.treelets, t.count, flags, prims, root_out, err);

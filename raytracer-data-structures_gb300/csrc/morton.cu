@@ -1,5 +1,7 @@
 // Morton codes over primitive centroids (accelerators.h:374-394, 575-580),
 // fused with the radix sort's digit histogram so the codes are read once.
+#include <atomic>
+
 #include "lbvh_device.cuh"
 
 namespace rq {
@@ -53,9 +55,19 @@ struct SharedHist {
 __device__ __forceinline__ void hist_zero(SharedHist& sh) {
   for (int i = threadIdx.x; i < 1024; i += blockDim.x) (&sh.h[0][0])[i] = 0;
 }
-__device__ __forceinline__ void hist_add(SharedHist& sh, uint32_t code) {
+// One shared atomic per distinct digit value in the warp (the upper digits
+// of spatially sorted codes repeat across most lanes).  Called by whole
+// warps: `active` is the lanes holding a code.
+__device__ __forceinline__ void hist_add(SharedHist& sh, uint32_t code, bool active) {
+  const uint32_t lanes = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const uint32_t lane = threadIdx.x & 31u;
 #pragma unroll
-  for (int p = 0; p < 4; ++p) atomicAdd(&sh.h[p][(code >> (8 * p)) & 255u], 1u);
+  for (int p = 0; p < 4; ++p) {
+    const uint32_t d = (code >> (8 * p)) & 255u;
+    const uint32_t same = __match_any_sync(lanes, d);
+    if ((same & ((1u << lane) - 1u)) == 0u) atomicAdd(&sh.h[p][d], (uint32_t)__popc(same));
+  }
 }
 __device__ __forceinline__ void hist_flush(SharedHist& sh, uint32_t* hist) {
   for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
@@ -94,11 +106,17 @@ __global__ void __launch_bounds__(kThreads) k_morton_tris(const float4* __restri
   }
   __syncthreads();
   float lo[3] = {s_lo[0], s_lo[1], s_lo[2]}, ext[3] = {s_ext[0], s_ext[1], s_ext[2]};
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
-    uint32_t code = code_scene(tri_centroid(verts, idx, i), lo, ext);
-    keys[i] = code;
-    vals[i] = i;
-    if (hist) hist_add(sh, code);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < nt; i0 += stride) {  // whole warps run every round
+    const uint32_t i = i0 + threadIdx.x;
+    const bool live = i < nt;
+    uint32_t code = 0;
+    if (live) {
+      code = code_scene(tri_centroid(verts, idx, i), lo, ext);
+      keys[i] = code;
+      vals[i] = i;
+    }
+    if (hist) hist_add(sh, code, live);
   }
   if (hist) {
     __syncthreads();
@@ -119,19 +137,24 @@ __global__ void __launch_bounds__(kThreads) k_morton_spheres(const float4* __res
     if (mode == RQ_MORTON_SCENE_CUBE) cube_extent(s_ext);
   }
   __syncthreads();
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 s = __ldg(sph + i);
-    uint32_t code;
-    if (mode == RQ_MORTON_REFERENCE) {
-      // (center + 30) / 1000, accelerators.h:577
-      code = morton3d(__fdiv_rn(__fadd_rn(s.x, 30.f), 1000.f), __fdiv_rn(__fadd_rn(s.y, 30.f), 1000.f),
-                      __fdiv_rn(__fadd_rn(s.z, 30.f), 1000.f));
-    } else {
-      code = code_scene({s.x, s.y, s.z}, s_lo, s_ext);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {  // whole warps run every round
+    const uint32_t i = i0 + threadIdx.x;
+    const bool live = i < n;
+    uint32_t code = 0;
+    if (live) {
+      float4 s = __ldg(sph + i);
+      if (mode == RQ_MORTON_REFERENCE) {
+        // (center + 30) / 1000, accelerators.h:577
+        code = morton3d(__fdiv_rn(__fadd_rn(s.x, 30.f), 1000.f), __fdiv_rn(__fadd_rn(s.y, 30.f), 1000.f),
+                        __fdiv_rn(__fadd_rn(s.z, 30.f), 1000.f));
+      } else {
+        code = code_scene({s.x, s.y, s.z}, s_lo, s_ext);
+      }
+      keys[i] = code;
+      vals[i] = i;
     }
-    keys[i] = code;
-    vals[i] = i;
-    if (hist) hist_add(sh, code);
+    if (hist) hist_add(sh, code, live);
   }
   if (hist) {
     __syncthreads();
@@ -144,7 +167,27 @@ int grid_for(uint32_t n) {
   return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
+// Morton kernels: a few blocks per SM, each looping over many primitives, so
+// that each block's shared histogram flushes once for thousands of codes
+// (one block per 256 codes meant over a million global atomics on 1024 bins).
+int grid_for_hist(uint32_t n) {
+  const int g = grid_for(n), cap = 4 * device_sm_count();
+  return g < cap ? g : cap;
+}
+
 }  // namespace
+
+int device_sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  int v = cache[dev & 63].load();
+  if (v == 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    cache[dev & 63].store(v);
+  }
+  return v;
+}
 
 void launch_init_bounds(int32_t* lohi, cudaStream_t s) {
   count_launch();
@@ -170,14 +213,15 @@ void launch_morton_tris(const float4* verts, const uint4* idx, uint32_t nt, int 
                         uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s) {
   if (nt == 0) return;
   count_launch();
-  k_morton_tris<<<grid_for(nt), kThreads, 0, s>>>(verts, idx, nt, mode, lohi, keys, vals, hist);
+  k_morton_tris<<<hist ? grid_for_hist(nt) : grid_for(nt), kThreads, 0, s>>>(verts, idx, nt, mode, lohi, keys,
+                                                                             vals, hist);
 }
 
 void launch_morton_spheres(const float4* sph, uint32_t n, int mode, const int32_t* lohi,
                            uint32_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t s) {
   if (n == 0) return;
   count_launch();
-  k_morton_spheres<<<grid_for(n), kThreads, 0, s>>>(sph, n, mode, lohi, keys, vals, hist);
+  k_morton_spheres<<<hist ? grid_for_hist(n) : grid_for(n), kThreads, 0, s>>>(sph, n, mode, lohi, keys, vals, hist);
 }
 
 }  // namespace rq

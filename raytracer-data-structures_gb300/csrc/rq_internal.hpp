@@ -75,6 +75,8 @@ void launch_point_bounds(const float* pts, uint32_t n, uint32_t stride, int32_t*
                          cudaStream_t s);
 // mode: rq_morton_t (SCENE_BOUNDS and SCENE_CUBE use lohi).  hist may be
 // null; otherwise the 4-pass digit histogram is accumulated into it.
+// SM count of the current device (cached per device); 1 if it cannot be read.
+int device_sm_count();
 // 16-byte copies of a triangle scene (vertices as float4, triangles as uint4,
 // w = 0) for the gathers of the LBVH build; idx4 may be null (vertices only).
 void launch_pack_tris(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, float4* verts4,
