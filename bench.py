@@ -780,25 +780,52 @@ class CpuBaseline:
                 break
             self.sample *= 4
 
-    def measure(self):
+    def measure(self, threads=None, limit=None):
         O = self.O
         per = {}
         for k, (rays, q) in self.pool.items():
-            r = rays[self.sel[k]]
+            r = rays[self.sel[k][:limit]]
             t1 = time.perf_counter()
-            O.trace_bvh2(O.TRIANGLES, O.REFERENCE, q, self.bvh, self.prims, r, nthreads=self.cores)
+            O.trace_bvh2(O.TRIANGLES, O.REFERENCE, q, self.bvh, self.prims, r, nthreads=threads or self.cores)
             per[k] = (time.perf_counter() - t1) / len(r)
         return per
 
+    def whole_job(self, per):
+        return sum(self.counts.values()) / (self.build_s + sum(per[k] * self.counts[k] for k in per)) / 1e9
+
     def record(self, per):
-        trace_s = sum(per[k] * self.counts[k] for k in per)
-        value = sum(self.counts.values()) / (self.build_s + trace_s) / 1e9
-        return {"value": value, "unit": UNIT, "cores": self.cores, "kind": "port",
+        one_n = max(256, self.sample // 8)
+        one = self.measure(threads=1, limit=one_n)  # the same rays' first eighth on one thread
+        return {"value": self.whole_job(per), "unit": UNIT, "cores": self.cores, "kind": "port",
                 "sample": (f"median-BVH build of all {self.n_tri} triangles (1 thread, {self.build_s:.2f} s) + "
                            f"{self.sample} seeded rays per class (primary/secondary/shadow) traced with the "
                            f"reference's collect-all traversal on {self.cores} threads; whole job = build + "
                            f"per-ray cost x full ray counts"),
-                "build_s": round(self.build_s, 3), "per_ray_us": {k: round(v * 1e6, 3) for k, v in per.items()}}
+                "build_s": round(self.build_s, 3), "per_ray_us": {k: round(v * 1e6, 3) for k, v in per.items()},
+                "nproc": self.cores, "cpu_model": cpu_model(),
+                "one_core": {"value": self.whole_job(one), "rays_per_class": min(one_n, self.sample),
+                             "per_ray_us": {k: round(v * 1e6, 3) for k, v in one.items()}}}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
 
 
 def cpu_baseline(verts, idx, primary, secondary, shadow, budget_s=20.0):
