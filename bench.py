@@ -235,7 +235,7 @@ def run_ours(args):
                   rq.RAY_SORT_ORIGIN_DIRECTION: "origin_direction", rq.RAY_SORT_DIRECTION_ORIGIN: "direction_origin",
                   rq.RAY_SORT_OCTANT_MORTON12: "octant_morton12"}
     sched_names = {rq.SCHEDULING_THREAD_PER_RAY: "thread_per_ray", rq.SCHEDULING_LANE_REFILL: "lane_refill",
-                   rq.SCHEDULING_SPECULATIVE: "speculative"}
+                   rq.SCHEDULING_SPECULATIVE: "speculative", rq.SCHEDULING_WARP_PACKET: "warp_packet"}
     morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
     tuning = {}
     best = None
@@ -260,6 +260,8 @@ def run_ours(args):
                     eng.configure(ray_sort=srt, scheduling=sch)
                     opts[(srt, sch)] = timed(class_call(cand, name))
                 choice[name] = min(opts, key=opts.get)
+                log(f"[bench] tune width {width} {morton_names[morton]} {name}: " +
+                    ", ".join(f"{sort_names[a]}/{sched_names[b]} {t:.3f}" for (a, b), t in sorted(opts.items(), key=lambda kv: kv[1])))
                 total += opts[choice[name]]
             tuning[f"width{max(width, 2)}_{morton_names[morton]}"] = {
                 "est_step_ms": round(total, 4),
@@ -917,7 +919,7 @@ def run_case(args):
                 "shadow": scenes.shadow_rays(verts, idx, primary, hits_p, LIGHT)}[args.case]
         d_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8)).to(dev)
         d_out = torch.empty(len(rays) * HIT_BYTES, dtype=torch.uint8, device=dev)
-        eng.configure(ray_sort=args.ray_sort)
+        eng.configure(ray_sort=args.ray_sort, scheduling=args.scheduling)
         if args.case == "build":
             call = acc.rebuild
         elif args.case == "shadow":
@@ -948,6 +950,7 @@ def main():
     ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "batched"],
                     help="profiling driver: run one query class, print no bench line")
     ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
+    ap.add_argument("--scheduling", type=int, default=0, help="--case: settings.scheduling (0-3)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner and use its GB300 choice (binary nodes, cube Morton codes, "
                          "15-bit ray order for secondary rays): profiling the measured kernel mix")

@@ -184,7 +184,8 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   const bool sorted = fast && cfg.ray_sort != RQ_RAY_SORT_NONE && q.n >= kRaySortMin;
   const bool refill = fast && cfg.scheduling == RQ_SCHEDULING_LANE_REFILL && a.node_width != 4;
   const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && a.node_width != 4;
-  if (!sorted && !refill && !spec) {
+  const bool packet = fast && cfg.scheduling == RQ_SCHEDULING_WARP_PACKET && a.node_width != 4;
+  if (!sorted && !refill && !spec && !packet) {
     launch_query(type, s, a, cfg.traversal, any, q, err, st);
     RQ_B(cudaGetLastError(), "trace launch");
     return {};
@@ -205,6 +206,11 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   }
   Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
              a.root.as<const float>(), a.n_nodes, a.n_slots};
+  if (packet) {
+    launch_trace_bvh2_packet(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, perm, st);
+    RQ_B(cudaGetLastError(), "trace launch");
+    return {};
+  }
   if (spec) {
     launch_trace_bvh2_spec(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, perm, st);
     RQ_B(cudaGetLastError(), "trace launch");

@@ -93,6 +93,98 @@ void dispatch_bvh4(const Bvh4View& v, const float4* rays, uint32_t n, float4* hi
     k_trace_bvh4<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm, nullptr);
 }
 
+// Warp-packet walk (RQ_SCHEDULING_WARP_PACKET): the warp walks the tree as
+// one, with one stack whose entries carry the mask of lanes whose ray entered
+// that child.  Each node is fetched once for the warp (a broadcast load); the
+// lanes in the node's mask test its two child boxes against their own
+// closest hit, and the warp goes next to the child most of them reach first.
+// Every lane tests only nodes its ray entered, so results are those of the
+// per-ray walk (the closest-hit rule makes them independent of visit order);
+// coherent rays (camera, shadow) trade a few extra visits for full warps.
+template <int KIND, bool ANY>
+__global__ void __launch_bounds__(kThreads, 10) k_trace_packet(Bvh2View bvh, const float4* __restrict__ rays,
+                                                               uint32_t n, float4* __restrict__ hits,
+                                                               uint32_t* __restrict__ occ, uint32_t* err,
+                                                               const uint32_t* __restrict__ perm) {
+  __shared__ int4 stack_s[kThreads / 32][kStackSize];  // (node, count, lane mask, -)
+  int4* stack = stack_s[threadIdx.x >> 5];
+  const uint32_t lane = threadIdx.x & 31u, bit = 1u << lane;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < n;
+  const uint32_t r = (perm && live) ? __ldg(perm + i) : i;
+  Ray ray = live ? load_ray(rays, r) : Ray{{0.f, 0.f, 0.f}, {0.f, 0.f, 1.f}, 0.f, 0.f};
+  Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+  const SlabRay sr = slab_ray(ray.o, ray.d);
+  const float* rb = bvh.root;
+  float tn;
+  const bool in_root = live && slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn);
+  uint32_t mask = __ballot_sync(0xffffffffu, in_root);
+  uint32_t alive = mask;  // lanes still searching (any hit: not yet occluded)
+  bool occluded = false;
+  int sp = 0;
+  int cur = bvh.n_internal ? 0 : -1;
+  int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
+  const uint32_t max_steps = 2u * (bvh.n_internal + bvh.n_slots) + 8u;
+  for (uint32_t steps = 0; mask; ++steps) {  // mask, cur, cnt, sp: uniform across the warp
+    if (steps > max_steps) {
+      if (lane == 0) atomicOr(err, kErrCorrupt);
+      break;
+    }
+    const bool act = (mask & bit) != 0u;
+    if (cur >= 0) {
+      const float4* nd = bvh.nodes + 4 * (size_t)cur;
+      const float4 a = __ldg(nd), b = __ldg(nd + 1), z = __ldg(nd + 2);
+      const int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+      bool hl = false, hr = false;
+      float tl = 0.f, tr = 0.f;
+      if (act) {
+        const float tfar = ANY ? ray.tmax : c.t;
+        hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+        hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+      }
+      const uint32_t ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
+      if (ml && mr) {
+        const uint32_t lfirst = __ballot_sync(0xffffffffu, hl && (!hr || tl <= tr));
+        const bool left = 2 * __popc(lfirst) >= __popc(ml | mr);
+        if (sp >= kStackSize) {
+          if (lane == 0) atomicOr(err, kErrStackOverflow);
+          break;
+        }
+        if (lane == 0) stack[sp] = left ? make_int4(l.y, l.w, (int)mr, 0) : make_int4(l.x, l.z, (int)ml, 0);
+        __syncwarp();
+        ++sp;
+        cur = left ? l.x : l.y;
+        cnt = left ? l.z : l.w;
+        mask = left ? ml : mr;
+        continue;
+      }
+      if (ml) { cur = l.x; cnt = l.z; mask = ml; continue; }
+      if (mr) { cur = l.y; cnt = l.w; mask = mr; continue; }
+    } else {
+      if (act && test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) occluded = true;
+      if (ANY) alive &= ~__ballot_sync(0xffffffffu, occluded);
+    }
+    // Next entry that still has a lane to serve.
+    mask = 0u;
+    while (sp > 0 && !mask) {
+      const int4 e = stack[--sp];
+      cur = e.x;
+      cnt = e.y;
+      mask = (uint32_t)e.z & alive;
+    }
+  }
+  if (live && !ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  if (ANY) {
+    if (perm) {
+      if (live && occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+    } else {
+      const uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+      const uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+      if (lane == 0 && w0 < n) occ[w0 >> 5] = bits;
+    }
+  }
+}
+
 // -------------------------------------------------------- speculative walk
 // While-while walk with speculative leaf postponement (Aila and Laine 2009,
 // "Understanding the Efficiency of Ray Traversal on GPUs"): a lane that meets
@@ -599,6 +691,21 @@ void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4*
   } else {
     if (any) k_trace_spec<kSpheres, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
     else k_trace_spec<kSpheres, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
+  }
+}
+
+void launch_trace_bvh2_packet(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
+                              uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch();
+  if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
+  const uint32_t g = (n + kThreads - 1) / kThreads;
+  if (kind == kTriangles) {
+    if (any) k_trace_packet<kTriangles, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
+    else k_trace_packet<kTriangles, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
+  } else {
+    if (any) k_trace_packet<kSpheres, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
+    else k_trace_packet<kSpheres, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm);
   }
 }
 

@@ -70,12 +70,13 @@ def test_streamed_host_queries_equal_device_queries(engine, rqm):
 
 @pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])
 @pytest.mark.parametrize("ray_sort", [0, 1])
-@pytest.mark.parametrize("sched", ["LANE_REFILL", "SPECULATIVE"])
+@pytest.mark.parametrize("sched", ["LANE_REFILL", "SPECULATIVE", "WARP_PACKET"])
 def test_scheduling_is_result_neutral(engine, oracle, rqm, acc_name, ray_sort, sched):
-    """Persistent warps that refill finished lanes, and the speculative
-    while-while walk (settings.scheduling), give bit-identical hits and
-    occlusion bits, with and without ray reordering, for triangles and
-    spheres, equal to the oracle's plain walk."""
+    """Persistent warps that refill finished lanes, the speculative
+    while-while walk and the warp-packet walk (settings.scheduling) give
+    bit-identical hits and occlusion bits, with and without ray reordering,
+    for camera and secondary rays, triangles and spheres, equal to the
+    oracle's plain walk."""
     mode = getattr(rqm, "SCHEDULING_" + sched)
     v, f = scenes.heightfield(301, 150, seed=17)
     s = engine.scene_triangles(v, f)
@@ -85,7 +86,10 @@ def test_scheduling_is_result_neutral(engine, oracle, rqm, acc_name, ray_sort, s
     sec = scenes.cosine_rays(v, f, primary, h0, seed=19)
     ref_c = engine.trace_closest(acc, sec)
     ref_a = engine.trace_any(acc, sec)
+    ref_pa = engine.trace_any(acc, primary)
     engine.configure(scheduling=mode, ray_sort=ray_sort)
+    assert np.array_equal(engine.trace_closest(acc, primary).view(np.uint32), h0.view(np.uint32))
+    assert np.array_equal(engine.trace_any(acc, primary), ref_pa)
     assert np.array_equal(engine.trace_closest(acc, sec).view(np.uint32), ref_c.view(np.uint32))
     assert np.array_equal(engine.trace_any(acc, sec), ref_a)
     for n in (1, 31, 33, 1000):  # partial warps and tiny batches
