@@ -229,7 +229,7 @@ __device__ __forceinline__ void climb_top(uint32_t pw, Box6 b, bool top_mode, fl
 // the treelet: one block gathers the leaves' primitives, climbs with
 // shared-memory boxes and arrival bits (block-scope ordering only) and at
 // the end stores the finished nodes' boxes, coalesced.
-__global__ void __launch_bounds__(kTreeletThreads, 2) k_refit(int kind, const float4* __restrict__ verts,
+__global__ void __launch_bounds__(kTreeletThreads, kTreeletBlocksPerSM) k_refit(int kind, const float4* __restrict__ verts,
                                                           const uint4* __restrict__ idx,
                                                           const float4* __restrict__ sph,
                                                           const uint32_t* __restrict__ order, uint32_t n,
@@ -447,8 +447,8 @@ cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const 
     if (e != cudaSuccess) return e;
     attr_set.fetch_or(bit);
   }
-  // Persistent: two treelet blocks per SM take treelets from a queue.
-  const uint32_t blocks = n == 1 ? 1u : 2u * (uint32_t)device_sm_count();
+  // Persistent: kTreeletBlocksPerSM treelet blocks per SM take treelets from a queue.
+  const uint32_t blocks = n == 1 ? 1u : kTreeletBlocksPerSM * (uint32_t)device_sm_count();
   count_launch();
   k_refit<<<blocks, kTreeletThreads, sizeof(RefitShared), s>>>(kind, verts, idx, sph, order, n, nodes, parent,
                                                                t.treelets, t.count, flags, prims, root_out, err);

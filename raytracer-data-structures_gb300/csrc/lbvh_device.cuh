@@ -109,6 +109,7 @@ __device__ __forceinline__ int2 karras_children(const uint32_t* __restrict__ cod
 // block when there are at most kRefitTopCap, else by device-scope climbing.
 constexpr uint32_t kTreeletSpan = 2048;
 constexpr uint32_t kTreeletThreads = 1024;
+constexpr uint32_t kTreeletBlocksPerSM = 2;  // 2 x 112 KB of shared memory, 32 registers per thread
 constexpr uint32_t kRefitTopCap = 2048;
 constexpr uint32_t kRefitTopThreads = 1024;
 constexpr uint32_t kTopMark = 0x80000000u;
