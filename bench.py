@@ -721,11 +721,12 @@ def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_
     tb, out_b = pinned(np.zeros((len(shadow) + 31) // 32, np.uint32)); keep.append(tb)
 
     def step():
-        # one call for the three queries: copies and traversals overlap across them
+        # one call for the three queries: copies and traversals overlap across
+        # them; the incoherent secondary rays (the longest traversal) first
         scene.update(hv, hi)
         acc.rebuild()
-        eng.trace_queries(acc, [(hp, False, out_p, sort_choice["primary"][0], sort_choice["primary"][1]),
-                                (hs, False, out_s, sort_choice["secondary"][0], sort_choice["secondary"][1]),
+        eng.trace_queries(acc, [(hs, False, out_s, sort_choice["secondary"][0], sort_choice["secondary"][1]),
+                                (hp, False, out_p, sort_choice["primary"][0], sort_choice["primary"][1]),
                                 (hsh, True, out_b, sort_choice["shadow"][0], sort_choice["shadow"][1])])
 
     for _ in range(max(1, args.warmup)):

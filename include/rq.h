@@ -304,9 +304,13 @@ typedef struct rq_query_t {
   int32_t scheduling;     /* rq_scheduling_t for this query; -1: the context's setting */
 } rq_query_t;
 /* Several host-buffer queries on one structure in one call, with copies
- * and traversals overlapped across queries: the first query streams chunk
- * by chunk, later ones upload whole while earlier ones trace (each then
- * traced as one batch) and download while later ones trace.  Results equal
+ * and traversals overlapped across queries: queries run in the given order;
+ * the first streams chunk by chunk when it has no ray order, the others (and
+ * a first query with a ray order, whose order pays off only over the whole
+ * batch) upload whole while earlier ones trace, each traced as one batch,
+ * and download while later ones trace.  Uploads begin at once, overlapping
+ * work already queued on the context's stream such as a rebuild.  Put the
+ * query with the longest traversal first.  Results equal
  * rq_trace_closest / rq_trace_any per query; returns when every result is in
  * host memory.  Device memory: each query after the first keeps a buffer of
  * its rays and results (grow-only, per context). */

@@ -600,11 +600,14 @@ static rq_status_t trace_streamed_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_r
     RQ_TRY_CUDA(ctx, p.rays[k].ensure((size_t)kPipeChunk * 32));
     RQ_TRY_CUDA(ctx, p.out[k].ensure(out_chunk));
   }
-  // copies start after everything already queued on the context's stream
+  // Traversals start after everything already queued on the context's
+  // stream (a rebuild, say); uploads start at once, overlapping that work,
+  // after only the previous call's use of each slot (events never recorded
+  // are complete).
   RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, ctx->stream));
-  RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, p.start, 0));
   RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.down, p.start, 0));
   RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.lane2, p.start, 0));
+  for (int k = 0; k < kPipeSlots; ++k) RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, p.downloaded[k], 0));
   const SceneView sv = scene_view(a->scene);
   // Chunk plan: a quarter and a half chunk first (a short first upload), full
   // chunks, then halving chunks at the end (a short last traversal and
@@ -784,13 +787,15 @@ static rq_status_t trace_queries_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_qu
     if (q.scheduling >= 0) c.scheduling = q.scheduling;
     return c;
   };
+  // The first query streams in chunks unless it has a ray order: an order
+  // pays off over the whole batch (sorted chunks of 2M rays trace about as
+  // slowly as unsorted ones), so such a query uploads whole like the others.
   uint32_t first = 0;
-  if (qs[0].n >= 2 * kPipeChunk) {
+  if (qs[0].n >= 2 * kPipeChunk && cfg_of(qs[0]).ray_sort == RQ_RAY_SORT_NONE) {
     RQ_TRY(trace_streamed_enqueue(ctx, a, qs[0].rays, qs[0].n, qs[0].out, qs[0].any != 0, cfg_of(qs[0]), false));
     first = 1;
   } else {
     RQ_TRY_CUDA(ctx, cudaEventRecord(p.start, ctx->stream));
-    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, p.start, 0));
     RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.down, p.start, 0));
   }
   if (p.q_rays.size() < nq) {
@@ -813,6 +818,9 @@ static rq_status_t trace_queries_enqueue(rq_ctx_t ctx, rq_accel_t a, const rq_qu
     const rq_query_t& q = qs[k];
     if (q.n == 0) continue;
     cudaEvent_t up = p.q_events[2 * k], done = p.q_events[2 * k + 1];
+    // the upload overwrites this query's buffer once the previous call's
+    // traversal of it is done (uploads overlap work queued before the call)
+    RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(p.up, done, 0));
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(p.q_rays[k].p, q.rays, (size_t)q.n * 32, cudaMemcpyHostToDevice, p.up));
     RQ_TRY_CUDA(ctx, cudaEventRecord(up, p.up));
     RQ_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, up, 0));
