@@ -134,3 +134,29 @@ def test_trace_queries_equal_single_queries(engine, rqm):
     got = engine.trace_queries(acc, [(sec, False, None, -1, -1), (sh, True, None, -1, -1)])
     assert np.array_equal(got[0].view(np.uint32), want[1].view(np.uint32))
     assert np.array_equal(got[1], want[2])
+    # so does a large first query with a ray order; back-to-back calls reuse the buffers
+    for _ in range(2):
+        got = engine.trace_queries(acc, [(primary, False, None, rqm.RAY_SORT_OCTANT_MORTON12, -1),
+                                         (sec, False, None, -1, -1), (sh, True, None, -1, -1)])
+        assert np.array_equal(got[0].view(np.uint32), h0.view(np.uint32))
+        assert np.array_equal(got[1].view(np.uint32), want[1].view(np.uint32))
+        assert np.array_equal(got[2], want[2])
+
+
+def test_trace_queries_follow_a_queued_rebuild(engine, rqm):
+    """The uploads of rq_trace_queries overlap a rebuild queued just before
+    the call; the traversals must still see the rebuilt structure."""
+    v, f = scenes.heightfield(301, 150, seed=24)
+    s = engine.scene_triangles(v, f)
+    acc = engine.build(s, "LBVH")
+    primary = scenes.pinhole_rays(1250, 1000, 4, eye=(0, -0.6, 1.1), target=(0, 0, 0), seed=25)
+    engine.trace_queries(acc, [(primary, False, None, -1, -1)])  # buffers of the old geometry in flight before
+    v2 = v.copy()
+    v2[:, 2] += 0.05 * np.sin(7.0 * v[:, 0]).astype(np.float32)
+    s.update(v2)
+    acc.rebuild()
+    got = engine.trace_queries(acc, [(primary, False, None, rqm.RAY_SORT_OCTANT_MORTON12, -1),
+                                     (primary[:1_000_000], True, None, -1, -1)])
+    ref = engine.build(engine.scene_triangles(v2, f), "LBVH")
+    assert np.array_equal(got[0].view(np.uint32), engine.trace_closest(ref, primary).view(np.uint32))
+    assert np.array_equal(got[1], engine.trace_any(ref, primary[:1_000_000]))
