@@ -609,7 +609,9 @@ def run_batch_leg(eng, stream, dev, args):
                        "build_mtri_s": round(n_tri / (batched_build_ms * 1e-3) / 1e6, 1),
                        "graph_kernels": int(info.graph_kernels),
                        "shape": {"block": int(info.block_threads), "stack": int(info.stack_entries),
-                                 "tuned_ms": [round(float(x), 3) for x in info.shape_ms]}},
+                                 "ray_order": bool(info.ray_order),
+                                 "tuned_ms": [round(float(x), 3) for x in info.shape_ms],
+                                 "tuned_ordered_ms": [round(float(x), 3) for x in info.ordered_ms]}},
            "speedup": round(plain_ms / batched_ms, 3), "hits_identical": same}
     log(f"[bench] batched: {out}")
     return out

@@ -354,6 +354,8 @@ typedef struct rq_plan_info_t {
   uint32_t n_rays;
   uint32_t rebuilds;        /* 1 when the step rebuilds the batch */
   float shape_ms[4];        /* query time of 128/shallow, 128/deep, 256/shallow, 256/deep; < 0: dropped */
+  uint32_t ray_order;       /* 1 when the plan traces through a per-scene ray order (chosen by time) */
+  float ordered_ms[4];      /* the same shapes with the ray order (keys + sort + query); < 0: not offered */
 } rq_plan_info_t;
 rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, int32_t rebuild,
                            const rq_ray_t* rays, const uint32_t* ray_offsets, int32_t any, void* out,

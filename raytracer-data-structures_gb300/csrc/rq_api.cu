@@ -905,6 +905,21 @@ static rq_status_t batch_tables(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t
   return RQ_SUCCESS;
 }
 
+// The per-scene ray order of a many-structure query: keys, a stable sort,
+// and t.perm pointing at the permutation.
+static BuildResult enqueue_batch_order(BatchedTrace& t, DevBuf& keys, DevBuf& vals, BuildScratch& sc, uint32_t* err,
+                                       cudaStream_t st) {
+  const int bits = batch_key_bits(t.n_views);
+  if (bits > 32) return BuildResult::error(RQ_ERROR_UNSUPPORTED, "ray order: more than 2^17 structures");
+  cudaError_t e = keys.ensure((size_t)t.n * 4);
+  if (e == cudaSuccess) e = vals.ensure((size_t)t.n * 4);
+  if (e != cudaSuccess) return BuildResult::cuda_error(e, "ray order buffers");
+  launch_batch_ray_keys(t, keys.as<uint32_t>(), vals.as<uint32_t>(), st);
+  BuildResult r = sort_pairs(keys.as<uint32_t>(), vals.as<uint32_t>(), t.n, (bits + 7) / 8, true, sc, err, st);
+  t.perm = vals.as<const uint32_t>();
+  return r;
+}
+
 rq_status_t rq_trace_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, const rq_ray_t* rays,
                              const uint32_t* ray_offsets, int32_t any, void* out, uint32_t flags) {
   RQ_TRY(bind(ctx));
@@ -924,6 +939,11 @@ rq_status_t rq_trace_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_
   t.rays = d_rays;
   t.hits = any ? nullptr : static_cast<float4*>(d_out);
   t.occ = any ? static_cast<uint32_t*>(d_out) : nullptr;
+  if (ctx->settings.ray_sort != RQ_RAY_SORT_NONE && batch_key_bits(t.n_views) <= 32) {
+    BuildResult br = enqueue_batch_order(t, ctx->scratch.keys, ctx->scratch.vals, ctx->scratch, ctx->d_err, ctx->stream);
+    if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+    if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
+  }
   RQ_TRY_CUDA(ctx, launch_trace_batched(t, 128, 1, ctx->stream));
   if (dev) return RQ_SUCCESS;
   RQ_TRY_CUDA(ctx, cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
@@ -962,7 +982,18 @@ rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_ac
     RQ_TRY(rq_accel_rebuild_batched(ctx, accels, n_accels));
     RQ_TRY(collect_device_errors(ctx));
   }
-  // Autotuning: time every launch shape on these rays; a shape whose stack
+  // The per-scene ray order, once outside the capture (sizes its buffers
+  // and sort scratch), when the keys fit 32 bits.
+  const bool can_order = p->trace.n > 0 && batch_key_bits(p->trace.n_views) <= 32;
+  if (can_order) {
+    BatchedTrace t = p->trace;
+    BuildResult br = enqueue_batch_order(t, p->order_keys, p->order_vals, p->order_scratch, ctx->d_err, ctx->stream);
+    if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
+    if (br.status != RQ_SUCCESS) return fail(ctx, br.status, br.what);
+    RQ_TRY(collect_device_errors(ctx));
+  }
+  // Autotuning: time every launch shape on these rays, without and with the
+  // ray order (whose time includes its keys and sort); a shape whose stack
   // overflows on these trees is dropped.
   const int shapes[4][2] = {{128, 0}, {128, 1}, {256, 0}, {256, 1}};
   float best = -1.f;
@@ -970,36 +1001,45 @@ rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_ac
     cudaEvent_t e0, e1;
     RQ_TRY_CUDA(ctx, cudaEventCreate(&e0));
     RQ_TRY_CUDA(ctx, cudaEventCreate(&e1));
-    for (int k = 0; k < 4; ++k) {
-      float ms = 1e30f;
-      cudaError_t ce = cudaSuccess;
-      for (int rep = 0; rep < 3 && ce == cudaSuccess; ++rep) {
-        ce = cudaEventRecord(e0, ctx->stream);
-        if (ce == cudaSuccess) ce = launch_trace_batched(p->trace, shapes[k][0], shapes[k][1], ctx->stream);
-        if (ce == cudaSuccess) ce = cudaEventRecord(e1, ctx->stream);
-        if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
-        float t = 0.f;
-        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
-        if (ce == cudaSuccess && rep > 0) ms = std::min(ms, t);
-      }
-      uint32_t derr = 0;
-      if (ce == cudaSuccess) ce = take_device_errors(ctx, &derr);
-      if (ce != cudaSuccess) {
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        return cuda_fail(ctx, ce, "plan autotuning");
-      }
-      if (derr & ~kErrStackOverflow) {
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed structure or input seen while autotuning");
-      }
-      if (derr & kErrStackOverflow) continue;
-      p->shape_ms[k] = ms;
-      if (best < 0.f || ms < best) {
-        best = ms;
-        p->block = shapes[k][0];
-        p->deep = shapes[k][1];
+    for (int v = 0; v < (can_order ? 2 : 1); ++v) {
+      for (int k = 0; k < 4; ++k) {
+        float ms = 1e30f;
+        cudaError_t ce = cudaSuccess;
+        for (int rep = 0; rep < 3 && ce == cudaSuccess; ++rep) {
+          BatchedTrace t = p->trace;
+          ce = cudaEventRecord(e0, ctx->stream);
+          if (ce == cudaSuccess && v == 1) {
+            BuildResult br = enqueue_batch_order(t, p->order_keys, p->order_vals, p->order_scratch, ctx->d_err,
+                                                 ctx->stream);
+            if (!br.ok()) ce = br.cuda != cudaSuccess ? br.cuda : cudaErrorInvalidValue;
+          }
+          if (ce == cudaSuccess) ce = launch_trace_batched(t, shapes[k][0], shapes[k][1], ctx->stream);
+          if (ce == cudaSuccess) ce = cudaEventRecord(e1, ctx->stream);
+          if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+          float tm = 0.f;
+          if (ce == cudaSuccess) ce = cudaEventElapsedTime(&tm, e0, e1);
+          if (ce == cudaSuccess && rep > 0) ms = std::min(ms, tm);
+        }
+        uint32_t derr = 0;
+        if (ce == cudaSuccess) ce = take_device_errors(ctx, &derr);
+        if (ce != cudaSuccess) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return cuda_fail(ctx, ce, "plan autotuning");
+        }
+        if (derr & ~kErrStackOverflow) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed structure or input seen while autotuning");
+        }
+        if (derr & kErrStackOverflow) continue;
+        (v ? p->ordered_ms : p->shape_ms)[k] = ms;
+        if (best < 0.f || ms < best) {
+          best = ms;
+          p->block = shapes[k][0];
+          p->deep = shapes[k][1];
+          p->ordered = v == 1;
+        }
       }
     }
     cudaEventDestroy(e0);
@@ -1017,7 +1057,10 @@ rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_ac
     for (uint32_t k = 0; br.ok() && k < n_accels; ++k)
       if (accels[k]->buf.node_width == 4) br = collapse_bvh4(accels[k]->buf, ctx->scratch, ctx->d_err, cap);
   }
-  if (ce == cudaSuccess && br.ok()) ce = launch_trace_batched(p->trace, p->block, p->deep, cap);
+  BatchedTrace qt = p->trace;
+  if (ce == cudaSuccess && br.ok() && p->ordered)
+    br = enqueue_batch_order(qt, p->order_keys, p->order_vals, p->order_scratch, ctx->d_err, cap);
+  if (ce == cudaSuccess && br.ok()) ce = launch_trace_batched(qt, p->block, p->deep, cap);
   cudaError_t end = cudaStreamEndCapture(cap, &p->graph);
   p->kernels = launch_total() - k0;
   cudaStreamDestroy(cap);
@@ -1051,6 +1094,8 @@ rq_status_t rq_plan_get_info(rq_plan_t p, rq_plan_info_t* info) {
   info->n_rays = p->trace.n;
   info->rebuilds = p->store ? 1 : 0;
   for (int k = 0; k < 4; ++k) info->shape_ms[k] = p->shape_ms[k];
+  info->ray_order = p->ordered ? 1u : 0u;
+  for (int k = 0; k < 4; ++k) info->ordered_ms[k] = p->ordered_ms[k];
   return RQ_SUCCESS;
 }
 
@@ -1061,6 +1106,9 @@ rq_status_t rq_plan_destroy(rq_plan_t p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   p->table.release();
+  p->order_keys.release();
+  p->order_vals.release();
+  p->order_scratch.release();
   delete p;
   return RQ_SUCCESS;
 }

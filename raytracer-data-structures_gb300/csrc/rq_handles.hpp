@@ -89,7 +89,11 @@ struct rq_plan {
   BatchedTrace trace;
   DevBuf table;
   int block = 128, deep = 1;
+  bool ordered = false;                   // the query runs through a per-scene ray order
   float shape_ms[4] = {-1.f, -1.f, -1.f, -1.f};
+  float ordered_ms[4] = {-1.f, -1.f, -1.f, -1.f};
+  DevBuf order_keys, order_vals;          // ray order keys and the permutation
+  BuildScratch order_scratch;             // its sort's scratch (sized before the capture)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   uint64_t kernels = 0;

@@ -196,10 +196,16 @@ struct BatchedTrace {
   uint32_t* occ = nullptr;
   uint32_t* work = nullptr;
   uint32_t* err = nullptr;
+  const uint32_t* perm = nullptr;  // optional ray order: work index -> ray index
 };
 // block: 128 or 256 threads; deep: the deeper of the two stack sizes.
 cudaError_t launch_trace_batched(const BatchedTrace& t, int block, int deep, cudaStream_t s);
 int batched_stack_entries(int width, int deep);
+// Per-scene ray order: keys (scene << 15 | octant | 12-bit origin cell) and
+// vals = ray index for every ray; batch_key_bits = bits the keys use (more
+// than 32 when there are over 2^17 structures: no ray order then).
+int batch_key_bits(uint32_t n_views);
+void launch_batch_ray_keys(const BatchedTrace& t, uint32_t* keys, uint32_t* vals, cudaStream_t s);
 
 struct KdView {
   const int4* nodes;      // {word0, word1, word2, 0}

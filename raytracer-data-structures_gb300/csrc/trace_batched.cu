@@ -23,7 +23,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restr
                                                          const uint32_t* __restrict__ roff, uint32_t n_views,
                                                          const float4* __restrict__ rays, uint32_t n,
                                                          float4* __restrict__ hits, uint32_t* __restrict__ occ,
-                                                         uint32_t* __restrict__ work, uint32_t* err) {
+                                                         uint32_t* __restrict__ work, uint32_t* err,
+                                                         const uint32_t* __restrict__ perm) {
   const uint32_t lane = threadIdx.x & 31;
   for (;;) {
     uint32_t base = 0;
@@ -32,9 +33,10 @@ __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restr
     if (base >= n) return;  // the whole warp leaves together
 #pragma unroll 1
     for (uint32_t sub = 0; sub < kGrab; sub += 32) {
-      const uint32_t r = base + sub + lane;
+      const uint32_t w = base + sub + lane;  // work index; the ray itself through perm
+      const uint32_t r = (perm && w < n) ? __ldg(perm + w) : w;
       bool occluded = false;
-      if (r < n) {
+      if (w < n) {
         const Bvh2View v = views[segment_of(roff, n_views, r)];
         const Ray ray = load_ray(rays, r);
         Closest c = {ray.tmax, kMiss, 0.f, 0.f};
@@ -48,8 +50,12 @@ __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restr
         if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
       }
       if (ANY) {
-        const uint32_t bits = __ballot_sync(0xffffffffu, occluded);
-        if (lane == 0 && base + sub < n) occ[(base + sub) >> 5] = bits;
+        if (perm) {  // bits of scattered rays: set one by one in the zeroed words
+          if (occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+        } else {
+          const uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+          if (lane == 0 && base + sub < n) occ[(base + sub) >> 5] = bits;
+        }
       }
     }
   }
@@ -71,9 +77,44 @@ cudaError_t launch_shape(const BatchedTrace& t, cudaStream_t s) {
   if (blocks > enough) blocks = enough;
   if (blocks < 1) blocks = 1;
   if ((e = cudaMemsetAsync(t.work, 0, 4, s)) != cudaSuccess) return e;
+  if (ANY && t.perm && (e = cudaMemsetAsync(t.occ, 0, (size_t)((t.n + 31) / 32) * 4, s)) != cudaSuccess) return e;
   count_launch();
-  k<<<(unsigned)blocks, BLOCK, 0, s>>>(t.views, t.roff, t.n_views, t.rays, t.n, t.hits, t.occ, t.work, t.err);
+  k<<<(unsigned)blocks, BLOCK, 0, s>>>(t.views, t.roff, t.n_views, t.rays, t.n, t.hits, t.occ, t.work, t.err,
+                                       t.perm);
   return cudaGetLastError();
+}
+
+// Per-scene ray order keys: (scene << 15) | octant of the direction (3
+// bits) | 12-bit Morton code of the origin, quantised to 16 cells per axis in
+// the scene's root box.  Sorted stably, rays stay grouped by scene and, within
+// a scene, by direction octant and origin cell (the original order within a
+// cell).
+__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
+  v &= 15u;
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+
+__global__ void __launch_bounds__(256) k_batch_ray_keys(const Bvh2View* __restrict__ views,
+                                                        const uint32_t* __restrict__ roff, uint32_t n_views,
+                                                        const float4* __restrict__ rays, uint32_t n,
+                                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t sc = segment_of(roff, n_views, i);
+  const float* root = views[sc].root;
+  const float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+  const float o[3] = {a.x, a.y, a.z};
+  uint32_t q[3];
+  for (int k = 0; k < 3; ++k) {
+    const float lo = __ldg(root + k), ext = __ldg(root + 3 + k) - lo;
+    float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
+    u = fminf(fmaxf(u * 16.f, 0.f), 15.f);
+    q[k] = (uint32_t)u;
+  }
+  const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
+  const uint32_t morton = (spread4(q[0]) << 2) | (spread4(q[1]) << 1) | spread4(q[2]);
+  keys[i] = (sc << 15) | (oct << 12) | morton;
+  vals[i] = i;
 }
 
 template <int KIND, bool ANY, int W>
@@ -93,6 +134,18 @@ cudaError_t dispatch_width(const BatchedTrace& t, int block, int deep, cudaStrea
 }  // namespace
 
 int batched_stack_entries(int width, int deep) { return width == 4 ? (deep ? 96 : 48) : (deep ? 64 : 32); }
+
+int batch_key_bits(uint32_t n_views) {
+  int b = 0;
+  while (b < 32 && ((uint64_t)1 << b) < n_views) ++b;
+  return 15 + b;
+}
+
+void launch_batch_ray_keys(const BatchedTrace& t, uint32_t* keys, uint32_t* vals, cudaStream_t s) {
+  if (t.n == 0) return;
+  count_launch();
+  k_batch_ray_keys<<<(t.n + 255) / 256, 256, 0, s>>>(t.views, t.roff, t.n_views, t.rays, t.n, keys, vals);
+}
 
 cudaError_t launch_trace_batched(const BatchedTrace& t, int block, int deep, cudaStream_t s) {
   if (t.n == 0) return cudaSuccess;

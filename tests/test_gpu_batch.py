@@ -93,15 +93,21 @@ def test_batched_rebuild_after_updates(engine):
 
 
 @pytest.mark.parametrize("width", [2, 4])
-def test_batched_query_equals_single_queries(engine, rqm, width):
+@pytest.mark.parametrize("ray_order", [0, 1])
+def test_batched_query_equals_single_queries(engine, rqm, width, ray_order):
+    """Hits and occlusion bits of the many-structure query equal the
+    one-structure queries, with and without the per-scene ray order
+    (settings.ray_sort)."""
     engine.configure(node_width=rqm.NODE_WIDTH_4 if width == 4 else rqm.NODE_WIDTH_2)
     meshes = _meshes(seed=80)
     sc = [engine.scene_triangles(v, f) for v, f in meshes]
     accs = engine.build_batched(sc, "LBVH")
     accs[2] = engine.build(sc[2], "BVH")  # structures need not come from one batch
     rays, offs = _rays_for(meshes, seed=81)
+    engine.configure(ray_sort=ray_order)
     hits = engine.trace_batched(accs, rays, offs)
     bits = engine.trace_batched(accs, rays, offs, any_hit=True)
+    engine.configure(ray_sort=rqm.RAY_SORT_NONE)
     occ = rqm.unpack_bits(bits, len(rays))
     for k, acc in enumerate(accs):
         a, b = offs[k], offs[k + 1]
@@ -126,9 +132,10 @@ def test_plan_replays_rebuild_and_query(engine, rqm):
     info = plan.info()
     assert info.block_threads in (128, 256) and info.n_rays == n and info.rebuilds == 1
     assert info.graph_kernels >= 8  # the batched build's stages + the query
-    assert max(info.shape_ms) > 0
+    assert max(info.shape_ms) > 0 and max(info.ordered_ms) > 0  # both variants timed
     k = [128, 128, 256, 256].index(info.block_threads) + (1 if info.stack_entries == 64 else 0)
-    assert info.shape_ms[k] == min(t for t in info.shape_ms if t >= 0)
+    chosen = (info.ordered_ms if info.ray_order else info.shape_ms)[k]
+    assert chosen == min(t for t in list(info.shape_ms) + list(info.ordered_ms) if t >= 0)
     # move every mesh, then one replay rebuilds and traces
     for k2, (v, f) in enumerate(meshes):
         sc[k2].update((v + np.float32(0.25 * k2)).astype(np.float32))
