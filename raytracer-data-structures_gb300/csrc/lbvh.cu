@@ -4,8 +4,11 @@
 // findSplit (accelerators.h:397-449) is discarded and no refit exists; this
 // file implements the cited method: Karras 2012, "Maximizing Parallelism in
 // the Construction of BVHs, Octrees, and k-d Trees", one thread per internal
-// node, then one thread per leaf climbing to the root, the second thread to
-// reach a node computing its box.
+// node, then a bottom-up refit in which the second of a node's two children
+// to finish computes the node's box.  The refit runs by treelets (maximal
+// subtrees of at most kTreeletSpan leaves, one block each, in shared memory)
+// and then the top nodes above them (one block), so no level of the climb
+// waits on device-scope memory unless the top nodes exceed that block.
 //
 // BVH2 node (64 B, 4 x float4):
 //   [0] left  child box (lo.x, hi.x, lo.y, hi.y)
