@@ -233,7 +233,8 @@ def run_ours(args):
     # walk binary nodes only.
     sort_names = {rq.RAY_SORT_NONE: "none", rq.RAY_SORT_OCTANT_MORTON: "octant_morton",
                   rq.RAY_SORT_ORIGIN_DIRECTION: "origin_direction", rq.RAY_SORT_DIRECTION_ORIGIN: "direction_origin",
-                  rq.RAY_SORT_OCTANT_MORTON12: "octant_morton12"}
+                  rq.RAY_SORT_OCTANT_MORTON12: "octant_morton12", rq.RAY_SORT_OCTANT: "octant",
+                  rq.RAY_SORT_OCTANT_MORTON3: "octant_morton3"}
     sched_names = {rq.SCHEDULING_THREAD_PER_RAY: "thread_per_ray", rq.SCHEDULING_LANE_REFILL: "lane_refill",
                    rq.SCHEDULING_SPECULATIVE: "speculative", rq.SCHEDULING_WARP_PACKET: "warp_packet"}
     morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
@@ -252,7 +253,7 @@ def run_ours(args):
             for name in ("primary", "secondary", "shadow"):
                 opts = {}
                 if args.no_tune:
-                    fixed = rq.RAY_SORT_OCTANT_MORTON12 if name == "secondary" else rq.RAY_SORT_NONE
+                    fixed = rq.RAY_SORT_OCTANT if name == "secondary" else rq.RAY_SORT_NONE
                     pairs = [(fixed, rq.SCHEDULING_THREAD_PER_RAY)]
                 else:
                     pairs = [(srt, sch) for srt in sort_names for sch in scheds]
@@ -956,7 +957,7 @@ def main():
     ap.add_argument("--scheduling", type=int, default=0, help="--case: settings.scheduling (0-3)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner and use its GB300 choice (binary nodes, cube Morton codes, "
-                         "15-bit ray order for secondary rays): profiling the measured kernel mix")
+                         "octant ray order for secondary rays): profiling the measured kernel mix")
     args = ap.parse_args()
     if args.case:
         run_case(args)

@@ -111,7 +111,9 @@ typedef enum rq_ray_sort_t {
   RQ_RAY_SORT_OCTANT_MORTON = 1,    /* direction octant, then 27-bit Morton code of the origin */
   RQ_RAY_SORT_ORIGIN_DIRECTION = 2, /* octant, 15-bit origin Morton code, 12-bit direction (|dx|, |dy|) */
   RQ_RAY_SORT_DIRECTION_ORIGIN = 3, /* octant, 12-bit direction, 15-bit origin Morton code */
-  RQ_RAY_SORT_OCTANT_MORTON12 = 4   /* octant, 12-bit origin Morton code: a 15-bit key, half the sort passes */
+  RQ_RAY_SORT_OCTANT_MORTON12 = 4,  /* octant, 12-bit origin Morton code: a 15-bit key, half the sort passes */
+  RQ_RAY_SORT_OCTANT = 5,           /* direction octant only: a 3-bit key, one sort pass */
+  RQ_RAY_SORT_OCTANT_MORTON3 = 6    /* octant, 3-bit origin Morton code (2x2x2 cells): one sort pass */
 } rq_ray_sort_t;
 
 /* How rays meet boxes and primitives. */

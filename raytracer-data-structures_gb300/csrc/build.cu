@@ -199,7 +199,8 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
     uint32_t* keys = sc.keys.as<uint32_t>();
     uint32_t* p = sc.vals.as<uint32_t>();
     launch_ray_keys(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, keys, p, st);
-    const int passes = cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON12 ? 2 : 4;
+    const int passes = cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON12 ? 2
+                       : (cfg.ray_sort == RQ_RAY_SORT_OCTANT || cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON3) ? 1 : 4;
     BuildResult r = sort_pairs(keys, p, q.n, passes, true, sc, err, st);
     if (!r.ok()) return r;
     perm = p;

@@ -723,6 +723,8 @@ void launch_candidates(const Bvh2View& v, const float4* rays, uint32_t n, uint32
 //   RQ_RAY_SORT_ORIGIN_DIRECTION octant | 15-bit origin Morton | 12-bit direction
 //   RQ_RAY_SORT_DIRECTION_ORIGIN octant | 12-bit direction | 15-bit origin Morton
 //   RQ_RAY_SORT_OCTANT_MORTON12  octant | 12-bit origin Morton (15 bits: a 2-pass sort)
+//   RQ_RAY_SORT_OCTANT_MORTON3   octant | 3-bit origin Morton (6 bits: one pass)
+//   RQ_RAY_SORT_OCTANT           octant (3 bits: one pass)
 // The origin is quantised in the root box; the direction by |dx|, |dy| of the
 // unit direction, 6 bits each (|dz| follows within the octant).
 __device__ __forceinline__ uint32_t spread_bits(uint32_t v) {  // 10 bits -> every third bit
@@ -740,7 +742,8 @@ __global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ ray
   if (i >= n) return;
   float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
   const float o[3] = {a.x, a.y, a.z};
-  const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4 : 5;
+  const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4
+                    : mode == RQ_RAY_SORT_OCTANT_MORTON3 ? 1 : mode == RQ_RAY_SORT_OCTANT ? 0 : 5;
   const float cells = (float)(1u << obits);
   uint32_t q[3];
   for (int k = 0; k < 3; ++k) {
@@ -756,6 +759,10 @@ __global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ ray
     key = (oct << 27) | morton;
   } else if (mode == RQ_RAY_SORT_OCTANT_MORTON12) {
     key = (oct << 12) | morton;
+  } else if (mode == RQ_RAY_SORT_OCTANT_MORTON3) {
+    key = (oct << 3) | morton;
+  } else if (mode == RQ_RAY_SORT_OCTANT) {
+    key = oct;
   } else {
     const float len = sqrtf(b.x * b.x + b.y * b.y + b.z * b.z);
     const float inv = len > 0.f ? 1.0f / len : 0.f;

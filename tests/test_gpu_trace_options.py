@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])
-@pytest.mark.parametrize("key", ["OCTANT_MORTON", "ORIGIN_DIRECTION", "DIRECTION_ORIGIN", "OCTANT_MORTON12"])
+@pytest.mark.parametrize("key", ["OCTANT_MORTON", "ORIGIN_DIRECTION", "DIRECTION_ORIGIN", "OCTANT_MORTON12", "OCTANT",
+                                 "OCTANT_MORTON3"])
 def test_ray_sort_is_result_neutral(engine, oracle, rqm, acc_name, key):
     v, f = scenes.heightfield(301, 150, seed=12)
     s = engine.scene_triangles(v, f)
