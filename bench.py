@@ -384,6 +384,7 @@ def run_ours(args):
     render = None
     if not args.skip_render:
         render = run_render_legs(eng, stream, dev, args)
+        render["reference_scene"] = run_reference_scene_leg()
 
     batched = None
     if not args.skip_batch:
@@ -431,6 +432,43 @@ def run_ours(args):
     eng.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_reference_scene_leg(reps=5):
+    """The reference program's own workload: its default bunny scene (35,948
+    spheres from createScene_new, taken from the golden fixture) rendered at
+    640x480, 1 sample, with render()'s camera and jitter and castRay's shading
+    (rq_render_reference), for each builder of the dataStructure switch.  A
+    fresh context with the reference's default settings; host output buffers;
+    wall time per call, as a caller of the reference's render() sees it."""
+    import rq
+    sph = np.load(os.path.join(ROOT, "tests", "golden", "bunny.npz"))["spheres"]
+    colors = np.tile(np.array([0.8, 0.7, 0.0], np.float32), (len(sph), 1))  # main.cpp:689
+    colors[-1] = 0.0  # the ground sphere (main.cpp:703)
+    eng = rq.Engine(0)
+    s = eng.settings
+    out = {"spheres": int(len(sph)), "image": f"{s.width}x{s.height}x{s.aa_samples}",
+           "rays": int(s.width * s.height * s.aa_samples)}
+    scene = eng.scene_spheres(sph)
+    for name in ("BVH", "LBVH", "KDTREE"):
+        builds = []
+        for _ in range(3):
+            eng.synchronize()
+            t0 = time.perf_counter()
+            acc = eng.build(scene, name)
+            eng.synchronize()
+            builds.append(time.perf_counter() - t0)
+        for _ in range(2):
+            eng.render_reference(acc, surface_rgb=colors)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            eng.render_reference(acc, surface_rgb=colors)
+        render_s = (time.perf_counter() - t0) / reps
+        out[name] = {"build_ms": round(1e3 * min(builds[1:]), 3), "render_ms": round(1e3 * render_s, 3),
+                     "rays_per_s": round(out["rays"] / render_s, 0)}
+        acc.close()
+    eng.close()
+    return out
 
 
 def run_render_legs(eng, stream, dev, args):

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads) k_shade(const float4* __restrict__ s
 
 cudaError_t render_reference(int type, const SceneView& s, const AccelBuffers& a,
                              const rq_settings_t& cfg, float angle, float aspect,
-                             const double* jitter_host, const float* surface_rgb_host,
+                             const double* jitter, bool jitter_on_device, const float* surface_rgb_host,
                              DevBuf& stage_a, DevBuf& stage_b, DevBuf& stage_c,
                              uint8_t* pixels_host, float* rgb_sum_host, uint32_t* err,
                              cudaStream_t st) {
@@ -139,7 +139,9 @@ cudaError_t render_reference(int type, const SceneView& s, const AccelBuffers& a
   uint8_t* pix = reinterpret_cast<uint8_t*>(cbase + surf_bytes);
   float* sums = reinterpret_cast<float*>(cbase + ((surf_bytes + npix * 3 + 15) & ~size_t(15)));
   // jitter shares stage_b with the query results: rays are generated first
-  if ((e = cudaMemcpyAsync(stage_b.p, jitter_host, jit_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(stage_b.p, jitter, jit_bytes,
+                           jitter_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
   if ((e = cudaMemcpyAsync(surf, surface_rgb_host, surf_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
   float invW = 1 / float(cfg.width), invH = 1 / float(cfg.height);
   count_launch(2);  // camera rays + shading

@@ -162,6 +162,7 @@ rq_status_t rq_destroy(rq_ctx_t ctx) {
   ctx->stage_in.release();
   ctx->stage_out.release();
   ctx->stage_aux.release();
+  ctx->ref_jitter.release();
   ctx->scratch.release();
   ctx->render.release();
   ctx->pipe.release();
@@ -1210,21 +1211,30 @@ rq_status_t rq_render_reference(rq_ctx_t ctx, rq_accel_t a, const rq_settings_t*
   const uint64_t nray = npix * s.aa_samples;
   if (nray > (1ull << 31)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "image too large");
   // Jitter: the caller's, or the reference's default-seeded mt19937 draws
-  // (random_double, main.cpp:503-508) in render()'s call order.
-  std::vector<double> own;
+  // (random_double, main.cpp:503-508) in render()'s call order.  The
+  // default sequence depends only on the sample count: drawn once on the
+  // host and kept on the device for later calls.
+  bool jitter_on_device = false;
   if (!jitter) {
-    own.resize(2 * nray);
-    std::mt19937 gen;
-    std::uniform_real_distribution<double> dist(0.0, 1.0);
-    for (auto& v : own) v = dist(gen);
-    jitter = own.data();
+    if (ctx->ref_jitter_n != nray || !ctx->ref_jitter.p) {
+      std::vector<double> own(2 * nray);
+      std::mt19937 gen;
+      std::uniform_real_distribution<double> dist(0.0, 1.0);
+      for (auto& v : own) v = dist(gen);
+      ctx->ref_jitter_n = 0;
+      RQ_TRY_CUDA(ctx, ctx->ref_jitter.ensure(own.size() * 8));
+      RQ_TRY_CUDA(ctx, cudaMemcpy(ctx->ref_jitter.p, own.data(), own.size() * 8, cudaMemcpyHostToDevice));
+      ctx->ref_jitter_n = nray;
+    }
+    jitter = ctx->ref_jitter.as<const double>();
+    jitter_on_device = true;
   }
   // render() camera constants (main.cpp:544-546), computed on the host with
   // the same double-precision tan the reference calls.
   float fov = 30, aspect = s.width / float(s.height);
   float angle = (float)std::tan(3.141592653589793 * 0.5 * fov / 180.);
   cudaError_t e = render_reference(a->type, scene_view(a->scene), a->buf, s, angle, aspect, jitter,
-                                   surface_rgb, ctx->stage_in, ctx->stage_out, ctx->stage_aux,
+                                   jitter_on_device, surface_rgb, ctx->stage_in, ctx->stage_out, ctx->stage_aux,
                                    pixels, rgb_sum, ctx->d_err, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
   return collect_device_errors(ctx);

@@ -172,7 +172,7 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
                         cudaStream_t st, rq_status_t* status);
 cudaError_t render_reference(int type, const SceneView& s, const AccelBuffers& a,
                              const rq_settings_t& settings, float angle, float aspect,
-                             const double* jitter_host, const float* surface_rgb_host,
+                             const double* jitter, bool jitter_on_device, const float* surface_rgb_host,
                              DevBuf& stage_a, DevBuf& stage_b, DevBuf& stage_c,
                              uint8_t* pixels_host, float* rgb_sum_host, uint32_t* err,
                              cudaStream_t st);

@@ -80,6 +80,8 @@ struct rq_context {
   RenderScratch render;
   HostPipe pipe;
   DevBuf batch_table;  // views + ray offsets + work counter of rq_trace_batched
+  DevBuf ref_jitter;   // the reference render's default-seeded jitter, generated once per sample count
+  uint64_t ref_jitter_n = 0;
 };
 
 struct rq_plan {

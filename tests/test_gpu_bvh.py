@@ -86,6 +86,13 @@ def test_render_bvh_reproduces_golden_image(engine, rqm, oracle):
     diff = np.abs(pixels.astype(int) - gold.astype(int))
     assert diff.max() <= 1, (diff.max(), int((diff > 1).sum()))
     assert (diff == 0).mean() > 0.999
+    # later calls reuse the context's copy of the default jitter sequence
+    again, rgb2 = engine.render_reference(acc, rqm.default_settings(), None, sphere_surface_colors(len(sph)))
+    assert np.array_equal(again, pixels) and np.array_equal(rgb2.view(np.uint32), rgb.view(np.uint32))
+    # as does a call with the jitter given explicitly
+    jit = oracle.jitter_mt19937(640 * 480 * 2)
+    given, _ = engine.render_reference(acc, rqm.default_settings(), jit, sphere_surface_colors(len(sph)))
+    assert np.array_equal(given, pixels)
 
 
 @pytest.mark.parametrize("acc_name", ["LBVH", "NONE"])
