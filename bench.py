@@ -487,7 +487,7 @@ def run_render_legs(eng, stream, dev, args):
     saved = eng.settings
     out = {}
 
-    def leg(verts, idx, structures, width, height, spp, view_kw, frames):
+    def leg(verts, idx, structures, width, height, spp, view_kw, frames, count_work=False):
         eng.configure(width=width, height=height, aa_samples=spp, ray_sort=rq.RAY_SORT_NONE,
                       scheduling=rq.SCHEDULING_THREAD_PER_RAY)
         dv = torch.from_numpy(verts).to(dev)
@@ -496,10 +496,17 @@ def run_render_legs(eng, stream, dev, args):
         view = rq.make_view(**view_kw)
         pix = torch.empty(width * height * 3, dtype=torch.uint8, device=dev)
         res = {"triangles": int(len(idx)), "image": f"{width}x{height}x{spp}", "bounces": view_kw["bounces"]}
+        cam = scenes.pinhole_rays(width, height, spp, eye=view_kw["eye"], target=view_kw["target"],
+                                  up=view_kw["up"], fov_deg=view_kw["fov_deg"], seed=SEED + 7) if count_work else None
         for name in structures:
             acc = eng.build(scene, name)
             _, _, cnt = eng.render(acc, view)  # synchronous: the ray counts
             rays = int(cnt.sum())
+            work = None
+            if cam is not None and name != "KDTREE":  # counters exist for BVH structures
+                _, wc = eng.trace_counters(acc, cam)
+                work = {"rays": "every camera ray of the view (seeded jitter)", "node_bytes": 64,
+                        "nodes_per_ray": round(int(wc[0]) / len(cam), 3), "tris_per_ray": round(int(wc[1]) / len(cam), 3)}
             for _ in range(2):
                 acc.rebuild()
                 eng.render(acc, view, pix)
@@ -520,12 +527,14 @@ def run_render_legs(eng, stream, dev, args):
             res[name] = {"frame_ms": round(t, 3), "render_ms": round(tr, 3), "build_ms": round(t - tr, 3),
                          "rays": rays, "ray_counts": [int(c) for c in cnt],
                          "grays_s": round(rays / (t * 1e-3) / 1e9, 4)}
+            if work:
+                res[name]["traversal_work"] = work
             acc.close()
         scene.close()
         return res
 
     v1, f1 = scenes.c1_mesh()
-    out["c1"] = leg(v1, f1, ("BVH", "KDTREE", "LBVH"), 640, 480, 1, scenes.C1_VIEW, 10)
+    out["c1"] = leg(v1, f1, ("BVH", "KDTREE", "LBVH"), 640, 480, 1, scenes.C1_VIEW, 10, count_work=True)
     if not args.small:
         v3, f3, _ = scenes.merged_icospheres()
         out["c3"] = leg(v3, f3, ("LBVH",), 3840, 2160, 4, scenes.C3_VIEW, 3)
@@ -633,6 +642,18 @@ def run_batch_leg(eng, stream, dev, args):
     eng.synchronize()
     same = bool(torch.equal(d_hits, ref_hits))
     batched_build_ms = timed(lambda: eng.rebuild_batched(accs), 4)
+    # Traversal work (node visits, triangle tests per ray) on a seeded 1% sample
+    # of every scene's rays, through the counting walk of the same structures.
+    work_rng = np.random.default_rng(SEED + 42)
+    ray_rows = d_rays.view(-1, 32)
+    visits = tests = sampled = 0
+    for k in range(n_sc):
+        a, b = int(offs[k]), int(offs[k + 1])
+        m = max(1, (b - a) // 100)
+        sel = np.sort(work_rng.choice(b - a, size=m, replace=False)) + a
+        sample = ray_rows[torch.from_numpy(sel).to(dev)].cpu().numpy().reshape(-1).view(rq.RAY_DTYPE)
+        _, cnt = eng.trace_counters(accs[k], sample)
+        visits, tests, sampled = visits + int(cnt[0]), tests + int(cnt[1]), sampled + m
     info = plan.info()
     plan.close()
     for a in accs:
@@ -651,7 +672,9 @@ def run_batch_leg(eng, stream, dev, args):
                                  "ray_order": bool(info.ray_order),
                                  "tuned_ms": [round(float(x), 3) for x in info.shape_ms],
                                  "tuned_ordered_ms": [round(float(x), 3) for x in info.ordered_ms]}},
-           "speedup": round(plain_ms / batched_ms, 3), "hits_identical": same}
+           "speedup": round(plain_ms / batched_ms, 3), "hits_identical": same,
+           "traversal_work": {"sample": f"{sampled} rays (1% of each scene's, seeded)", "node_bytes": 64,
+                              "nodes_per_ray": round(visits / sampled, 3), "tris_per_ray": round(tests / sampled, 3)}}
     log(f"[bench] batched: {out}")
     return out
 
