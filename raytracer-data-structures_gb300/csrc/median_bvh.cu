@@ -20,6 +20,7 @@
 // partition of all three lists by one prefix sum over their left flags.  The
 // leaves end up as position ranges of the x-sorted list, which becomes the
 // slot order.  Internal nodes are numbered breadth-first, left before right.
+#include <algorithm>
 #include <vector>
 
 #include "rq_build.hpp"
@@ -78,10 +79,11 @@ __global__ void __launch_bounds__(kThreads) k_prim_info(int kind, const float* _
 
 // Segment of every list position (-1 for positions already in a leaf).
 __global__ void __launch_bounds__(kThreads) k_seg_id(const uint32_t* __restrict__ start,
-                                                     const uint32_t* __restrict__ end, uint32_t S, uint32_t n,
-                                                     int32_t* __restrict__ seg_id) {
+                                                     const uint32_t* __restrict__ end, const uint32_t* S_dev,
+                                                     uint32_t n, int32_t* __restrict__ seg_id) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
+  const uint32_t S = *S_dev;
   uint32_t lo = 0, hi = S;  // first segment with start > p
   while (lo < hi) {
     uint32_t m = (lo + hi) >> 1;
@@ -98,13 +100,13 @@ template <int G>
 __global__ void __launch_bounds__(kThreads) k_seg_bounds(const uint32_t* __restrict__ list0,
                                                          const float* __restrict__ aabb,
                                                          const uint32_t* __restrict__ start,
-                                                         const uint32_t* __restrict__ end, uint32_t S,
+                                                         const uint32_t* __restrict__ end, const uint32_t* S_dev,
                                                          uint32_t slices, int32_t* __restrict__ box) {
   constexpr int kPer = 8;
   const uint32_t group = (blockIdx.x * kThreads + threadIdx.x) / G;
   const uint32_t t = threadIdx.x % G;
   const uint32_t seg = group / slices, slice = group % slices;
-  const bool live = seg < S;
+  const bool live = seg < *S_dev;
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   if (live) {
     const uint32_t s = __ldg(start + seg), e = __ldg(end + seg);
@@ -179,10 +181,15 @@ struct Segs {
 };
 
 // The split decision of one segment (constructBVHNew's rules).
-__global__ void __launch_bounds__(kThreads) k_seg_decide(Segs g, uint32_t S, const uint32_t* __restrict__ lists,
-                                                         uint32_t n, const float* __restrict__ cen) {
+__global__ void __launch_bounds__(kThreads) k_seg_decide(Segs g, const uint32_t* S_dev, uint32_t S_bound,
+                                                         const uint32_t* __restrict__ lists, uint32_t n,
+                                                         const float* __restrict__ cen) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= S) return;
+  if (k >= S_bound) return;
+  if (k >= *S_dev) {  // past this level's segments: no split (the scan runs over S_bound flags)
+    g.split[k] = 0;
+    return;
+  }
   const uint32_t s = g.start[k], e = g.end[k], m = e - s;
   uint32_t split = 0, mid = s, dim = 0;
   if (m > 1) {
@@ -222,9 +229,17 @@ __global__ void __launch_bounds__(kThreads) k_seg_decide(Segs g, uint32_t S, con
 
 // Write each segment into its parent (box, link, count) and emit the next
 // level's segments.
-__global__ void __launch_bounds__(kThreads) k_seg_link(Segs g, uint32_t S, uint32_t node_base, Segs next,
-                                                       float4* __restrict__ nodes, float* __restrict__ root) {
+// ctl[2 * level] = segments of the level, ctl[2 * level + 1] = the level's
+// first node index; thread 0 also writes the next level's pair.
+__global__ void __launch_bounds__(kThreads) k_seg_link(Segs g, uint32_t* ctl, int level, const uint32_t* splits,
+                                                       Segs next, float4* __restrict__ nodes,
+                                                       float* __restrict__ root) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t S = ctl[2 * level], node_base = ctl[2 * level + 1];
+  if (k == 0) {
+    ctl[2 * level + 2] = 2 * *splits;
+    ctl[2 * level + 3] = node_base + *splits;
+  }
   if (k >= S) return;
   const uint32_t s = g.start[k], e = g.end[k];
   float lo[3], hi[3];
@@ -304,9 +319,11 @@ __global__ void __launch_bounds__(kThreads) k_partition(Segs g, const int32_t* _
     if (e_ != cudaSuccess) return BuildResult::cuda_error(e_, what); \
   } while (0)
 
+// S: an upper bound of the level's segments (the kernels read the count);
+// max_size: an upper bound of their sizes.
 template <int G>
-void seg_bounds(const uint32_t* list0, const float* aabb, const Segs& g, uint32_t S, uint32_t max_size,
-                cudaStream_t st) {
+void seg_bounds(const uint32_t* list0, const float* aabb, const Segs& g, const uint32_t* S_dev, uint32_t S,
+                uint32_t max_size, cudaStream_t st) {
   const uint32_t per_slice = G * 8;
   const uint32_t slices = (max_size + per_slice - 1) / per_slice;
   if (slices > 1) {
@@ -316,15 +333,15 @@ void seg_bounds(const uint32_t* list0, const float* aabb, const Segs& g, uint32_
   const uint64_t groups = (uint64_t)S * slices;
   const uint64_t blocks = (groups * G + kThreads - 1) / kThreads;
   count_launch();
-  k_seg_bounds<G><<<(unsigned)blocks, kThreads, 0, st>>>(list0, aabb, g.start, g.end, S, slices, g.box);
+  k_seg_bounds<G><<<(unsigned)blocks, kThreads, 0, st>>>(list0, aabb, g.start, g.end, S_dev, slices, g.box);
 }
 
-void seg_bounds_dispatch(const uint32_t* list0, const float* aabb, const Segs& g, uint32_t S,
+void seg_bounds_dispatch(const uint32_t* list0, const float* aabb, const Segs& g, const uint32_t* S_dev, uint32_t S,
                          uint32_t max_size, cudaStream_t st) {
-  if (max_size <= 8) seg_bounds<1>(list0, aabb, g, S, max_size, st);
-  else if (max_size <= 32) seg_bounds<4>(list0, aabb, g, S, max_size, st);
-  else if (max_size <= 256) seg_bounds<32>(list0, aabb, g, S, max_size, st);
-  else seg_bounds<256>(list0, aabb, g, S, max_size, st);
+  if (max_size <= 8) seg_bounds<1>(list0, aabb, g, S_dev, S, max_size, st);
+  else if (max_size <= 32) seg_bounds<4>(list0, aabb, g, S_dev, S, max_size, st);
+  else if (max_size <= 256) seg_bounds<32>(list0, aabb, g, S_dev, S, max_size, st);
+  else seg_bounds<256>(list0, aabb, g, S_dev, S, max_size, st);
 }
 
 Segs segs_at(uint32_t* base, uint32_t cap) {
@@ -380,40 +397,50 @@ BuildResult build_median_bvh(const SceneView& s, AccelBuffers& a, BuildScratch& 
     BuildResult r = sort_pairs(keys + (size_t)ax * n, lists + (size_t)ax * n, n, 4, true, sc, err, st);
     if (!r.ok()) return r;
   }
-  // level 0: one segment, the root
-  const uint32_t h_root[3] = {0u, n, kRoot};
+  // Level 0: one segment, the root.  The host runs a fixed number of levels
+  // (median splits halve the largest segment, so after ceil(log2 n) + 1
+  // levels none can split) with upper bounds for the segment counts and
+  // sizes; the counts themselves and each level's first node index stay on
+  // the device (ctl), so the levels run without a host round trip.
+  MB_TRY(sc.m7.ensure(2 * 72 * 4), "BVH scratch");
+  uint32_t* ctl = sc.m7.as<uint32_t>();
+  const uint32_t h_root[3] = {0u, n, kRoot}, h_ctl[2] = {1u, 0u};
   MB_TRY(cudaMemcpyAsync(cur.start, &h_root[0], 4, cudaMemcpyHostToDevice, st), "BVH init");
   MB_TRY(cudaMemcpyAsync(cur.end, &h_root[1], 4, cudaMemcpyHostToDevice, st), "BVH init");
   MB_TRY(cudaMemcpyAsync(cur.parent, &h_root[2], 4, cudaMemcpyHostToDevice, st), "BVH init");
-  uint32_t S = 1, max_size = n, node_base = 0;
-  for (int level = 0; S > 0; ++level) {
+  MB_TRY(cudaMemcpyAsync(ctl, h_ctl, 8, cudaMemcpyHostToDevice, st), "BVH init");
+  uint32_t S = 1, max_size = n;  // upper bounds of this level's segments and their sizes
+  int level = 0;
+  for (;; ++level) {
     if (level > 64) return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "median BVH deeper than 64 levels");
+    const uint32_t* S_dev = ctl + 2 * level;
     count_launch(1);
-    k_seg_id<<<grid(n), kThreads, 0, st>>>(cur.start, cur.end, S, n, seg_id);
-    seg_bounds_dispatch(lists, aabb, cur, S, max_size, st);
+    k_seg_id<<<grid(n), kThreads, 0, st>>>(cur.start, cur.end, S_dev, n, seg_id);
+    seg_bounds_dispatch(lists, aabb, cur, S_dev, S, max_size, st);
     count_launch(1);
-    k_seg_decide<<<grid(S), kThreads, 0, st>>>(cur, S, lists, n, cen);
+    k_seg_decide<<<grid(S), kThreads, 0, st>>>(cur, S_dev, S, lists, n, cen);
     launch_scan_excl(cur.split, cur.rank, S, scan_tmp, total, st);
     count_launch(1);
-    k_seg_link<<<grid(S), kThreads, 0, st>>>(cur, S, node_base, nxt, a.nodes.as<float4>(), a.root.as<float>());
+    k_seg_link<<<grid(S), kThreads, 0, st>>>(cur, ctl, level, total, nxt, a.nodes.as<float4>(), a.root.as<float>());
     MB_TRY(cudaGetLastError(), "BVH level");
-    uint32_t splits = 0;
-    MB_TRY(cudaMemcpyAsync(&splits, total, 4, cudaMemcpyDeviceToHost, st), "BVH level");
-    MB_TRY(cudaStreamSynchronize(st), "BVH level");
-    if (splits) {
-      count_launch(3);
-      k_mark<<<grid(n), kThreads, 0, st>>>(cur, seg_id, lists, n, left);
-      k_left_flags<<<grid(3ull * n), kThreads, 0, st>>>(cur, seg_id, lists, n, left, keys);
-      launch_scan_excl(keys, scan, 3ull * n, scan_tmp, nullptr, st);
-      k_partition<<<grid(3ull * n), kThreads, 0, st>>>(cur, seg_id, lists, n, left, scan, lists_alt);
-      MB_TRY(cudaGetLastError(), "BVH partition");
-      uint32_t* t = lists; lists = lists_alt; lists_alt = t;
+    if (max_size <= 1) {  // no segment of this level can split: it was the last
+      ++level;
+      break;
     }
-    node_base += splits;
-    S = 2 * splits;
+    count_launch(3);
+    k_mark<<<grid(n), kThreads, 0, st>>>(cur, seg_id, lists, n, left);
+    k_left_flags<<<grid(3ull * n), kThreads, 0, st>>>(cur, seg_id, lists, n, left, keys);
+    launch_scan_excl(keys, scan, 3ull * n, scan_tmp, nullptr, st);
+    k_partition<<<grid(3ull * n), kThreads, 0, st>>>(cur, seg_id, lists, n, left, scan, lists_alt);
+    MB_TRY(cudaGetLastError(), "BVH partition");
+    uint32_t* t = lists; lists = lists_alt; lists_alt = t;
+    S = (uint32_t)std::min<uint64_t>(2ull * S, n);
     max_size = (max_size + 1) / 2;
     Segs tg = cur; cur = nxt; nxt = tg;
   }
+  uint32_t node_base = 0;
+  MB_TRY(cudaMemcpyAsync(&node_base, ctl + 2 * level + 1, 4, cudaMemcpyDeviceToHost, st), "BVH nodes");
+  MB_TRY(cudaStreamSynchronize(st), "BVH nodes");
   // slot order = the x-sorted list; gather the payload in that order
   MB_TRY(cudaMemcpyAsync(a.order.p, lists, (size_t)n * 4, cudaMemcpyDeviceToDevice, st), "BVH order");
   launch_prims_gather(s.kind, s.verts, s.idx, s.sph, a.order.as<uint32_t>(), n, a.prims.as<float4>(), st);
