@@ -76,6 +76,21 @@ def test_median_bvh_degenerate_inputs(engine, oracle, rqm):
         assert np.array_equal(h["t"], hn["t"])
 
 
+def test_median_bvh_degenerate_clusters_match_oracle(engine, oracle, rqm):
+    """Degenerate nodes (all centroids equal: one leaf for the whole range)
+    above and inside the subtrees that finish in one block, and a scene just
+    past the in-block span."""
+    rng = np.random.default_rng(40)
+    same = np.tile(np.array([[1.0, 2.0, 3.0, 0.5]], np.float32), (3000, 1))
+    cloud = np.concatenate([rng.random((5000, 3), dtype=np.float32) * 10, np.full((5000, 1), 0.05, np.float32)], 1)
+    cloud[1000:1600] = np.array([4.0, 4.0, 4.0, 0.05], np.float32)  # a 600-sphere cluster of one point
+    edge = np.concatenate([rng.random((513, 3), dtype=np.float32), np.full((513, 1), 0.01, np.float32)], 1)
+    for sph in (same, cloud, edge):
+        acc = engine.build(engine.scene_spheres(sph), rqm.BVH)
+        aabb, cen = oracle.sphere_prims(sph)
+        _compare_median(engine, oracle, rqm, acc, aabb, cen)
+
+
 def test_render_bvh_reproduces_golden_image(engine, rqm, oracle):
     b = golden("bunny")
     sph = b["spheres"]
