@@ -30,52 +30,78 @@ __global__ void k_batch_init_bounds(int32_t* lohi, uint32_t n_scenes) {
   lohi[i] = (i % 6) < 3 ? ordered_pos_inf() : ordered_neg_inf();
 }
 
-// Box of each scene's points (triangle vertices, or sphere centres).
+// Box of each scene's points (triangle vertices, or sphere centres).  Each
+// warp takes kBoundsGroups groups of 32 consecutive points and folds a
+// running box for the current scene, flushing it (one warp reduction, six
+// atomics) only when the scene changes and at the end; a group that
+// straddles two scenes uses per-lane atomics.  (One flush per 32 points put
+// about two million atomics on the 6 x n_scenes words.)
+constexpr int kBoundsGroups = 16;
+
 __global__ void __launch_bounds__(kThreads) k_batch_point_bounds(const BatchDesc* __restrict__ desc, int kind,
                                                                  const uint32_t* __restrict__ voff, uint32_t n_scenes,
                                                                  int32_t* lohi) {
   const uint32_t total = __ldg(voff + n_scenes);
-  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = v < total;
-  uint32_t s = 0;
-  float p[3] = {0.f, 0.f, 0.f};
-  if (active) {
-    s = segment_of(voff, n_scenes, v);
-    const uint32_t local = v - __ldg(voff + s);
-    if (kind == kTriangles) {
-      const float* q = desc[s].verts + 3 * (size_t)local;
-      p[0] = __ldg(q); p[1] = __ldg(q + 1); p[2] = __ldg(q + 2);
-    } else {
-      const float4 c = __ldg(desc[s].sph + local);
-      p[0] = c.x; p[1] = c.y; p[2] = c.z;
-    }
-  }
-  // One warp-wide reduction when the whole warp lies in one scene, else per-lane atomics.
-  const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
-  const bool uniform = __all_sync(0xffffffffu, !active || s == s0);
-  float lo[3], hi[3];
-  for (int k = 0; k < 3; ++k) {
-    lo[k] = active ? p[k] : INFINITY;
-    hi[k] = active ? p[k] : -INFINITY;
-  }
-  if (uniform) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t base = (uint64_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32u * kBoundsGroups);
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  uint32_t cur = ~0u;  // scene of the running box (warp-uniform)
+  auto flush = [&]() {
     for (int k = 0; k < 3; ++k)
       for (int o = 16; o > 0; o >>= 1) {
         lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
         hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
       }
-    if ((threadIdx.x & 31) == 0 && lo[0] <= hi[0]) {
+    if (lane == 0 && lo[0] <= hi[0])
       for (int k = 0; k < 3; ++k) {
-        atomicMin(&lohi[6 * s0 + k], float_to_ordered(lo[k]));
-        atomicMax(&lohi[6 * s0 + 3 + k], float_to_ordered(hi[k]));
+        atomicMin(&lohi[6 * cur + k], float_to_ordered(lo[k]));
+        atomicMax(&lohi[6 * cur + 3 + k], float_to_ordered(hi[k]));
+      }
+    for (int k = 0; k < 3; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; }
+  };
+  for (int g = 0; g < kBoundsGroups; ++g) {
+    const uint64_t first = base + (uint64_t)g * 32u;
+    if (first >= total) break;  // warp-uniform
+    const uint32_t v = (uint32_t)first + lane;
+    const bool active = (uint64_t)v < total;
+    // scene of the group's first point; the group is in one scene when its
+    // last active point lies before that scene's end
+    uint32_t s0 = 0, end0 = 0;
+    if (lane == 0) {
+      s0 = segment_of(voff, n_scenes, (uint32_t)first);
+      end0 = __ldg(voff + s0 + 1);
+    }
+    s0 = __shfl_sync(0xffffffffu, s0, 0);
+    end0 = __shfl_sync(0xffffffffu, end0, 0);
+    const uint64_t last = first + 31u < (uint64_t)total ? first + 31u : (uint64_t)total - 1u;
+    const bool uniform = last < (uint64_t)end0;
+    const uint32_t s = uniform ? s0 : (active ? segment_of(voff, n_scenes, v) : 0u);
+    float p[3] = {0.f, 0.f, 0.f};
+    if (active) {
+      const uint32_t local = v - __ldg(voff + s);
+      if (kind == kTriangles) {
+        const float* q = desc[s].verts + 3 * (size_t)local;
+        p[0] = __ldg(q); p[1] = __ldg(q + 1); p[2] = __ldg(q + 2);
+      } else {
+        const float4 c = __ldg(desc[s].sph + local);
+        p[0] = c.x; p[1] = c.y; p[2] = c.z;
       }
     }
-  } else if (active) {
-    for (int k = 0; k < 3; ++k) {
-      atomicMin(&lohi[6 * s + k], float_to_ordered(p[k]));
-      atomicMax(&lohi[6 * s + 3 + k], float_to_ordered(p[k]));
+    if (uniform) {
+      if (s0 != cur) {
+        if (cur != ~0u) flush();
+        cur = s0;
+      }
+      if (active)
+        for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], p[k]); hi[k] = fmaxf(hi[k], p[k]); }
+    } else if (active) {
+      for (int k = 0; k < 3; ++k) {
+        atomicMin(&lohi[6 * s + k], float_to_ordered(p[k]));
+        atomicMax(&lohi[6 * s + 3 + k], float_to_ordered(p[k]));
+      }
     }
   }
+  if (cur != ~0u) flush();
 }
 
 __global__ void __launch_bounds__(kThreads) k_batch_morton(const BatchDesc* __restrict__ desc, int kind, int mode,
@@ -137,19 +163,24 @@ __global__ void __launch_bounds__(kThreads) k_batch_karras(const uint32_t* __res
                                                            float4* __restrict__ nodes, uint32_t* __restrict__ parent) {
   const uint32_t total = __ldg(ioff + n_scenes);
   const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= total) return;
-  const uint32_t s = segment_of(ioff, n_scenes, gi);
-  const uint32_t p0 = __ldg(poff + s), i0 = __ldg(ioff + s);
-  const int64_t N = (int64_t)__ldg(poff + s + 1) - p0;
-  const int64_t i = (int64_t)gi - i0;
-  const uint32_t* c = codes + p0;
-  const uint32_t ki = __ldg(c + i);
-  const int dnext = karras_delta(c, N, i, i + 1, ki);
-  const int dprev = karras_delta(c, N, i, i - 1, ki);
-  const int2 ch = karras_children(c, N, i, ki, dprev, dnext);
+  const bool active = gi < total;  // every lane stays for the warp searches
+  uint32_t s = 0, p0 = 0, i0 = 0, ki = 0;
+  int N = 2, i = 0, dprev = -1, dnext = -1;
+  if (active) {
+    s = segment_of(ioff, n_scenes, gi);
+    p0 = __ldg(poff + s);
+    i0 = __ldg(ioff + s);
+    N = (int)(__ldg(poff + s + 1) - p0);
+    i = (int)(gi - i0);
+    ki = __ldg(codes + p0 + i);
+    dnext = delta32(codes + p0, N, i, i + 1, ki);
+    dprev = delta32(codes + p0, N, i, i - 1, ki);
+  }
+  const int4 ch = karras_node_warp(codes + p0, N, i, ki, dprev, dnext, active);
+  if (!active) return;
   float4* nd = nodes + 4 * (size_t)i0;
   uint32_t* par = parent + (2 * (size_t)p0 - s);
-  reinterpret_cast<int4*>(nd)[4 * i + 3] = make_int4(ch.x, ch.y, ch.x < 0 ? 1 : 0, ch.y < 0 ? 1 : 0);
+  reinterpret_cast<int4*>(nd)[4 * (size_t)i + 3] = make_int4(ch.x, ch.y, ch.x < 0 ? 1 : 0, ch.y < 0 ? 1 : 0);
   par[ch.x >= 0 ? ch.x : (N - 1 + ~ch.x)] = ((uint32_t)i << 1) | 0u;
   par[ch.y >= 0 ? ch.y : (N - 1 + ~ch.y)] = ((uint32_t)i << 1) | 1u;
 }
@@ -237,7 +268,8 @@ BuildResult build_batch(BatchStore& b, int morton_mode, uint32_t* err, cudaStrea
   int32_t* lohi = b.lohi.as<int32_t>();
   count_launch(2);
   k_batch_init_bounds<<<grid(6 * (uint64_t)n), kThreads, 0, st>>>(lohi, n);
-  k_batch_point_bounds<<<grid(vtotal), kThreads, 0, st>>>(desc, b.kind, V, n, lohi);
+  const uint64_t bound_warps = (vtotal + 32u * kBoundsGroups - 1) / (32u * kBoundsGroups);
+  k_batch_point_bounds<<<grid(bound_warps * 32), kThreads, 0, st>>>(desc, b.kind, V, n, lohi);
   count_launch();
   k_batch_morton<<<grid(total), kThreads, 0, st>>>(desc, b.kind, morton_mode, P, n, lohi, b.keys.as<uint64_t>(),
                                                    b.vals.as<uint32_t>());

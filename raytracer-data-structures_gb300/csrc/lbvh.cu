@@ -26,42 +26,6 @@ namespace {
 constexpr int kThreads = 256;
 static_assert(kRefitTopCap == kRefitTopCapHost, "top list capacity");
 
-// Karras 2012 prefix length between sorted codes i and j with the index
-// tiebreak; -1 outside the keys.  32-bit indices: scenes hold fewer than
-// 2^30 primitives.
-__device__ __forceinline__ int delta32(const uint32_t* __restrict__ k, int n, int i, int j, uint32_t ki) {
-  if (j < 0 || j >= n) return -1;
-  const uint32_t kj = __ldg(k + j);
-  return ki != kj ? __clz(ki ^ kj) : 32 + __clz((uint32_t)i ^ (uint32_t)j);
-}
-
-// Largest x in [lo, hi) with delta(i, i + x * d) > bound, given that it
-// holds at lo and fails at hi (the common prefix of sorted keys shrinks with
-// distance, so the predicate is monotone).  The whole warp tests 32 points
-// per round: ranges of a million keys take four rounds instead of the
-// twenty dependent loads of a binary search.
-__device__ __forceinline__ int warp_search(const uint32_t* __restrict__ codes, int n, int i, uint32_t ki, int d,
-                                           int bound, int lo, int hi) {
-  const int lane = threadIdx.x & 31;
-  for (int round = 0; round < 16 && hi - lo > 1; ++round) {
-    const int span = hi - lo, q = span / 33, r = span % 33;
-    const int p = lo + q * (lane + 1) + (r * (lane + 1)) / 33;  // lo + floor(span * (lane + 1) / 33)
-    const bool t = p <= lo ? true : p >= hi ? false : delta32(codes, n, i, i + p * d, ki) > bound;
-    const uint32_t yes = __ballot_sync(0xffffffffu, t);  // a prefix of the lanes
-    if (yes == 0u) {  // the answer lies below lane 0's point
-      hi = __shfl_sync(0xffffffffu, p, 0);
-      continue;
-    }
-    const int last = 31 - __clz(yes);
-    const int nlo = __shfl_sync(0xffffffffu, p, last);
-    const int nhi = __shfl_sync(0xffffffffu, p, last < 31 ? last + 1 : 31);
-    lo = nlo;
-    if (last < 31) hi = nhi;
-  }
-  return lo;
-}
-
-constexpr int kSoloSpan = 64;  // longer ranges are searched by the warp
 
 // Internal node i of the radix tree (one thread per node; Karras 2012).
 // Also lays out the refit: a node of more than kTreeletSpan leaves is a top
@@ -83,62 +47,18 @@ __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict_
   uint32_t knext = __shfl_down_sync(0xffffffffu, ki, 1);
   const bool active = i + 1 < n;  // every lane stays for the warp searches
   const int lane = threadIdx.x & 31;
-  int d = 1, dmin = 0, l = 0;
-  bool wide = false;
+  int dprev = -1, dnext = -1;
   if (active) {
     if (lane == 0 && i > 0) kprev = __ldg(codes + i - 1);
     if (lane == 31) knext = __ldg(codes + i + 1);
-    const int dnext = ki != knext ? __clz(ki ^ knext) : 32 + __clz((uint32_t)i ^ (uint32_t)(i + 1));
-    const int dprev = i == 0 ? -1 : (ki != kprev ? __clz(ki ^ kprev) : 32 + __clz((uint32_t)i ^ (uint32_t)(i - 1)));
-    d = (dnext - dprev) > 0 ? 1 : -1;
-    dmin = d > 0 ? dprev : dnext;
-    int lmax = 2;
-    while (delta32(codes, n, i, i + lmax * d, ki) > dmin) {
-      lmax *= 2;
-      if (lmax > kSoloSpan) { wide = true; break; }
-    }
-    if (!wide)
-      for (int t = lmax / 2; t >= 1; t /= 2)
-        if (delta32(codes, n, i, i + (l + t) * d, ki) > dmin) l += t;
+    dnext = ki != knext ? __clz(ki ^ knext) : 32 + __clz((uint32_t)i ^ (uint32_t)(i + 1));
+    dprev = i == 0 ? -1 : (ki != kprev ? __clz(ki ^ kprev) : 32 + __clz((uint32_t)i ^ (uint32_t)(i - 1)));
   }
-  // Range end of the wide lanes, one lane at a time, by the whole warp.
-  for (uint32_t pend = __ballot_sync(0xffffffffu, wide); pend; pend &= pend - 1) {
-    const int src = __ffs(pend) - 1;
-    const int si = __shfl_sync(0xffffffffu, i, src);
-    const uint32_t sk = __shfl_sync(0xffffffffu, ki, src);
-    const int sd = __shfl_sync(0xffffffffu, d, src);
-    const int sb = __shfl_sync(0xffffffffu, dmin, src);
-    const int lim = (sd > 0 ? n - 1 - si : si) + 1;  // first distance outside the keys
-    const int r = warp_search(codes, n, si, sk, sd, sb, kSoloSpan, lim);
-    if (lane == src) l = r;
-  }
-  const int j = i + l * d;
-  const int dnode = active ? delta32(codes, n, i, j, ki) : 0;
-  // Split: the largest s < l with delta(i, i + s d) > dnode.
-  int sp = 0;
-  const bool wide_split = active && l > kSoloSpan;
-  if (active && !wide_split) {
-    int t = l;
-    do {
-      t = (t + 1) >> 1;
-      if (delta32(codes, n, i, i + (sp + t) * d, ki) > dnode) sp += t;
-    } while (t > 1);
-  }
-  for (uint32_t pend = __ballot_sync(0xffffffffu, wide_split); pend; pend &= pend - 1) {
-    const int src = __ffs(pend) - 1;
-    const int si = __shfl_sync(0xffffffffu, i, src);
-    const uint32_t sk = __shfl_sync(0xffffffffu, ki, src);
-    const int sd = __shfl_sync(0xffffffffu, d, src);
-    const int sb = __shfl_sync(0xffffffffu, dnode, src);
-    const int sl = __shfl_sync(0xffffffffu, l, src);
-    const int r = warp_search(codes, n, si, sk, sd, sb, 0, sl);
-    if (lane == src) sp = r;
-  }
+  const int4 nd = karras_node_warp(codes, n, i, ki, dprev, dnext, active);
   if (!active) return;
-  const int gamma = i + sp * d + (d < 0 ? -1 : 0);
-  const int lo = i < j ? i : j, hi = i < j ? j : i;
-  const int32_t lc = (lo == gamma) ? ~gamma : gamma;
-  const int32_t rc = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  const int32_t lc = nd.x, rc = nd.y;
+  const int lo = nd.z, hi = nd.w;
+  const int gamma = lc >= 0 ? lc : ~lc;  // the left child ends at the split
   reinterpret_cast<int4*>(nodes)[4 * (size_t)i + 3] = make_int4(lc, rc, lc < 0 ? 1 : 0, rc < 0 ? 1 : 0);
   parent[lc >= 0 ? lc : (n - 1 + ~lc)] = ((uint32_t)i << 1) | 0u;
   parent[rc >= 0 ? rc : (n - 1 + ~rc)] = ((uint32_t)i << 1) | 1u;

@@ -60,46 +60,110 @@ __device__ __forceinline__ F3 tri_centroid(const float4* __restrict__ verts4, co
   return cen;
 }
 
-// Karras 2012 prefix length between sorted codes i and j (index tiebreak).
-__device__ __forceinline__ int karras_delta(const uint32_t* __restrict__ k, int64_t n, int64_t i, int64_t j,
-                                            uint32_t ki) {
+// Karras 2012 prefix length between sorted codes i and j with the index
+// tiebreak; -1 outside the keys.  32-bit indices: scenes hold fewer than
+// 2^30 primitives.
+__device__ __forceinline__ int delta32(const uint32_t* __restrict__ k, int n, int i, int j, uint32_t ki) {
   if (j < 0 || j >= n) return -1;
-  uint32_t kj = __ldg(k + j);
-  if (ki != kj) return __clz(ki ^ kj);
-  return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+  const uint32_t kj = __ldg(k + j);
+  return ki != kj ? __clz(ki ^ kj) : 32 + __clz((uint32_t)i ^ (uint32_t)j);
 }
 
-// Internal node i (0 <= i < n - 1) of the radix tree over n sorted codes,
-// given the neighbour deltas: (left, right, first leaf, last leaf), children
-// encoded as ~slot for leaves.
-__device__ __forceinline__ int4 karras_node(const uint32_t* __restrict__ codes, int64_t N, int64_t i,
-                                           uint32_t ki, int dprev, int dnext) {
-  int d = (dnext - dprev) > 0 ? 1 : -1;
-  int dmin = d > 0 ? dprev : dnext;
-  int64_t lmax = 2;
-  while (karras_delta(codes, N, i, i + lmax * d, ki) > dmin) lmax *= 2;
-  int64_t l = 0;
-  for (int64_t t = lmax / 2; t >= 1; t /= 2)
-    if (karras_delta(codes, N, i, i + (l + t) * d, ki) > dmin) l += t;
-  int64_t j = i + l * d;
-  int dnode = karras_delta(codes, N, i, j, ki);
-  int64_t s = 0, t = l;
-  do {
-    t = (t + 1) >> 1;
-    if (karras_delta(codes, N, i, i + (s + t) * d, ki) > dnode) s += t;
-  } while (t > 1);
-  int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
-  int64_t lo = i < j ? i : j, hi = i < j ? j : i;
-  int32_t lc = (lo == gamma) ? ~(int32_t)gamma : (int32_t)gamma;
-  int32_t rc = (hi == gamma + 1) ? ~(int32_t)(gamma + 1) : (int32_t)(gamma + 1);
-  return make_int4(lc, rc, (int32_t)lo, (int32_t)hi);
+// Largest x in [lo, hi) with delta(i, i + x * d) > bound, given that it
+// holds at lo and fails at hi (the common prefix of sorted keys shrinks with
+// distance, so the predicate is monotone).  The whole warp tests 32 points
+// per round: ranges of a million keys take four rounds instead of the
+// twenty dependent loads of a binary search.
+__device__ __forceinline__ int warp_search(const uint32_t* __restrict__ codes, int n, int i, uint32_t ki, int d,
+                                           int bound, int lo, int hi) {
+  const int lane = threadIdx.x & 31;
+  for (int round = 0; round < 16 && hi - lo > 1; ++round) {
+    const int span = hi - lo, q = span / 33, r = span % 33;
+    const int p = lo + q * (lane + 1) + (r * (lane + 1)) / 33;  // lo + floor(span * (lane + 1) / 33)
+    const bool t = p <= lo ? true : p >= hi ? false : delta32(codes, n, i, i + p * d, ki) > bound;
+    const uint32_t yes = __ballot_sync(0xffffffffu, t);  // a prefix of the lanes
+    if (yes == 0u) {  // the answer lies below lane 0's point
+      hi = __shfl_sync(0xffffffffu, p, 0);
+      continue;
+    }
+    const int last = 31 - __clz(yes);
+    const int nlo = __shfl_sync(0xffffffffu, p, last);
+    const int nhi = __shfl_sync(0xffffffffu, p, last < 31 ? last + 1 : 31);
+    lo = nlo;
+    if (last < 31) hi = nhi;
+  }
+  return lo;
 }
 
-// (left, right) of internal node i; leaves encoded as ~slot.
-__device__ __forceinline__ int2 karras_children(const uint32_t* __restrict__ codes, int64_t N, int64_t i,
-                                                uint32_t ki, int dprev, int dnext) {
-  const int4 c = karras_node(codes, N, i, ki, dprev, dnext);
-  return make_int2(c.x, c.y);
+constexpr int kSoloSpan = 64;  // longer ranges are searched by the warp
+
+// Internal node i (0 <= i < n - 1) of the radix tree over the n sorted codes
+// at `codes` (Karras 2012), given the neighbour deltas: (left, right, first
+// leaf, last leaf), children encoded as ~slot for leaves.  A lane searches
+// ranges and splits of up to kSoloSpan keys alone; longer ones are searched
+// by the whole warp, one lane at a time, with that lane's code array and key
+// count broadcast (lanes of one warp may belong to different key sets).  All
+// 32 lanes must call it; inactive lanes only take part in the searches.
+__device__ __forceinline__ int4 karras_node_warp(const uint32_t* __restrict__ codes, int n, int i, uint32_t ki,
+                                                 int dprev, int dnext, bool active) {
+  const int lane = threadIdx.x & 31;
+  int d = 1, dmin = 0, l = 0;
+  bool wide = false;
+  if (active) {
+    d = (dnext - dprev) > 0 ? 1 : -1;
+    dmin = d > 0 ? dprev : dnext;
+    int lmax = 2;
+    while (delta32(codes, n, i, i + lmax * d, ki) > dmin) {
+      lmax *= 2;
+      if (lmax > kSoloSpan) { wide = true; break; }
+    }
+    if (!wide)
+      for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta32(codes, n, i, i + (l + t) * d, ki) > dmin) l += t;
+  }
+  const unsigned long long cw = reinterpret_cast<unsigned long long>(codes);
+  // Range end of the wide lanes, one lane at a time, by the whole warp.
+  for (uint32_t pend = __ballot_sync(0xffffffffu, wide); pend; pend &= pend - 1) {
+    const int src = __ffs(pend) - 1;
+    const uint32_t* sc = reinterpret_cast<const uint32_t*>(__shfl_sync(0xffffffffu, cw, src));
+    const int sn = __shfl_sync(0xffffffffu, n, src);
+    const int si = __shfl_sync(0xffffffffu, i, src);
+    const uint32_t sk = __shfl_sync(0xffffffffu, ki, src);
+    const int sd = __shfl_sync(0xffffffffu, d, src);
+    const int sb = __shfl_sync(0xffffffffu, dmin, src);
+    const int lim = (sd > 0 ? sn - 1 - si : si) + 1;  // first distance outside the keys
+    const int r = warp_search(sc, sn, si, sk, sd, sb, kSoloSpan, lim);
+    if (lane == src) l = r;
+  }
+  const int j = i + l * d;
+  const int dnode = active ? delta32(codes, n, i, j, ki) : 0;
+  // Split: the largest s < l with delta(i, i + s d) > dnode.
+  int sp = 0;
+  const bool wide_split = active && l > kSoloSpan;
+  if (active && !wide_split) {
+    int t = l;
+    do {
+      t = (t + 1) >> 1;
+      if (delta32(codes, n, i, i + (sp + t) * d, ki) > dnode) sp += t;
+    } while (t > 1);
+  }
+  for (uint32_t pend = __ballot_sync(0xffffffffu, wide_split); pend; pend &= pend - 1) {
+    const int src = __ffs(pend) - 1;
+    const uint32_t* sc = reinterpret_cast<const uint32_t*>(__shfl_sync(0xffffffffu, cw, src));
+    const int sn = __shfl_sync(0xffffffffu, n, src);
+    const int si = __shfl_sync(0xffffffffu, i, src);
+    const uint32_t sk = __shfl_sync(0xffffffffu, ki, src);
+    const int sd = __shfl_sync(0xffffffffu, d, src);
+    const int sb = __shfl_sync(0xffffffffu, dnode, src);
+    const int sl = __shfl_sync(0xffffffffu, l, src);
+    const int r = warp_search(sc, sn, si, sk, sd, sb, 0, sl);
+    if (lane == src) sp = r;
+  }
+  const int gamma = i + sp * d + (d < 0 ? -1 : 0);
+  const int lo = i < j ? i : j, hi = i < j ? j : i;
+  const int32_t lc = (lo == gamma) ? ~gamma : gamma;
+  const int32_t rc = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  return make_int4(lc, rc, lo, hi);
 }
 
 // Refit decomposition of an LBVH: treelets are the maximal subtrees of at
