@@ -53,16 +53,26 @@ struct LevelNodes {
   int32_t* bad;       // badRefines
   uint32_t* rs;       // first ref
   uint32_t* rc;       // ref count
-  int32_t* axis0;
-  int32_t* eval;      // axis evaluated in the current pass, -1 when not pending
-  int32_t* retries;
-  unsigned long long* best;  // (cost key << 32) | edge offset
-  uint32_t* edge_base;
+  int32_t* axis0;     // longest axis of the node box
+  unsigned long long* best;  // 3 per node, one per axis: (cost key << 32) | edge offset in the node
   int32_t* state;     // 0 undecided, 1 leaf, 2 interior
   int32_t* best_axis;
   uint32_t* best_off;
   float* tsplit;
-  int32_t* pass_found;  // pass in which the split was found
+};
+
+// Edge lists: one per axis, each holding 2 edges per ref of the level (the
+// node's refs' edges at [2 rs, 2 rs + 2 rc)), sorted inside every node by
+// (t, start before end, ref), the order buildTree's edge sort gives
+// (:872-879) with ties in primitive-id order.  Structure of arrays:
+// t[a] (ordered float keys) and v[a] (ref << 1 | end).  A child's lists come
+// from its parent's by a stable partition, so the edges are sorted once, at
+// the root.
+struct EdgeLists {
+  uint32_t* base;
+  size_t cap;  // edges per list
+  __host__ __device__ uint32_t* t(int a) const { return base + (size_t)a * cap; }
+  __host__ __device__ uint32_t* v(int a) const { return base + (size_t)(3 + a) * cap; }
 };
 
 // Pre-leaf test and first axis (:843, :860).
@@ -70,134 +80,313 @@ __global__ void k_node_init(LevelNodes L, uint32_t M) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= M) return;
   const float* b = L.box + 6 * (size_t)k;
-  L.best[k] = kNone;
-  L.retries[k] = 0;
-  L.pass_found[k] = -1;
+  for (int a = 0; a < 3; ++a) L.best[3 * (size_t)k + a] = kNone;
   L.best_axis[k] = -1;
   if ((int)L.rc[k] <= kMaxPrims || L.depth[k] == 0) {
     L.state[k] = 1;
-    L.eval[k] = -1;
     return;
   }
   float ax = __fsub_rn(b[3], b[0]), ay = __fsub_rn(b[4], b[1]), az = __fsub_rn(b[5], b[2]);
-  int a = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
   L.state[k] = 0;
-  L.axis0[k] = a;
-  L.eval[k] = a;
+  L.axis0[k] = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
 }
 
-__global__ void k_pending_flags(const uint32_t* __restrict__ ref_node, uint32_t R, const int32_t* __restrict__ eval,
-                                uint32_t* __restrict__ flag) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r > R) return;
-  flag[r] = r < R && eval[ref_node[r]] >= 0 ? 1u : 0u;
+// Root edge lists before the sort: starts of refs 0..n-1, then their ends,
+// so a stable sort by t alone orders equal t start-first and by ref.
+__global__ void k_root_edges(const float* __restrict__ aabb, uint32_t n, int a, uint32_t* __restrict__ t,
+                             uint32_t* __restrict__ v) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float* q = aabb + 6 * (size_t)p;
+  t[p] = float_key(__ldg(q + a));
+  v[p] = p << 1;
+  t[n + p] = float_key(__ldg(q + 3 + a));
+  v[n + p] = (p << 1) | 1u;
 }
 
-// Two edges per pending ref: (min, start) and (max, end) along the node's axis.
-__global__ void k_edges(const uint32_t* __restrict__ ref_prim, const uint32_t* __restrict__ ref_node, uint32_t R,
-                        const uint32_t* __restrict__ flag, const uint32_t* __restrict__ epos, LevelNodes L,
-                        const float* __restrict__ aabb, unsigned long long* __restrict__ keys,
-                        uint32_t* __restrict__ vals, uint32_t E, uint32_t* err) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= R || !flag[r]) return;
-  const uint32_t k = ref_node[r];
-  const int a = L.eval[k];
-  const uint32_t e = 2 * epos[r];
-  if (e + 1 >= E || a < 0 || a > 2) { atomicOr(err, kErrCorrupt); return; }
-  if (r == L.rs[k]) L.edge_base[k] = e;
-  const float* q = aabb + 6 * (size_t)ref_prim[r];
-  const unsigned long long hi = (unsigned long long)k << 33;
-  keys[e] = hi | ((unsigned long long)float_key(__ldg(q + a)) << 1) | 0ull;
-  keys[e + 1] = hi | ((unsigned long long)float_key(__ldg(q + 3 + a)) << 1) | 1ull;
-  vals[e] = r;
-  vals[e + 1] = r;
+// Single-pass prefix counts over the three edge lists.  A block takes one
+// tile of kEdgeTile edges (tiles numbered in launch order by an atomic
+// counter, list-major), warp w its 256-edge run, lane l edge 32 j + l of the
+// run in round j.  Per-edge 0/1 flags are counted with ballots; the tile's
+// prefix across earlier tiles of the same list comes from decoupled
+// look-back over 64-bit status words (two 31-bit counts, flag in the top
+// bits; the counts never carry into each other because lists hold fewer than
+// 2^31 edges).  A wait that gives up marks the tile failed and the build
+// reports kErrTimeout.
+constexpr int kEdgeItems = 8;
+constexpr uint32_t kEdgeTile = kThreads * kEdgeItems;  // 2048
+constexpr unsigned long long kStAgg = 1ull << 62, kStIncl = 2ull << 62, kStFail = 3ull << 62;
+constexpr unsigned long long kStValue = (1ull << 62) - 1;
+
+struct TileScan {
+  uint32_t tile, list, local;
+  unsigned long long warp_pre[kThreads / 32];
+  unsigned long long tile_pre;
+  int fail;
+};
+
+__device__ __forceinline__ void tile_claim(TileScan& ts, uint32_t* counter, uint32_t tiles_per_list) {
+  if (threadIdx.x == 0) {
+    const uint32_t t = atomicAdd(counter, 1u);
+    ts.tile = t;
+    ts.list = t / tiles_per_list;
+    ts.local = t - ts.list * tiles_per_list;
+    ts.fail = 0;
+  }
+  __syncthreads();
 }
 
-__global__ void k_edge_flags(const unsigned long long* __restrict__ keys, uint32_t E, uint32_t* __restrict__ fs,
-                             uint32_t* __restrict__ fe) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > E) return;
-  const bool end = i < E && (keys[i] & 1ull);
-  fs[i] = i < E && !end ? 1u : 0u;
-  fe[i] = end ? 1u : 0u;
+// Exclusive prefix (packed) of this warp's first edge; `mine` is the warp's
+// packed total.  All threads call it.
+__device__ __forceinline__ unsigned long long tile_prefix(TileScan& ts, unsigned long long mine,
+                                                          unsigned long long* status, uint32_t* err) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) ts.warp_pre[warp] = mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long run = 0;
+    for (int w = 0; w < kThreads / 32; ++w) {
+      const unsigned long long c = ts.warp_pre[w];
+      ts.warp_pre[w] = run;
+      run += c;
+    }
+    volatile unsigned long long* st = status;
+    const uint32_t first = ts.tile - ts.local;  // tile 0 of this list
+    unsigned long long excl = 0;
+    if (ts.local == 0) {
+      st[ts.tile] = kStIncl | run;
+    } else {
+      st[ts.tile] = kStAgg | run;
+      bool failed = false;
+      for (uint32_t j = ts.tile - 1;; --j) {
+        unsigned long long s = 0;
+        const bool ok = spin_until([&] { s = st[j]; return (s >> 62) != 0; }, 1u << 20);
+        if (!ok || (s & ~kStValue) == kStFail) { failed = true; break; }
+        excl += s & kStValue;
+        if ((s & ~kStValue) == kStIncl || j == first) break;
+      }
+      if (failed) {
+        st[ts.tile] = kStFail;
+        ts.fail = 1;
+        atomicOr(err, kErrTimeout);
+      } else {
+        st[ts.tile] = kStIncl | ((excl + run) & kStValue);
+      }
+    }
+    ts.tile_pre = excl;
+  }
+  __syncthreads();
+  return ts.tile_pre + ts.warp_pre[warp];
 }
 
-// SAH cost of splitting at every edge (buildTree :883-912, same float ops).
-__global__ void k_cost(const unsigned long long* __restrict__ keys, uint32_t E, const uint32_t* __restrict__ ss,
-                       const uint32_t* __restrict__ se, LevelNodes L) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= E) return;
-  const unsigned long long key = keys[i];
-  const uint32_t k = (uint32_t)(key >> 33);
-  const int axis = L.eval[k];
-  const float t = key_float((uint32_t)(key >> 1));
-  const float* b = L.box + 6 * (size_t)k;
-  const float lo = b[axis], hi = b[3 + axis];
-  if (!(t > lo && t < hi)) return;
-  const uint32_t base = L.edge_base[k];
-  const uint32_t n = L.rc[k];
-  const uint32_t nBelow = ss[i] - ss[base];
-  const uint32_t nEndIncl = se[i] - se[base] + (uint32_t)(key & 1ull);
-  const uint32_t nAbove = n - nEndIncl;
-  float d[3] = {__fsub_rn(b[3], b[0]), __fsub_rn(b[4], b[1]), __fsub_rn(b[5], b[2])};
-  float totalSA = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[1]), __fmul_rn(d[0], d[2])),
-                                            __fmul_rn(d[1], d[2])));
-  float invTotalSA = __fdiv_rn(1.f, totalSA);
-  const int o0 = (axis + 1) % 3, o1 = (axis + 2) % 3;
-  float dd = __fmul_rn(d[o0], d[o1]), ds = __fadd_rn(d[o0], d[o1]);
-  float belowSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(t, lo), ds)));
-  float aboveSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(hi, t), ds)));
-  float pB = __fmul_rn(belowSA, invTotalSA), pA = __fmul_rn(aboveSA, invTotalSA);
-  float eb = (nAbove == 0 || nBelow == 0) ? kEmptyBonus : 0.f;
-  float cost = __fadd_rn(kTrav, __fmul_rn(__fmul_rn(kIsect, __fsub_rn(1.f, eb)),
-                                          __fadd_rn(__fmul_rn(pB, (float)nBelow), __fmul_rn(pA, (float)nAbove))));
-  const unsigned long long ck = ((unsigned long long)float_key(cost) << 32) | (unsigned long long)(i - base);
-  atomicMin(L.best + k, ck);
+// SAH cost of splitting at every edge of every undecided node, on all three
+// axes at once (buildTree :883-912, same float operations).  buildTree tries
+// the longest axis and moves to the next only when it has no candidate edge
+// (:915-919); every axis's minimum is kept and k_decide takes the first axis
+// in that order that has a candidate, which is the same choice.
+//
+// nBelow of edge e in node k is the number of start edges before it: the
+// list-wide start count before e minus rs[k] (every ref has exactly one start
+// edge in each list).  The lanes of a warp that share a node are consecutive,
+// so each round takes the node's minimum by a segmented shuffle reduction
+// and only the first lane of each node's run issues the atomicMin, and only
+// when the node's current best is above its value (the best only falls).
+__global__ void __launch_bounds__(kThreads) k_cost(EdgeLists el, uint32_t E2, uint32_t tiles_per_list,
+                                                   const uint32_t* __restrict__ ref_node, uint32_t R, uint32_t M,
+                                                   LevelNodes L,
+                                                   unsigned long long* status, uint32_t* counter, uint32_t* err) {
+  __shared__ TileScan ts;
+  tile_claim(ts, counter, tiles_per_list);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int a = (int)ts.list;
+  const uint32_t run0 = ts.local * kEdgeTile + (uint32_t)warp * (32 * kEdgeItems);
+  const uint32_t* __restrict__ tl = el.t(a);
+  const uint32_t* __restrict__ vl = el.v(a);
+  uint32_t tk[kEdgeItems], vv[kEdgeItems], starts[kEdgeItems];
+  uint32_t total = 0;
+#pragma unroll
+  for (int j = 0; j < kEdgeItems; ++j) {
+    const uint32_t e = run0 + 32 * j + lane;
+    const bool in = e < E2;
+    tk[j] = in ? __ldg(tl + e) : 0u;
+    vv[j] = in ? __ldg(vl + e) : 1u;
+    starts[j] = __ballot_sync(0xffffffffu, in && !(vv[j] & 1u));
+    total += __popc(starts[j]);
+  }
+  uint32_t below_run = (uint32_t)tile_prefix(ts, total, status, err);
+  if (ts.fail) return;
+  const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < kEdgeItems; ++j) {
+    const uint32_t e = run0 + 32 * j + lane;
+    const uint32_t r = vv[j] >> 1;
+    bool in = e < E2;
+    if (in && r >= R) { atomicOr(err, kErrCorrupt); in = false; }
+    uint32_t k = in ? __ldg(ref_node + r) : 0xFFFFFFFFu;
+    if (in && k >= M) { atomicOr(err, kErrCorrupt); in = false; k = 0xFFFFFFFFu; }
+    unsigned long long ck = kNone;
+    if (in && L.state[k] == 0) {
+      const float t = key_float(tk[j]);
+      const float* b = L.box + 6 * (size_t)k;
+      const float lo = b[a], hi = b[3 + a];
+      if (t > lo && t < hi) {
+        const uint32_t rs = L.rs[k], n = L.rc[k];
+        const uint32_t nBelow = below_run + __popc(starts[j] & lt) - rs;
+        const uint32_t off = e - 2 * rs;
+        const uint32_t nEndIncl = off - nBelow + (vv[j] & 1u);
+        const uint32_t nAbove = n - nEndIncl;
+        float d[3] = {__fsub_rn(b[3], b[0]), __fsub_rn(b[4], b[1]), __fsub_rn(b[5], b[2])};
+        float totalSA = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[1]), __fmul_rn(d[0], d[2])),
+                                                  __fmul_rn(d[1], d[2])));
+        float invTotalSA = __fdiv_rn(1.f, totalSA);
+        const int o0 = (a + 1) % 3, o1 = (a + 2) % 3;
+        float dd = __fmul_rn(d[o0], d[o1]), ds = __fadd_rn(d[o0], d[o1]);
+        float belowSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(t, lo), ds)));
+        float aboveSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(hi, t), ds)));
+        float pB = __fmul_rn(belowSA, invTotalSA), pA = __fmul_rn(aboveSA, invTotalSA);
+        float eb = (nAbove == 0 || nBelow == 0) ? kEmptyBonus : 0.f;
+        float cost = __fadd_rn(kTrav, __fmul_rn(__fmul_rn(kIsect, __fsub_rn(1.f, eb)),
+                                                __fadd_rn(__fmul_rn(pB, (float)nBelow),
+                                                          __fmul_rn(pA, (float)nAbove))));
+        ck = ((unsigned long long)float_key(cost) << 32) | (unsigned long long)off;
+      }
+    }
+    below_run += __popc(starts[j]);
+    // Minimum over the lane's run of equal nodes from this lane on.
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long x = __shfl_down_sync(0xffffffffu, ck, o);
+      const uint32_t kk = __shfl_down_sync(0xffffffffu, k, o);
+      if (lane + o < 32 && kk == k && x < ck) ck = x;
+    }
+    const uint32_t kprev = __shfl_up_sync(0xffffffffu, k, 1);
+    const bool head = in && (lane == 0 || kprev != k);
+    unsigned long long* slot = L.best + 3 * (size_t)k + a;
+    if (head && ck != kNone && __ldcg(slot) > ck) atomicMin(slot, ck);
+  }
 }
 
-// After a pass: found split -> leaf/interior decision (:920-925); none -> next axis.
-__global__ void k_pass_decide(LevelNodes L, uint32_t M, int pass) {
+// Split decision (:915-925): the first axis from the longest on with a
+// candidate edge; none -> leaf.
+__global__ void k_decide(LevelNodes L, uint32_t M) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= M || L.eval[k] < 0) return;
-  const unsigned long long b = L.best[k];
-  if (b != kNone) {
+  if (k >= M || L.state[k] != 0) return;
+  for (int q = 0; q < 3; ++q) {
+    const int a = (L.axis0[k] + q) % 3;
+    const unsigned long long b = L.best[3 * (size_t)k + a];
+    if (b == kNone) continue;
     const float bestCost = key_float((uint32_t)(b >> 32));
     const float oldCost = __fmul_rn(kIsect, (float)L.rc[k]);
-    int bad = L.bad[k] + (bestCost > oldCost ? 1 : 0);
+    const int bad = L.bad[k] + (bestCost > oldCost ? 1 : 0);
     L.bad[k] = bad;
     const bool leaf = (bestCost > __fmul_rn(4.f, oldCost) && L.rc[k] < 16) || bad == 3;
     L.state[k] = leaf ? 1 : 2;
-    L.best_axis[k] = L.eval[k];
+    L.best_axis[k] = a;
     L.best_off[k] = (uint32_t)(b & 0xFFFFFFFFull);
-    L.pass_found[k] = pass;
-    L.eval[k] = -1;
     return;
   }
-  int r = L.retries[k] + 1;
-  L.retries[k] = r;
-  if (r <= 2) {
-    L.eval[k] = (L.axis0[k] + r) % 3;
-  } else {
-    L.state[k] = 1;  // no split found on any axis
-    L.eval[k] = -1;
-  }
+  L.state[k] = 1;  // no split found on any axis
 }
 
-// Below/above sides from the winning pass's sorted edges (:928-934).
-__global__ void k_classify(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t E,
-                           LevelNodes L, int pass, uint32_t* __restrict__ below, uint32_t* __restrict__ above,
-                           uint32_t R, uint32_t* err) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= E) return;
-  const unsigned long long key = keys[i];
-  const uint32_t k = (uint32_t)(key >> 33);
-  if (L.pass_found[k] != pass || L.state[k] != 2) return;
-  const uint32_t off = i - L.edge_base[k], best = L.best_off[k];
-  const uint32_t r = vals[i];
+// Below/above sides from the chosen axis's edges (:928-934): a ref whose
+// start edge precedes the split edge goes below, one whose end edge follows
+// it goes above.
+__global__ void k_classify(EdgeLists el, uint32_t E2, const uint32_t* __restrict__ ref_node, uint32_t M,
+                           LevelNodes L, uint32_t* __restrict__ below, uint32_t* __restrict__ above, uint32_t R,
+                           uint32_t* err) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 3ull * E2) return;
+  const int a = (int)(g / E2);
+  const uint32_t e = (uint32_t)(g - (uint64_t)a * E2);
+  const uint32_t v = __ldg(el.v(a) + e), r = v >> 1;
   if (r >= R) { atomicOr(err, kErrCorrupt); return; }
-  if (key & 1ull) above[r] = off > best ? 1u : 0u;
+  const uint32_t k = __ldg(ref_node + r);
+  if (k >= M) { atomicOr(err, kErrCorrupt); return; }
+  if (L.state[k] != 2 || L.best_axis[k] != a) return;
+  const uint32_t off = e - 2 * L.rs[k], best = L.best_off[k];
+  if (v & 1u) above[r] = off > best ? 1u : 0u;
   else below[r] = off < best ? 1u : 0u;
-  if (off == best) L.tsplit[k] = key_float((uint32_t)(key >> 1));
+  if (off == best) L.tsplit[k] = key_float(__ldg(el.t(a) + e));
+}
+
+// Children's edge lists: a stable partition of every interior node's edges,
+// on each axis, into its below child (refs with below[r]) and above child
+// (refs with above[r]); straddling refs go to both.  With sB / sA the
+// exclusive scans of below / above over the level's refs and EB(e) / EA(e)
+// the list-wide counts of below / above edges before e:
+//   below child position  EB(e) + 2 sA[rs],        its ref  sA[rs] + sB[r]
+//   above child position  EA(e) + 2 sB[rs + rc],   its ref  sB[rs + rc] + sA[r]
+// (children are laid out node by node, below before above, and leaf refs
+// count in neither scan), matching k_emit_refs's numbering of the refs.
+__global__ void __launch_bounds__(kThreads) k_partition(EdgeLists el, uint32_t E2, uint32_t tiles_per_list,
+                                                        const uint32_t* __restrict__ ref_node, uint32_t R,
+                                                        uint32_t M, LevelNodes L,
+                                                        const uint32_t* __restrict__ below,
+                                                        const uint32_t* __restrict__ above,
+                                                        const uint32_t* __restrict__ sB,
+                                                        const uint32_t* __restrict__ sA, EdgeLists out,
+                                                        uint32_t E2next, unsigned long long* status,
+                                                        uint32_t* counter, uint32_t* err) {
+  __shared__ TileScan ts;
+  tile_claim(ts, counter, tiles_per_list);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int a = (int)ts.list;
+  const uint32_t run0 = ts.local * kEdgeTile + (uint32_t)warp * (32 * kEdgeItems);
+  uint32_t tk[kEdgeItems], vv[kEdgeItems], kb[kEdgeItems], ka[kEdgeItems];
+  unsigned long long total = 0;
+#pragma unroll
+  for (int j = 0; j < kEdgeItems; ++j) {
+    const uint32_t e = run0 + 32 * j + lane;
+    const bool in = e < E2;
+    tk[j] = in ? __ldg(el.t(a) + e) : 0u;
+    vv[j] = in ? __ldg(el.v(a) + e) : 0u;
+    bool b = false, ab = false;
+    if (in) {
+      const uint32_t r = vv[j] >> 1;
+      if (r < R) {
+        b = __ldg(below + r) != 0u;
+        ab = __ldg(above + r) != 0u;
+      } else {
+        atomicOr(err, kErrCorrupt);
+      }
+    }
+    kb[j] = __ballot_sync(0xffffffffu, b);
+    ka[j] = __ballot_sync(0xffffffffu, ab);
+    total += ((unsigned long long)__popc(ka[j]) << 31) | (unsigned long long)__popc(kb[j]);
+  }
+  const unsigned long long pre = tile_prefix(ts, total, status, err);
+  if (ts.fail) return;
+  uint32_t eb = (uint32_t)(pre & 0x7FFFFFFFull), ea = (uint32_t)(pre >> 31);
+  const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < kEdgeItems; ++j) {
+    const bool b = (kb[j] >> lane) & 1u, ab = (ka[j] >> lane) & 1u;
+    const uint32_t r = vv[j] >> 1, end = vv[j] & 1u;
+    const uint32_t k = (b || ab) ? __ldg(ref_node + r) : 0u;
+    if ((b || ab) && k >= M) {
+      atomicOr(err, kErrCorrupt);
+    } else if (b || ab) {
+      const uint32_t rs = L.rs[k], re = rs + L.rc[k];
+      if (b) {
+        const uint32_t pos = eb + __popc(kb[j] & lt) + 2 * __ldg(sA + rs);
+        if (pos >= E2next) { atomicOr(err, kErrCorrupt); }
+        else {
+          out.t(a)[pos] = tk[j];
+          out.v(a)[pos] = ((__ldg(sA + rs) + __ldg(sB + r)) << 1) | end;
+        }
+      }
+      if (ab) {
+        const uint32_t pos = ea + __popc(ka[j] & lt) + 2 * __ldg(sB + re);
+        if (pos >= E2next) { atomicOr(err, kErrCorrupt); }
+        else {
+          out.t(a)[pos] = tk[j];
+          out.v(a)[pos] = ((__ldg(sB + re) + __ldg(sA + r)) << 1) | end;
+        }
+      }
+    }
+    eb += __popc(kb[j]);
+    ea += __popc(ka[j]);
+  }
 }
 
 __global__ void k_flag_of_state(LevelNodes L, uint32_t M, int want, uint32_t* __restrict__ out, int with_count) {
@@ -538,18 +727,14 @@ LevelNodes carve(char* base, uint32_t cap) {
   L.rs = (uint32_t*)take((size_t)cap * 4);
   L.rc = (uint32_t*)take((size_t)cap * 4);
   L.axis0 = (int32_t*)take((size_t)cap * 4);
-  L.eval = (int32_t*)take((size_t)cap * 4);
-  L.retries = (int32_t*)take((size_t)cap * 4);
-  L.best = (unsigned long long*)take((size_t)cap * 8);
-  L.edge_base = (uint32_t*)take((size_t)cap * 4);
+  L.best = (unsigned long long*)take((size_t)cap * 24);
   L.state = (int32_t*)take((size_t)cap * 4);
   L.best_axis = (int32_t*)take((size_t)cap * 4);
   L.best_off = (uint32_t*)take((size_t)cap * 4);
   L.tsplit = (float*)take((size_t)cap * 4);
-  L.pass_found = (int32_t*)take((size_t)cap * 4);
   return L;
 }
-size_t level_bytes(uint32_t cap) { return (size_t)cap * 100 + 16 * 256; }
+size_t level_bytes(uint32_t cap) { return (size_t)cap * 84 + 12 * 256; }
 
 Table table_at(char* base, uint32_t cap) {
   Table T;
@@ -612,12 +797,33 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
 
   // refs of the current level, double buffered: prim, node
   uint32_t R = n, M = 1;
+  if (2ull * n >= (1ull << 31)) return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "KD tree over 2^30 primitives");
   KD_TRY(sc.m1.ensure((size_t)n * 8 * 2), "KD scratch");
   uint32_t* ref_prim = sc.m1.as<uint32_t>();
   uint32_t* ref_node = ref_prim + (size_t)n;
   count_launch();
   k_iota<<<grid(n), kThreads, 0, st>>>(ref_prim, n);
   KD_TRY(cudaMemsetAsync(ref_node, 0, (size_t)n * 4, st), "KD init");
+  // root edge lists, one per axis, each sorted once by t (stable: equal t
+  // start-first, then by primitive id)
+  const uint32_t E0 = 2 * n;
+  KD_TRY(sc.keys.ensure((size_t)E0 * 6 * 4 + 64), "KD edges");
+  KD_TRY(sc.vals.ensure((size_t)E0 * 2 * 4 + 64), "KD edges");
+  EdgeLists el{sc.keys.as<uint32_t>(), (size_t)E0};
+  {
+    const size_t zwords = 1024 + 16 + sort_status_words(E0, 4);
+    KD_TRY(sc.m4.ensure(zwords * 4 + 64), "KD sort");
+    uint32_t* zero = sc.m4.as<uint32_t>();
+    SortScratch ss{sc.vals.as<uint32_t>(), sc.vals.as<uint32_t>() + E0, zero, zero + 1024 + 16, zero + 1024};
+    for (int ax = 0; ax < 3; ++ax) {
+      count_launch();
+      k_root_edges<<<grid(n), kThreads, 0, st>>>(aabb, n, ax, el.t(ax), el.v(ax));
+      KD_TRY(cudaMemsetAsync(zero, 0, zwords * 4, st), "KD sort");
+      launch_histogram(el.t(ax), E0, 4, zero, st);
+      launch_onesweep(el.t(ax), el.v(ax), E0, 4, ss, err, st);
+    }
+    KD_TRY(cudaGetLastError(), "KD root edges");
+  }
   // level 0 node
   KD_TRY(sc.m3.ensure(level_bytes(1)), "KD scratch");
   LevelNodes L = carve(sc.m3.as<char>(), 1);
@@ -662,86 +868,60 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
       table_cap = ncap;
     }
     Table T = table_at(tabbuf.as<char>(), table_cap);
-    // per-ref scratch: flags / scans (R + 1 each)
-    KD_TRY(sc.m2.ensure(((size_t)R + 1) * 4 * 6 + scan_tmp_words(2ull * R + 2) * 4 + 64), "KD scratch");
-    uint32_t* flag = sc.m2.as<uint32_t>();
-    uint32_t* epos = flag + (R + 1);
-    uint32_t* below = epos + (R + 1);
+    // per-ref scratch: below / above flags and their scans (R + 1 each)
+    KD_TRY(sc.m2.ensure(((size_t)R + 1) * 4 * 4 + scan_tmp_words((uint64_t)R + 1) * 4 + 64), "KD scratch");
+    uint32_t* below = sc.m2.as<uint32_t>();
     uint32_t* above = below + (R + 1);
     uint32_t* sB = above + (R + 1);
     uint32_t* sA = sB + (R + 1);
     uint32_t* tmp = sA + (R + 1);
-    uint32_t* tot = tmp + scan_tmp_words(2ull * R + 2) + 4;
     KD_TRY(cudaMemsetAsync(below, 0, ((size_t)R + 1) * 8, st), "KD flags");  // below + above
+    // look-back words of the two edge passes and their tile counters
+    const uint32_t E2 = 2 * R;
+    const uint32_t tiles = (E2 + kEdgeTile - 1) / kEdgeTile;
+    const size_t zbytes = (size_t)tiles * 3 * 8 * 2 + 64;
+    KD_TRY(sc.m4.ensure(zbytes), "KD edges");
+    unsigned long long* status = sc.m4.as<unsigned long long>();
+    uint32_t* counters = reinterpret_cast<uint32_t*>(status + (size_t)tiles * 3 * 2);
+    KD_TRY(cudaMemsetAsync(status, 0, zbytes, st), "KD edges");
     count_launch();
     k_node_init<<<grid(M), kThreads, 0, st>>>(L, M);
-    // edge arrays: keys (u64) x2, vals x2, start/end flags and scans
-    for (int pass = 0; pass < 3; ++pass) {
+    if (E2) {
       count_launch();
-      k_pending_flags<<<grid(R + 1), kThreads, 0, st>>>(ref_node, R, L.eval, flag);
-      launch_scan_excl(flag, epos, (uint64_t)R + 1, tmp, tot, st);
-      uint32_t pend = 0;
-      KD_TRY(cudaMemcpyAsync(&pend, tot, 4, cudaMemcpyDeviceToHost, st), "KD pass");
-      KD_TRY(cudaStreamSynchronize(st), "KD pass");
-      if (pend == 0) break;
-      const uint32_t E = 2 * pend;
-      const int passes = (33 + bitlen(M - 1) + 7) / 8;
-      KD_TRY(sc.keys.ensure((size_t)E * 8 * 2 + 64), "KD edges");
-      KD_TRY(sc.vals.ensure((size_t)E * 4 * 2 + 64), "KD edges");
-      KD_TRY(sc.m4.ensure(((size_t)E + 1) * 16 + scan_tmp_words((uint64_t)E + 1) * 4 +
-                          (2048 + 16 + sort_status_words64(E, passes)) * 4 + 256), "KD edges");
-      unsigned long long* keys = sc.keys.as<unsigned long long>();
-      unsigned long long* keys_alt = keys + E;
-      uint32_t* vals = sc.vals.as<uint32_t>();
-      uint32_t* vals_alt = vals + E;
-      uint32_t* fs = sc.m4.as<uint32_t>();
-      uint32_t* fe = fs + (E + 1);
-      uint32_t* ss = fe + (E + 1);
-      uint32_t* se = ss + (E + 1);
-      uint32_t* etmp = se + (E + 1);
-      uint32_t* zero = etmp + scan_tmp_words((uint64_t)E + 1) + 4;
-      const size_t zwords = 2048 + 16 + sort_status_words64(E, passes);
-      count_launch();
-      k_edges<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, flag, epos, L, aabb, keys, vals, E, err);
-      KD_TRY(cudaMemsetAsync(zero, 0, zwords * 4, st), "KD sort");
-      launch_histogram64(reinterpret_cast<uint64_t*>(keys), E, passes, zero, st);
-      launch_onesweep64(reinterpret_cast<uint64_t*>(keys), vals, E, passes, reinterpret_cast<uint64_t*>(keys_alt),
-                        vals_alt, zero, zero + 2048 + 16, zero + 2048, err, st);
-      count_launch(3);
-      k_edge_flags<<<grid((uint64_t)E + 1), kThreads, 0, st>>>(keys, E, fs, fe);
-      launch_scan_excl(fs, ss, (uint64_t)E + 1, etmp, nullptr, st);
-      launch_scan_excl(fe, se, (uint64_t)E + 1, etmp, nullptr, st);
-      k_cost<<<grid(E), kThreads, 0, st>>>(keys, E, ss, se, L);
-      k_pass_decide<<<grid(M), kThreads, 0, st>>>(L, M, pass);
-      count_launch();
-      k_classify<<<grid(E), kThreads, 0, st>>>(keys, vals, E, L, pass, below, above, R, err);
-      KD_TRY(cudaGetLastError(), "KD pass");
+      k_cost<<<3 * tiles, kThreads, 0, st>>>(el, E2, tiles, ref_node, R, M, L, status, counters, err);
     }
-    // interior ranks and leaf pool offsets
+    count_launch();
+    k_decide<<<grid(M), kThreads, 0, st>>>(L, M);
+    if (E2) {
+      count_launch();
+      k_classify<<<grid(3ull * E2), kThreads, 0, st>>>(el, E2, ref_node, M, L, below, above, R, err);
+    }
+    KD_TRY(cudaGetLastError(), "KD split");
+    // interior ranks, leaf pool offsets, children's ref counts
     KD_TRY(sc.m7.ensure(((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 4 + 64), "KD scratch");
     uint32_t* iflag = sc.m7.as<uint32_t>();
     uint32_t* irank = iflag + (M + 1);
     uint32_t* lcnt = irank + (M + 1);
     uint32_t* lofs = lcnt + (M + 1);
     uint32_t* mtmp = lofs + (M + 1);
-    uint32_t* mtot = mtmp + scan_tmp_words((uint64_t)M + 1) + 4;
+    uint32_t* mtot = mtmp + scan_tmp_words((uint64_t)M + 1) + 4;  // 4 totals
     count_launch(2);
     k_flag_of_state<<<grid(M + 1), kThreads, 0, st>>>(L, M, 2, iflag, 0);
     launch_scan_excl(iflag, irank, (uint64_t)M + 1, mtmp, mtot, st);
-    uint32_t interiors = 0;
-    KD_TRY(cudaMemcpyAsync(&interiors, mtot, 4, cudaMemcpyDeviceToHost, st), "KD level");
     k_flag_of_state<<<grid(M + 1), kThreads, 0, st>>>(L, M, 1, lcnt, 1);
-    launch_scan_excl(lcnt, lofs, (uint64_t)M + 1, mtmp, mtot, st);
-    uint32_t leaf_refs = 0;
-    KD_TRY(cudaMemcpyAsync(&leaf_refs, mtot, 4, cudaMemcpyDeviceToHost, st), "KD level");
-    launch_scan_excl(below, sB, (uint64_t)R + 1, tmp, nullptr, st);
-    launch_scan_excl(above, sA, (uint64_t)R + 1, tmp, nullptr, st);
+    launch_scan_excl(lcnt, lofs, (uint64_t)M + 1, mtmp, mtot + 1, st);
+    launch_scan_excl(below, sB, (uint64_t)R + 1, tmp, mtot + 2, st);
+    launch_scan_excl(above, sA, (uint64_t)R + 1, tmp, mtot + 3, st);
+    uint32_t h_tot[4] = {0, 0, 0, 0};
+    KD_TRY(cudaMemcpyAsync(h_tot, mtot, 16, cudaMemcpyDeviceToHost, st), "KD level");
     KD_TRY(cudaStreamSynchronize(st), "KD level");
+    const uint32_t interiors = h_tot[0], leaf_refs = h_tot[1];
+    const uint64_t R2l = (uint64_t)h_tot[2] + h_tot[3];
+    if (2 * R2l >= (1ull << 31)) return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "KD tree over 2^30 references");
+    const uint32_t R2 = (uint32_t)R2l;
     // next level nodes and child ref counts
     const uint32_t M2 = 2 * interiors;
     DevBuf& nextbuf = (level & 1) ? sc.m3 : sc.keys_alt;  // alternate level buffers
-    DevBuf& curbuf = (level & 1) ? sc.keys_alt : sc.m3;
-    (void)curbuf;
     KD_TRY(nextbuf.ensure(level_bytes(M2 ? M2 : 1) + ((size_t)M2 + 1) * 8 + scan_tmp_words((uint64_t)M2 + 1) * 4 + 64),
            "KD scratch");
     LevelNodes N = carve(nextbuf.as<char>(), M2 ? M2 : 1);
@@ -755,14 +935,11 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     k_spawn<<<grid(M), kThreads, 0, st>>>(L, M, irank, sB, sA, lofs, pool_used, total, total + M, T, N, ccnt, M2,
                                           err);
     KD_TRY(cudaGetLastError(), "KD spawn");
-    uint32_t R2 = 0;
     if (M2) {
       KD_TRY(cudaMemsetAsync(ccnt + M2, 0, 4, st), "KD spawn");
-      launch_scan_excl(ccnt, coff, (uint64_t)M2 + 1, ctmp, mtot, st);
+      launch_scan_excl(ccnt, coff, (uint64_t)M2 + 1, ctmp, nullptr, st);
       count_launch();
       k_set_ref_starts<<<grid(M2), kThreads, 0, st>>>(N, M2, ccnt, coff);
-      KD_TRY(cudaMemcpyAsync(&R2, mtot, 4, cudaMemcpyDeviceToHost, st), "KD spawn");
-      KD_TRY(cudaStreamSynchronize(st), "KD spawn");
     }
     // refs of the next level (separate buffer), leaf refs to the pool
     KD_TRY(sc.kd_refs.ensure(((size_t)R2 + 1) * 8), "KD refs");
@@ -773,11 +950,21 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
                                               out_node, lofs, pool_used, poolbuf.as<uint32_t>(), R2,
                                               (uint32_t)(poolbuf.cap / 4), err);
     KD_TRY(cudaGetLastError(), "KD emit");
+    // the children's edge lists
+    KD_TRY(sc.vals.ensure((size_t)R2 * 2 * 6 * 4 + 64), "KD edges");
+    EdgeLists eln{sc.vals.as<uint32_t>(), (size_t)R2 * 2};
+    if (E2 && R2) {
+      count_launch();
+      k_partition<<<3 * tiles, kThreads, 0, st>>>(el, E2, tiles, ref_node, R, M, L, below, above, sB, sA, eln, 2 * R2,
+                                                  status + (size_t)tiles * 3, counters + 1, err);
+      KD_TRY(cudaGetLastError(), "KD partition");
+    }
     pool_used += leaf_refs;
     total += M;
-    // swap ref buffers
     KD_TRY(cudaStreamSynchronize(st), "KD level");
     std::swap(sc.m1, sc.kd_refs);  // the children's refs become the current refs
+    std::swap(sc.keys, sc.vals);   // and their edge lists
+    el = EdgeLists{sc.keys.as<uint32_t>(), (size_t)R2 * 2};
     ref_prim = sc.m1.as<uint32_t>();
     ref_node = ref_prim + (R2 + 1);
     R = R2;
