@@ -59,13 +59,19 @@ struct LevelNodes {
   int32_t* best_axis;
   uint32_t* best_off;
   float* tsplit;
+  uint32_t* split_key;  // the split edge: ordered t key and (ref << 1 | end)
+  uint32_t* split_v;
+  float4* sa;           // node box extents d[0..2] and 1 / surface area, for the cost
+  uint4* plan;          // interior nodes: (sA[rs], sB[rs], sB[rs + rc], first child) for the partition
 };
 
 // Edge lists: one per axis, each holding 2 edges per ref of the level (the
 // node's refs' edges at [2 rs, 2 rs + 2 rc)), sorted inside every node by
 // (t, start before end, ref), the order buildTree's edge sort gives
 // (:872-879) with ties in primitive-id order.  Structure of arrays:
-// t[a] (ordered float keys) and v[a] (ref << 1 | end).  A child's lists come
+// t[a] (ordered float keys), v[a] (ref << 1 | end), n[a] (node) and s[a]
+// (the number of start edges before the edge in its node: the nBelow of the
+// cost, carried through the partitions).  A child's lists come
 // from its parent's by a stable partition, so the edges are sorted once, at
 // the root.
 struct EdgeLists {
@@ -73,7 +79,10 @@ struct EdgeLists {
   size_t cap;  // edges per list
   __host__ __device__ uint32_t* t(int a) const { return base + (size_t)a * cap; }
   __host__ __device__ uint32_t* v(int a) const { return base + (size_t)(3 + a) * cap; }
+  __host__ __device__ uint32_t* n(int a) const { return base + (size_t)(6 + a) * cap; }  // the edge's node
+  __host__ __device__ uint32_t* s(int a) const { return base + (size_t)(9 + a) * cap; }  // start edges before it in its node
 };
+constexpr int kEdgeWords = 12;  // t, v, node and start-rank arrays of the three lists
 
 // Pre-leaf test and first axis (:843, :860).
 __global__ void k_node_init(LevelNodes L, uint32_t M) {
@@ -89,6 +98,9 @@ __global__ void k_node_init(LevelNodes L, uint32_t M) {
   float ax = __fsub_rn(b[3], b[0]), ay = __fsub_rn(b[4], b[1]), az = __fsub_rn(b[5], b[2]);
   L.state[k] = 0;
   L.axis0[k] = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
+  // totalSA and its inverse as buildTree computes them (:855-857)
+  const float totalSA = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(ax, ay), __fmul_rn(ax, az)), __fmul_rn(ay, az)));
+  L.sa[k] = make_float4(ax, ay, az, __fdiv_rn(1.f, totalSA));
 }
 
 // Root edge lists before the sort: starts of refs 0..n-1, then their ends,
@@ -104,80 +116,14 @@ __global__ void k_root_edges(const float* __restrict__ aabb, uint32_t n, int a, 
   v[n + p] = (p << 1) | 1u;
 }
 
-// Single-pass prefix counts over the three edge lists.  A block takes one
-// tile of kEdgeTile edges (tiles numbered in launch order by an atomic
-// counter, list-major), warp w its 256-edge run, lane l edge 32 j + l of the
-// run in round j.  Per-edge 0/1 flags are counted with ballots; the tile's
-// prefix across earlier tiles of the same list comes from decoupled
-// look-back over 64-bit status words (two 31-bit counts, flag in the top
-// bits; the counts never carry into each other because lists hold fewer than
-// 2^31 edges).  A wait that gives up marks the tile failed and the build
-// reports kErrTimeout.
+__global__ void k_start_flags(const uint32_t* __restrict__ v, uint32_t E, uint32_t* __restrict__ f) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < E) f[e] = (v[e] & 1u) ? 0u : 1u;
+}
+
 constexpr int kEdgeItems = 8;
-constexpr uint32_t kEdgeTile = kThreads * kEdgeItems;  // 2048
-constexpr unsigned long long kStAgg = 1ull << 62, kStIncl = 2ull << 62, kStFail = 3ull << 62;
-constexpr unsigned long long kStValue = (1ull << 62) - 1;
-
-struct TileScan {
-  uint32_t tile, list, local;
-  unsigned long long warp_pre[kThreads / 32];
-  unsigned long long tile_pre;
-  int fail;
-};
-
-__device__ __forceinline__ void tile_claim(TileScan& ts, uint32_t* counter, uint32_t tiles_per_list) {
-  if (threadIdx.x == 0) {
-    const uint32_t t = atomicAdd(counter, 1u);
-    ts.tile = t;
-    ts.list = t / tiles_per_list;
-    ts.local = t - ts.list * tiles_per_list;
-    ts.fail = 0;
-  }
-  __syncthreads();
-}
-
-// Exclusive prefix (packed) of this warp's first edge; `mine` is the warp's
-// packed total.  All threads call it.
-__device__ __forceinline__ unsigned long long tile_prefix(TileScan& ts, unsigned long long mine,
-                                                          unsigned long long* status, uint32_t* err) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) ts.warp_pre[warp] = mine;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long run = 0;
-    for (int w = 0; w < kThreads / 32; ++w) {
-      const unsigned long long c = ts.warp_pre[w];
-      ts.warp_pre[w] = run;
-      run += c;
-    }
-    volatile unsigned long long* st = status;
-    const uint32_t first = ts.tile - ts.local;  // tile 0 of this list
-    unsigned long long excl = 0;
-    if (ts.local == 0) {
-      st[ts.tile] = kStIncl | run;
-    } else {
-      st[ts.tile] = kStAgg | run;
-      bool failed = false;
-      for (uint32_t j = ts.tile - 1;; --j) {
-        unsigned long long s = 0;
-        const bool ok = spin_until([&] { s = st[j]; return (s >> 62) != 0; }, 1u << 20);
-        if (!ok || (s & ~kStValue) == kStFail) { failed = true; break; }
-        excl += s & kStValue;
-        if ((s & ~kStValue) == kStIncl || j == first) break;
-      }
-      if (failed) {
-        st[ts.tile] = kStFail;
-        ts.fail = 1;
-        atomicOr(err, kErrTimeout);
-      } else {
-        st[ts.tile] = kStIncl | ((excl + run) & kStValue);
-      }
-    }
-    ts.tile_pre = excl;
-  }
-  __syncthreads();
-  return ts.tile_pre + ts.warp_pre[warp];
-}
+constexpr uint32_t kEdgeRun = 32 * kEdgeItems;               // edges per warp: lane l takes 32 j + l in round j
+constexpr uint32_t kEdgeTile = kEdgeRun * (kThreads / 32);  // edges per block of the partition passes
 
 // SAH cost of splitting at every edge of every undecided node, on all three
 // axes at once (buildTree :883-912, same float operations).  buildTree tries
@@ -185,62 +131,52 @@ __device__ __forceinline__ unsigned long long tile_prefix(TileScan& ts, unsigned
 // (:915-919); every axis's minimum is kept and k_decide takes the first axis
 // in that order that has a candidate, which is the same choice.
 //
-// nBelow of edge e in node k is the number of start edges before it: the
-// list-wide start count before e minus rs[k] (every ref has exactly one start
-// edge in each list).  The lanes of a warp that share a node are consecutive,
-// so each round takes the node's minimum by a segmented shuffle reduction
-// and only the first lane of each node's run issues the atomicMin, and only
-// when the node's current best is above its value (the best only falls).
-__global__ void __launch_bounds__(kThreads) k_cost(EdgeLists el, uint32_t E2, uint32_t tiles_per_list,
-                                                   const uint32_t* __restrict__ ref_node, uint32_t R, uint32_t M,
-                                                   LevelNodes L,
-                                                   unsigned long long* status, uint32_t* counter, uint32_t* err) {
-  __shared__ TileScan ts;
-  tile_claim(ts, counter, tiles_per_list);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int a = (int)ts.list;
-  const uint32_t run0 = ts.local * kEdgeTile + (uint32_t)warp * (32 * kEdgeItems);
+// One warp per run of 256 consecutive edges of one list, lane l taking edge
+// 32 j + l in round j.  The lanes that share a node are consecutive, so each
+// round takes every node's minimum by a segmented shuffle reduction; the
+// run that reaches lane 31 is carried into the next round, and only runs
+// that end issue an atomicMin (near the root a level has a few nodes of
+// millions of edges, and one atomic per edge on one address serialises in
+// L2).
+__device__ __forceinline__ void flush_best(LevelNodes L, uint32_t k, int a, unsigned long long ck) {
+  if (ck != kNone) atomicMin(L.best + 3 * (size_t)k + a, ck);
+}
+
+__global__ void __launch_bounds__(kThreads) k_cost(EdgeLists el, uint32_t E2, uint32_t runs_per_list, uint32_t M,
+                                                   LevelNodes L, uint32_t* err) {
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= 3 * runs_per_list) return;  // whole warps
+  const int lane = threadIdx.x & 31;
+  const int a = (int)(gw / runs_per_list);
+  const uint32_t run0 = (gw - (uint32_t)a * runs_per_list) * kEdgeRun;
   const uint32_t* __restrict__ tl = el.t(a);
   const uint32_t* __restrict__ vl = el.v(a);
-  uint32_t tk[kEdgeItems], vv[kEdgeItems], starts[kEdgeItems];
-  uint32_t total = 0;
-#pragma unroll
+  const uint32_t* __restrict__ nl = el.n(a);
+  const uint32_t* __restrict__ sl = el.s(a);
+  uint32_t carry_k = 0xFFFFFFFFu;  // the open run from the previous round (warp-uniform)
+  unsigned long long carry = kNone;
+#pragma unroll 2
   for (int j = 0; j < kEdgeItems; ++j) {
     const uint32_t e = run0 + 32 * j + lane;
     const bool in = e < E2;
-    tk[j] = in ? __ldg(tl + e) : 0u;
-    vv[j] = in ? __ldg(vl + e) : 1u;
-    starts[j] = __ballot_sync(0xffffffffu, in && !(vv[j] & 1u));
-    total += __popc(starts[j]);
-  }
-  uint32_t below_run = (uint32_t)tile_prefix(ts, total, status, err);
-  if (ts.fail) return;
-  const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int j = 0; j < kEdgeItems; ++j) {
-    const uint32_t e = run0 + 32 * j + lane;
-    const uint32_t r = vv[j] >> 1;
-    bool in = e < E2;
-    if (in && r >= R) { atomicOr(err, kErrCorrupt); in = false; }
-    uint32_t k = in ? __ldg(ref_node + r) : 0xFFFFFFFFu;
-    if (in && k >= M) { atomicOr(err, kErrCorrupt); in = false; k = 0xFFFFFFFFu; }
+    uint32_t k = in ? __ldg(nl + e) : 0xFFFFFFFFu;
+    if (in && k >= M) { atomicOr(err, kErrCorrupt); k = 0xFFFFFFFFu; }
     unsigned long long ck = kNone;
-    if (in && L.state[k] == 0) {
-      const float t = key_float(tk[j]);
+    if (k != 0xFFFFFFFFu && L.state[k] == 0) {
+      const float t = key_float(__ldg(tl + e));
       const float* b = L.box + 6 * (size_t)k;
       const float lo = b[a], hi = b[3 + a];
       if (t > lo && t < hi) {
         const uint32_t rs = L.rs[k], n = L.rc[k];
-        const uint32_t nBelow = below_run + __popc(starts[j] & lt) - rs;
+        const uint32_t nBelow = __ldg(sl + e);
         const uint32_t off = e - 2 * rs;
-        const uint32_t nEndIncl = off - nBelow + (vv[j] & 1u);
+        const uint32_t nEndIncl = off - nBelow + (__ldg(vl + e) & 1u);
         const uint32_t nAbove = n - nEndIncl;
-        float d[3] = {__fsub_rn(b[3], b[0]), __fsub_rn(b[4], b[1]), __fsub_rn(b[5], b[2])};
-        float totalSA = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[1]), __fmul_rn(d[0], d[2])),
-                                                  __fmul_rn(d[1], d[2])));
-        float invTotalSA = __fdiv_rn(1.f, totalSA);
-        const int o0 = (a + 1) % 3, o1 = (a + 2) % 3;
-        float dd = __fmul_rn(d[o0], d[o1]), ds = __fadd_rn(d[o0], d[o1]);
+        const float4 q = L.sa[k];
+        const float invTotalSA = q.w;
+        const float d0 = a == 0 ? q.y : a == 1 ? q.z : q.x;  // the other two axes, (a + 1) % 3 and (a + 2) % 3
+        const float d1 = a == 0 ? q.z : a == 1 ? q.x : q.y;
+        float dd = __fmul_rn(d0, d1), ds = __fadd_rn(d0, d1);
         float belowSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(t, lo), ds)));
         float aboveSA = __fmul_rn(2.f, __fadd_rn(dd, __fmul_rn(__fsub_rn(hi, t), ds)));
         float pB = __fmul_rn(belowSA, invTotalSA), pA = __fmul_rn(aboveSA, invTotalSA);
@@ -251,7 +187,6 @@ __global__ void __launch_bounds__(kThreads) k_cost(EdgeLists el, uint32_t E2, ui
         ck = ((unsigned long long)float_key(cost) << 32) | (unsigned long long)off;
       }
     }
-    below_run += __popc(starts[j]);
     // Minimum over the lane's run of equal nodes from this lane on.
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -260,15 +195,25 @@ __global__ void __launch_bounds__(kThreads) k_cost(EdgeLists el, uint32_t E2, ui
       if (lane + o < 32 && kk == k && x < ck) ck = x;
     }
     const uint32_t kprev = __shfl_up_sync(0xffffffffu, k, 1);
-    const bool head = in && (lane == 0 || kprev != k);
-    unsigned long long* slot = L.best + 3 * (size_t)k + a;
-    if (head && ck != kNone && __ldcg(slot) > ck) atomicMin(slot, ck);
+    const bool head = lane == 0 || kprev != k;
+    const uint32_t heads = __ballot_sync(0xffffffffu, head);
+    const int last = 31 - __clz(heads);  // head of the run that reaches lane 31
+    // the carried run continues into lane 0's run or ends here
+    const uint32_t k0 = __shfl_sync(0xffffffffu, k, 0);
+    if (lane == 0) {
+      if (carry_k == k0) { if (carry < ck) ck = carry; }
+      else if (carry_k != 0xFFFFFFFFu) flush_best(L, carry_k, a, carry);
+    }
+    if (head && lane != last && k != 0xFFFFFFFFu) flush_best(L, k, a, ck);
+    carry_k = __shfl_sync(0xffffffffu, k, last);
+    carry = __shfl_sync(0xffffffffu, ck, last);
   }
+  if (lane == 0 && carry_k != 0xFFFFFFFFu) flush_best(L, carry_k, a, carry);
 }
 
 // Split decision (:915-925): the first axis from the longest on with a
 // candidate edge; none -> leaf.
-__global__ void k_decide(LevelNodes L, uint32_t M) {
+__global__ void k_decide(EdgeLists el, LevelNodes L, uint32_t M, uint32_t E2, uint32_t* err) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= M || L.state[k] != 0) return;
   for (int q = 0; q < 3; ++q) {
@@ -282,110 +227,221 @@ __global__ void k_decide(LevelNodes L, uint32_t M) {
     const bool leaf = (bestCost > __fmul_rn(4.f, oldCost) && L.rc[k] < 16) || bad == 3;
     L.state[k] = leaf ? 1 : 2;
     L.best_axis[k] = a;
-    L.best_off[k] = (uint32_t)(b & 0xFFFFFFFFull);
+    const uint32_t off = (uint32_t)(b & 0xFFFFFFFFull), e = 2 * L.rs[k] + off;
+    L.best_off[k] = off;
+    if (e >= E2) { atomicOr(err, kErrCorrupt); L.state[k] = 1; return; }
+    const uint32_t key = el.t(a)[e];
+    L.split_key[k] = key;
+    L.split_v[k] = el.v(a)[e];
+    L.tsplit[k] = key_float(key);
     return;
   }
   L.state[k] = 1;  // no split found on any axis
 }
 
-// Below/above sides from the chosen axis's edges (:928-934): a ref whose
-// start edge precedes the split edge goes below, one whose end edge follows
-// it goes above.
-__global__ void k_classify(EdgeLists el, uint32_t E2, const uint32_t* __restrict__ ref_node, uint32_t M,
-                           LevelNodes L, uint32_t* __restrict__ below, uint32_t* __restrict__ above, uint32_t R,
-                           uint32_t* err) {
-  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= 3ull * E2) return;
-  const int a = (int)(g / E2);
-  const uint32_t e = (uint32_t)(g - (uint64_t)a * E2);
-  const uint32_t v = __ldg(el.v(a) + e), r = v >> 1;
-  if (r >= R) { atomicOr(err, kErrCorrupt); return; }
+// Below/above sides (:928-934): a ref whose start edge precedes the split
+// edge in the chosen axis's sorted order goes below, one whose end edge
+// follows it goes above.  The order is (t key, start before end, ref), so
+// the comparison needs only the ref's box and the split edge, not the list.
+__global__ void k_classify(const uint32_t* __restrict__ ref_prim, const uint32_t* __restrict__ ref_node,
+                           uint32_t R, uint32_t M, const float* __restrict__ aabb, LevelNodes L,
+                           uint32_t* __restrict__ below, uint32_t* __restrict__ above, uint32_t* err) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
   const uint32_t k = __ldg(ref_node + r);
   if (k >= M) { atomicOr(err, kErrCorrupt); return; }
-  if (L.state[k] != 2 || L.best_axis[k] != a) return;
-  const uint32_t off = e - 2 * L.rs[k], best = L.best_off[k];
-  if (v & 1u) above[r] = off > best ? 1u : 0u;
-  else below[r] = off < best ? 1u : 0u;
-  if (off == best) L.tsplit[k] = key_float(__ldg(el.t(a) + e));
+  if (L.state[k] != 2) return;
+  const int a = L.best_axis[k];
+  const uint32_t sk = L.split_key[k], sv = L.split_v[k], sr = sv >> 1;
+  const float* q = aabb + 6 * (size_t)__ldg(ref_prim + r);
+  const uint32_t lo = float_key(__ldg(q + a)), hi = float_key(__ldg(q + 3 + a));
+  below[r] = (lo < sk || (lo == sk && ((sv & 1u) || r < sr))) ? 1u : 0u;   // (lo, start, r) < split
+  above[r] = (hi > sk || (hi == sk && (!(sv & 1u) || r > sr))) ? 1u : 0u;  // (hi, end, r) > split
 }
 
 // Children's edge lists: a stable partition of every interior node's edges,
 // on each axis, into its below child (refs with below[r]) and above child
 // (refs with above[r]); straddling refs go to both.  With sB / sA the
-// exclusive scans of below / above over the level's refs and EB(e) / EA(e)
-// the list-wide counts of below / above edges before e:
-//   below child position  EB(e) + 2 sA[rs],        its ref  sA[rs] + sB[r]
-//   above child position  EA(e) + 2 sB[rs + rc],   its ref  sB[rs + rc] + sA[r]
-// (children are laid out node by node, below before above, and leaf refs
-// count in neither scan), matching k_emit_refs's numbering of the refs.
-__global__ void __launch_bounds__(kThreads) k_partition(EdgeLists el, uint32_t E2, uint32_t tiles_per_list,
-                                                        const uint32_t* __restrict__ ref_node, uint32_t R,
-                                                        uint32_t M, LevelNodes L,
-                                                        const uint32_t* __restrict__ below,
-                                                        const uint32_t* __restrict__ above,
-                                                        const uint32_t* __restrict__ sB,
-                                                        const uint32_t* __restrict__ sA, EdgeLists out,
-                                                        uint32_t E2next, unsigned long long* status,
-                                                        uint32_t* counter, uint32_t* err) {
-  __shared__ TileScan ts;
-  tile_claim(ts, counter, tiles_per_list);
+// exclusive scans of below / above over the level's refs, and BS, BE, AS, AE
+// the list-wide counts of below-start, below-end, above-start and above-end
+// edges before e:
+//   below child: position BS + BE + 2 sA[rs], ref sA[rs] + sB[r],
+//                start rank BS - sB[rs]
+//   above child: position AS + AE + 2 sB[re], ref sB[re] + sA[r],
+//                start rank AS - sA[rs]
+// (re = rs + rc; children are laid out node by node, below before above,
+// and leaf refs count in neither scan), matching k_emit_refs's numbering of
+// the refs.  Per node the bases come from plan[k] = (sA[rs], sB[rs], sB[re],
+// first child), written by k_spawn.
+//
+// Three passes, none waiting on another block: k_part_count counts each
+// tile's (BS, BE) and (AS, AE), packed 31 bits apiece in two 64-bit words
+// (lists hold fewer than 2^31 edges, so the fields never carry), and keeps
+// the side flags as one ballot word per 32 edges; k_part_scan turns the tile
+// counts of each list into exclusive prefixes; k_partition adds the warp
+// offsets inside the tile and scatters.
+__global__ void __launch_bounds__(kThreads) k_part_count(EdgeLists el, uint32_t E2, uint32_t tiles_per_list,
+                                                         uint32_t R, uint32_t M, const uint32_t* __restrict__ below,
+                                                         const uint32_t* __restrict__ above,
+                                                         uint32_t* __restrict__ sideB, uint32_t* __restrict__ sideA,
+                                                         unsigned long long* __restrict__ tile_cnt, uint32_t* err) {
+  __shared__ unsigned long long wsum[2][kThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int a = (int)ts.list;
-  const uint32_t run0 = ts.local * kEdgeTile + (uint32_t)warp * (32 * kEdgeItems);
-  uint32_t tk[kEdgeItems], vv[kEdgeItems], kb[kEdgeItems], ka[kEdgeItems];
-  unsigned long long total = 0;
+  const uint32_t tile = blockIdx.x, a = tile / tiles_per_list;
+  const uint32_t run0 = (tile - a * tiles_per_list) * kEdgeTile + (uint32_t)warp * kEdgeRun;
+  const size_t words = (size_t)(E2 + 31) / 32;  // ballot words per list
+  unsigned long long t0 = 0, t1 = 0;
 #pragma unroll
   for (int j = 0; j < kEdgeItems; ++j) {
     const uint32_t e = run0 + 32 * j + lane;
     const bool in = e < E2;
-    tk[j] = in ? __ldg(el.t(a) + e) : 0u;
-    vv[j] = in ? __ldg(el.v(a) + e) : 0u;
+    const uint32_t v = in ? __ldg(el.v(a) + e) : 0u;
     bool b = false, ab = false;
     if (in) {
-      const uint32_t r = vv[j] >> 1;
-      if (r < R) {
+      const uint32_t r = v >> 1, k = __ldg(el.n(a) + e);
+      if (r < R && k < M) {
         b = __ldg(below + r) != 0u;
         ab = __ldg(above + r) != 0u;
       } else {
         atomicOr(err, kErrCorrupt);
       }
     }
-    kb[j] = __ballot_sync(0xffffffffu, b);
-    ka[j] = __ballot_sync(0xffffffffu, ab);
-    total += ((unsigned long long)__popc(ka[j]) << 31) | (unsigned long long)__popc(kb[j]);
+    const uint32_t kb = __ballot_sync(0xffffffffu, b), ka = __ballot_sync(0xffffffffu, ab);
+    const uint32_t em = __ballot_sync(0xffffffffu, (v & 1u) != 0u);
+    const uint32_t w = (run0 >> 5) + (uint32_t)j;
+    if (lane == 0 && w < words) {
+      sideB[(size_t)a * words + w] = kb;
+      sideA[(size_t)a * words + w] = ka;
+    }
+    t0 += ((unsigned long long)__popc(kb & em) << 31) | (unsigned long long)__popc(kb & ~em);
+    t1 += ((unsigned long long)__popc(ka & em) << 31) | (unsigned long long)__popc(ka & ~em);
   }
-  const unsigned long long pre = tile_prefix(ts, total, status, err);
-  if (ts.fail) return;
-  uint32_t eb = (uint32_t)(pre & 0x7FFFFFFFull), ea = (uint32_t)(pre >> 31);
-  const uint32_t lt = (1u << lane) - 1u;
+  if (lane == 0) {
+    wsum[0][warp] = t0;
+    wsum[1][warp] = t1;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    unsigned long long x = 0;
+    for (int w = 0; w < kThreads / 32; ++w) x += wsum[threadIdx.x][w];
+    tile_cnt[2 * (size_t)tile + threadIdx.x] = x;
+  }
+}
+
+// Exclusive prefix of the tile counts of list blockIdx.x, both words, in
+// place (one block per list; each thread sums a contiguous chunk).
+__global__ void __launch_bounds__(1024) k_part_scan(unsigned long long* tile_cnt, uint32_t tiles_per_list) {
+  __shared__ unsigned long long part[2][1024];
+  const uint32_t t = threadIdx.x, per = (tiles_per_list + 1023) / 1024;
+  unsigned long long* c = tile_cnt + 2 * (size_t)blockIdx.x * tiles_per_list;
+  const uint32_t lo = t * per, hi = min(lo + per, tiles_per_list);
+  unsigned long long s0 = 0, s1 = 0;
+  for (uint32_t i = lo; i < hi; ++i) {
+    s0 += c[2 * (size_t)i];
+    s1 += c[2 * (size_t)i + 1];
+  }
+  part[0][t] = s0;
+  part[1][t] = s1;
+  __syncthreads();
+  for (uint32_t o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan of the chunk sums
+    const unsigned long long x0 = t >= o ? part[0][t - o] : 0ull, x1 = t >= o ? part[1][t - o] : 0ull;
+    __syncthreads();
+    part[0][t] += x0;
+    part[1][t] += x1;
+    __syncthreads();
+  }
+  unsigned long long r0 = part[0][t] - s0, r1 = part[1][t] - s1;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const unsigned long long v0 = c[2 * (size_t)i], v1 = c[2 * (size_t)i + 1];
+    c[2 * (size_t)i] = r0;
+    c[2 * (size_t)i + 1] = r1;
+    r0 += v0;
+    r1 += v1;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_partition(EdgeLists el, uint32_t E2, uint32_t tiles_per_list,
+                                                        LevelNodes L, const uint32_t* __restrict__ sideB,
+                                                        const uint32_t* __restrict__ sideA,
+                                                        const unsigned long long* __restrict__ tile_pre,
+                                                        const uint32_t* __restrict__ sB,
+                                                        const uint32_t* __restrict__ sA, EdgeLists out,
+                                                        uint32_t E2next, uint32_t* err) {
+  __shared__ unsigned long long wpre[2][kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t tile = blockIdx.x, a = tile / tiles_per_list;
+  const uint32_t run0 = (tile - a * tiles_per_list) * kEdgeTile + (uint32_t)warp * kEdgeRun;
+  const size_t words = (size_t)(E2 + 31) / 32;
+  // Side-flag words and end-edge ballots of round j (read twice: for the
+  // warp totals, then for the scatter; the second read hits the cache).
+  auto round_flags = [&](int j, uint32_t& kb, uint32_t& ka, uint32_t& em, uint32_t& v) {
+    const uint32_t e = run0 + 32 * j + lane;
+    const uint32_t w = (run0 >> 5) + (uint32_t)j;
+    const bool wv = w < words;
+    kb = wv ? __ldg(sideB + (size_t)a * words + w) : 0u;
+    ka = wv ? __ldg(sideA + (size_t)a * words + w) : 0u;
+    v = e < E2 ? __ldg(el.v(a) + e) : 0u;
+    em = __ballot_sync(0xffffffffu, (v & 1u) != 0u);
+  };
+  unsigned long long t0 = 0, t1 = 0;
 #pragma unroll
   for (int j = 0; j < kEdgeItems; ++j) {
-    const bool b = (kb[j] >> lane) & 1u, ab = (ka[j] >> lane) & 1u;
-    const uint32_t r = vv[j] >> 1, end = vv[j] & 1u;
-    const uint32_t k = (b || ab) ? __ldg(ref_node + r) : 0u;
-    if ((b || ab) && k >= M) {
-      atomicOr(err, kErrCorrupt);
-    } else if (b || ab) {
-      const uint32_t rs = L.rs[k], re = rs + L.rc[k];
+    uint32_t kb, ka, em, v;
+    round_flags(j, kb, ka, em, v);
+    t0 += ((unsigned long long)__popc(kb & em) << 31) | (unsigned long long)__popc(kb & ~em);
+    t1 += ((unsigned long long)__popc(ka & em) << 31) | (unsigned long long)__popc(ka & ~em);
+  }
+  if (lane == 0) {
+    wpre[0][warp] = t0;
+    wpre[1][warp] = t1;
+  }
+  __syncthreads();
+  unsigned long long p0 = __ldg(tile_pre + 2 * (size_t)tile), p1 = __ldg(tile_pre + 2 * (size_t)tile + 1);
+  for (int w = 0; w < warp; ++w) {
+    p0 += wpre[0][w];
+    p1 += wpre[1][w];
+  }
+  uint32_t cbs = (uint32_t)(p0 & 0x7FFFFFFFull), cbe = (uint32_t)(p0 >> 31);
+  uint32_t cas = (uint32_t)(p1 & 0x7FFFFFFFull), cae = (uint32_t)(p1 >> 31);
+  const uint32_t lt = (1u << lane) - 1u, me = 1u << lane;
+#pragma unroll 1
+  for (int j = 0; j < kEdgeItems; ++j) {
+    uint32_t kb, ka, em, v;
+    round_flags(j, kb, ka, em, v);
+    const uint32_t bs = kb & ~em, be = kb & em, as = ka & ~em, ae = ka & em;
+    const bool b = (kb & me) != 0u, ab = (ka & me) != 0u;
+    if (b || ab) {
+      const uint32_t e = run0 + 32 * j + lane;
+      const uint32_t tk = __ldg(el.t(a) + e), k = __ldg(el.n(a) + e);
+      const uint32_t r = v >> 1, end = v & 1u;
+      const uint4 pl = L.plan[k];  // (sA[rs], sB[rs], sB[re], first child)
       if (b) {
-        const uint32_t pos = eb + __popc(kb[j] & lt) + 2 * __ldg(sA + rs);
+        const uint32_t nbs = cbs + __popc(bs & lt), nbe = cbe + __popc(be & lt);
+        const uint32_t pos = nbs + nbe + 2 * pl.x;
         if (pos >= E2next) { atomicOr(err, kErrCorrupt); }
         else {
-          out.t(a)[pos] = tk[j];
-          out.v(a)[pos] = ((__ldg(sA + rs) + __ldg(sB + r)) << 1) | end;
+          out.t(a)[pos] = tk;
+          out.v(a)[pos] = ((pl.x + __ldg(sB + r)) << 1) | end;
+          out.n(a)[pos] = pl.w;
+          out.s(a)[pos] = nbs - pl.y;
         }
       }
       if (ab) {
-        const uint32_t pos = ea + __popc(ka[j] & lt) + 2 * __ldg(sB + re);
+        const uint32_t nas = cas + __popc(as & lt), nae = cae + __popc(ae & lt);
+        const uint32_t pos = nas + nae + 2 * pl.z;
         if (pos >= E2next) { atomicOr(err, kErrCorrupt); }
         else {
-          out.t(a)[pos] = tk[j];
-          out.v(a)[pos] = ((__ldg(sB + re) + __ldg(sA + r)) << 1) | end;
+          out.t(a)[pos] = tk;
+          out.v(a)[pos] = ((pl.z + __ldg(sA + r)) << 1) | end;
+          out.n(a)[pos] = pl.w + 1;
+          out.s(a)[pos] = nas - pl.x;
         }
       }
     }
-    eb += __popc(kb[j]);
-    ea += __popc(ka[j]);
+    cbs += __popc(bs);
+    cbe += __popc(be);
+    cas += __popc(as);
+    cae += __popc(ae);
   }
 }
 
@@ -441,6 +497,7 @@ __global__ void k_spawn(LevelNodes L, uint32_t M, const uint32_t* __restrict__ i
   }
   child_cnt[c] = sB[rs + rc] - sB[rs];
   child_cnt[c + 1] = sA[rs + rc] - sA[rs];
+  L.plan[k] = make_uint4(sA[rs], sB[rs], sB[rs + rc], c);
 }
 
 __global__ void k_set_ref_starts(LevelNodes N, uint32_t M2, const uint32_t* __restrict__ child_cnt,
@@ -732,9 +789,13 @@ LevelNodes carve(char* base, uint32_t cap) {
   L.best_axis = (int32_t*)take((size_t)cap * 4);
   L.best_off = (uint32_t*)take((size_t)cap * 4);
   L.tsplit = (float*)take((size_t)cap * 4);
+  L.split_key = (uint32_t*)take((size_t)cap * 4);
+  L.split_v = (uint32_t*)take((size_t)cap * 4);
+  L.sa = (float4*)take((size_t)cap * 16);
+  L.plan = (uint4*)take((size_t)cap * 16);
   return L;
 }
-size_t level_bytes(uint32_t cap) { return (size_t)cap * 84 + 12 * 256; }
+size_t level_bytes(uint32_t cap) { return (size_t)cap * 124 + 16 * 256; }
 
 Table table_at(char* base, uint32_t cap) {
   Table T;
@@ -807,7 +868,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
   // root edge lists, one per axis, each sorted once by t (stable: equal t
   // start-first, then by primitive id)
   const uint32_t E0 = 2 * n;
-  KD_TRY(sc.keys.ensure((size_t)E0 * 6 * 4 + 64), "KD edges");
+  KD_TRY(sc.keys.ensure((size_t)E0 * kEdgeWords * 4 + 64), "KD edges");
   KD_TRY(sc.vals.ensure((size_t)E0 * 2 * 4 + 64), "KD edges");
   EdgeLists el{sc.keys.as<uint32_t>(), (size_t)E0};
   {
@@ -821,6 +882,12 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
       KD_TRY(cudaMemsetAsync(zero, 0, zwords * 4, st), "KD sort");
       launch_histogram(el.t(ax), E0, 4, zero, st);
       launch_onesweep(el.t(ax), el.v(ax), E0, 4, ss, err, st);
+    }
+    for (int ax = 0; ax < 3; ++ax) {
+      KD_TRY(cudaMemsetAsync(el.n(ax), 0, (size_t)E0 * 4, st), "KD root edges");
+      count_launch();
+      k_start_flags<<<grid(E0), kThreads, 0, st>>>(el.v(ax), E0, el.s(ax));
+      launch_scan_excl(el.s(ax), el.s(ax), E0, sc.vals.as<uint32_t>(), nullptr, st);  // in place
     }
     KD_TRY(cudaGetLastError(), "KD root edges");
   }
@@ -876,26 +943,23 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     uint32_t* sA = sB + (R + 1);
     uint32_t* tmp = sA + (R + 1);
     KD_TRY(cudaMemsetAsync(below, 0, ((size_t)R + 1) * 8, st), "KD flags");  // below + above
-    // look-back words of the two edge passes and their tile counters
+    // partition scratch: tile counts and the side flags as ballot words
     const uint32_t E2 = 2 * R;
-    const uint32_t tiles = (E2 + kEdgeTile - 1) / kEdgeTile;
-    const size_t zbytes = (size_t)tiles * 3 * 8 * 2 + 64;
-    KD_TRY(sc.m4.ensure(zbytes), "KD edges");
-    unsigned long long* status = sc.m4.as<unsigned long long>();
-    uint32_t* counters = reinterpret_cast<uint32_t*>(status + (size_t)tiles * 3 * 2);
-    KD_TRY(cudaMemsetAsync(status, 0, zbytes, st), "KD edges");
+    const uint32_t runs = (E2 + kEdgeRun - 1) / kEdgeRun, tiles = (E2 + kEdgeTile - 1) / kEdgeTile;
+    const size_t words = ((size_t)E2 + 31) / 32;
+    KD_TRY(sc.m4.ensure((size_t)tiles * 3 * 16 + words * 3 * 8 + 64), "KD edges");
+    unsigned long long* tile_cnt = sc.m4.as<unsigned long long>();
+    uint32_t* sideB = reinterpret_cast<uint32_t*>(tile_cnt + (size_t)tiles * 3 * 2);
+    uint32_t* sideA = sideB + words * 3;
     count_launch();
     k_node_init<<<grid(M), kThreads, 0, st>>>(L, M);
     if (E2) {
       count_launch();
-      k_cost<<<3 * tiles, kThreads, 0, st>>>(el, E2, tiles, ref_node, R, M, L, status, counters, err);
+      k_cost<<<grid(3ull * runs * 32), kThreads, 0, st>>>(el, E2, runs, M, L, err);
     }
-    count_launch();
-    k_decide<<<grid(M), kThreads, 0, st>>>(L, M);
-    if (E2) {
-      count_launch();
-      k_classify<<<grid(3ull * E2), kThreads, 0, st>>>(el, E2, ref_node, M, L, below, above, R, err);
-    }
+    count_launch(2);
+    k_decide<<<grid(M), kThreads, 0, st>>>(el, L, M, E2, err);
+    k_classify<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, M, aabb, L, below, above, err);
     KD_TRY(cudaGetLastError(), "KD split");
     // interior ranks, leaf pool offsets, children's ref counts
     KD_TRY(sc.m7.ensure(((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 4 + 64), "KD scratch");
@@ -951,12 +1015,13 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
                                               (uint32_t)(poolbuf.cap / 4), err);
     KD_TRY(cudaGetLastError(), "KD emit");
     // the children's edge lists
-    KD_TRY(sc.vals.ensure((size_t)R2 * 2 * 6 * 4 + 64), "KD edges");
+    KD_TRY(sc.vals.ensure((size_t)R2 * 2 * kEdgeWords * 4 + 64), "KD edges");
     EdgeLists eln{sc.vals.as<uint32_t>(), (size_t)R2 * 2};
     if (E2 && R2) {
-      count_launch();
-      k_partition<<<3 * tiles, kThreads, 0, st>>>(el, E2, tiles, ref_node, R, M, L, below, above, sB, sA, eln, 2 * R2,
-                                                  status + (size_t)tiles * 3, counters + 1, err);
+      count_launch(3);
+      k_part_count<<<3 * tiles, kThreads, 0, st>>>(el, E2, tiles, R, M, below, above, sideB, sideA, tile_cnt, err);
+      k_part_scan<<<3, 1024, 0, st>>>(tile_cnt, tiles);
+      k_partition<<<3 * tiles, kThreads, 0, st>>>(el, E2, tiles, L, sideB, sideA, tile_cnt, sB, sA, eln, 2 * R2, err);
       KD_TRY(cudaGetLastError(), "KD partition");
     }
     pool_used += leaf_refs;
