@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(kThreads) k_partition(EdgeLists el, uint32_t E
   uint32_t cbs = (uint32_t)(p0 & 0x7FFFFFFFull), cbe = (uint32_t)(p0 >> 31);
   uint32_t cas = (uint32_t)(p1 & 0x7FFFFFFFull), cae = (uint32_t)(p1 >> 31);
   const uint32_t lt = (1u << lane) - 1u, me = 1u << lane;
-#pragma unroll 1
+#pragma unroll 2
   for (int j = 0; j < kEdgeItems; ++j) {
     uint32_t kb, ka, em, v;
     round_flags(j, kb, ka, em, v);
@@ -445,10 +445,13 @@ __global__ void __launch_bounds__(kThreads) k_partition(EdgeLists el, uint32_t E
   }
 }
 
-__global__ void k_flag_of_state(LevelNodes L, uint32_t M, int want, uint32_t* __restrict__ out, int with_count) {
+// Interior flag and leaf ref count of every node (M + 1 entries, last 0).
+__global__ void k_node_flags(LevelNodes L, uint32_t M, uint32_t* __restrict__ iflag, uint32_t* __restrict__ lcnt) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k > M) return;
-  out[k] = (k < M && L.state[k] == want) ? (with_count ? L.rc[k] : 1u) : 0u;
+  const int st = k < M ? L.state[k] : 0;
+  iflag[k] = st == 2 ? 1u : 0u;
+  lcnt[k] = st == 1 ? L.rc[k] : 0u;
 }
 
 // Global node table (breadth-first ids).
@@ -936,7 +939,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     }
     Table T = table_at(tabbuf.as<char>(), table_cap);
     // per-ref scratch: below / above flags and their scans (R + 1 each)
-    KD_TRY(sc.m2.ensure(((size_t)R + 1) * 4 * 4 + scan_tmp_words((uint64_t)R + 1) * 4 + 64), "KD scratch");
+    KD_TRY(sc.m2.ensure(((size_t)R + 1) * 4 * 4 + scan_tmp_words((uint64_t)R + 1) * 8 + 64), "KD scratch");
     uint32_t* below = sc.m2.as<uint32_t>();
     uint32_t* above = below + (R + 1);
     uint32_t* sB = above + (R + 1);
@@ -962,20 +965,17 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     k_classify<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, M, aabb, L, below, above, err);
     KD_TRY(cudaGetLastError(), "KD split");
     // interior ranks, leaf pool offsets, children's ref counts
-    KD_TRY(sc.m7.ensure(((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 4 + 64), "KD scratch");
+    KD_TRY(sc.m7.ensure(((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 8 + 64), "KD scratch");
     uint32_t* iflag = sc.m7.as<uint32_t>();
     uint32_t* irank = iflag + (M + 1);
     uint32_t* lcnt = irank + (M + 1);
     uint32_t* lofs = lcnt + (M + 1);
     uint32_t* mtmp = lofs + (M + 1);
-    uint32_t* mtot = mtmp + scan_tmp_words((uint64_t)M + 1) + 4;  // 4 totals
-    count_launch(2);
-    k_flag_of_state<<<grid(M + 1), kThreads, 0, st>>>(L, M, 2, iflag, 0);
-    launch_scan_excl(iflag, irank, (uint64_t)M + 1, mtmp, mtot, st);
-    k_flag_of_state<<<grid(M + 1), kThreads, 0, st>>>(L, M, 1, lcnt, 1);
-    launch_scan_excl(lcnt, lofs, (uint64_t)M + 1, mtmp, mtot + 1, st);
-    launch_scan_excl(below, sB, (uint64_t)R + 1, tmp, mtot + 2, st);
-    launch_scan_excl(above, sA, (uint64_t)R + 1, tmp, mtot + 3, st);
+    uint32_t* mtot = mtmp + 2 * scan_tmp_words((uint64_t)M + 1) + 4;  // 4 totals
+    count_launch();
+    k_node_flags<<<grid(M + 1), kThreads, 0, st>>>(L, M, iflag, lcnt);
+    launch_scan2_excl(iflag, irank, lcnt, lofs, (uint64_t)M + 1, mtmp, mtot, mtot + 1, st);
+    launch_scan2_excl(below, sB, above, sA, (uint64_t)R + 1, tmp, mtot + 2, mtot + 3, st);
     uint32_t h_tot[4] = {0, 0, 0, 0};
     KD_TRY(cudaMemcpyAsync(h_tot, mtot, 16, cudaMemcpyDeviceToHost, st), "KD level");
     KD_TRY(cudaStreamSynchronize(st), "KD level");

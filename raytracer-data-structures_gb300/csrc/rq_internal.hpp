@@ -123,6 +123,10 @@ void launch_prims_gather(int kind, const float* verts, const uint32_t* idx, cons
 size_t scan_tmp_words(uint64_t n);
 void launch_scan_excl(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp, uint32_t* total,
                       cudaStream_t s);
+// Two arrays of the same length in one set of launches; tmp holds
+// 2 * scan_tmp_words(n) words; either total may be null.
+void launch_scan2_excl(const uint32_t* in0, uint32_t* out0, const uint32_t* in1, uint32_t* out1, uint64_t n,
+                       uint32_t* tmp, uint32_t* total0, uint32_t* total1, cudaStream_t s);
 
 // ------------------------------------------------------------ traversal
 struct Bvh2View {
