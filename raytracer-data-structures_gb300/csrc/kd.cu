@@ -770,6 +770,14 @@ cudaError_t grow_keep(DevBuf& b, size_t bytes, size_t used, cudaStream_t st) {
   return cudaSuccess;
 }
 
+// Grow a scratch buffer that queued kernels may still read: wait for them
+// first (the level loop does not otherwise wait at the end of a level).
+cudaError_t ensure_after(DevBuf& b, size_t bytes, cudaStream_t st) {
+  if (bytes <= b.cap && b.p) return cudaSuccess;
+  const cudaError_t e = cudaStreamSynchronize(st);
+  return e != cudaSuccess ? e : b.ensure(bytes);
+}
+
 #define KD_TRY(call, what)                                           \
   do {                                                               \
     cudaError_t e_ = (call);                                         \
@@ -939,7 +947,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     }
     Table T = table_at(tabbuf.as<char>(), table_cap);
     // per-ref scratch: below / above flags and their scans (R + 1 each)
-    KD_TRY(sc.m2.ensure(((size_t)R + 1) * 4 * 4 + scan_tmp_words((uint64_t)R + 1) * 8 + 64), "KD scratch");
+    KD_TRY(ensure_after(sc.m2, ((size_t)R + 1) * 4 * 4 + scan_tmp_words((uint64_t)R + 1) * 8 + 64, st), "KD scratch");
     uint32_t* below = sc.m2.as<uint32_t>();
     uint32_t* above = below + (R + 1);
     uint32_t* sB = above + (R + 1);
@@ -950,7 +958,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     const uint32_t E2 = 2 * R;
     const uint32_t runs = (E2 + kEdgeRun - 1) / kEdgeRun, tiles = (E2 + kEdgeTile - 1) / kEdgeTile;
     const size_t words = ((size_t)E2 + 31) / 32;
-    KD_TRY(sc.m4.ensure((size_t)tiles * 3 * 16 + words * 3 * 8 + 64), "KD edges");
+    KD_TRY(ensure_after(sc.m4, (size_t)tiles * 3 * 16 + words * 3 * 8 + 64, st), "KD edges");
     unsigned long long* tile_cnt = sc.m4.as<unsigned long long>();
     uint32_t* sideB = reinterpret_cast<uint32_t*>(tile_cnt + (size_t)tiles * 3 * 2);
     uint32_t* sideA = sideB + words * 3;
@@ -965,7 +973,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     k_classify<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, M, aabb, L, below, above, err);
     KD_TRY(cudaGetLastError(), "KD split");
     // interior ranks, leaf pool offsets, children's ref counts
-    KD_TRY(sc.m7.ensure(((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 8 + 64), "KD scratch");
+    KD_TRY(ensure_after(sc.m7, ((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 8 + 64, st), "KD scratch");
     uint32_t* iflag = sc.m7.as<uint32_t>();
     uint32_t* irank = iflag + (M + 1);
     uint32_t* lcnt = irank + (M + 1);
@@ -986,7 +994,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     // next level nodes and child ref counts
     const uint32_t M2 = 2 * interiors;
     DevBuf& nextbuf = (level & 1) ? sc.m3 : sc.keys_alt;  // alternate level buffers
-    KD_TRY(nextbuf.ensure(level_bytes(M2 ? M2 : 1) + ((size_t)M2 + 1) * 8 + scan_tmp_words((uint64_t)M2 + 1) * 4 + 64),
+    KD_TRY(ensure_after(nextbuf, level_bytes(M2 ? M2 : 1) + ((size_t)M2 + 1) * 8 + scan_tmp_words((uint64_t)M2 + 1) * 4 + 64, st),
            "KD scratch");
     LevelNodes N = carve(nextbuf.as<char>(), M2 ? M2 : 1);
     uint32_t* ccnt = reinterpret_cast<uint32_t*>(nextbuf.as<char>() + level_bytes(M2 ? M2 : 1));
@@ -1006,7 +1014,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
       k_set_ref_starts<<<grid(M2), kThreads, 0, st>>>(N, M2, ccnt, coff);
     }
     // refs of the next level (separate buffer), leaf refs to the pool
-    KD_TRY(sc.kd_refs.ensure(((size_t)R2 + 1) * 8), "KD refs");
+    KD_TRY(ensure_after(sc.kd_refs, ((size_t)R2 + 1) * 8, st), "KD refs");
     uint32_t* out_prim = sc.kd_refs.as<uint32_t>();
     uint32_t* out_node = out_prim + (R2 + 1);
     count_launch();
@@ -1015,7 +1023,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
                                               (uint32_t)(poolbuf.cap / 4), err);
     KD_TRY(cudaGetLastError(), "KD emit");
     // the children's edge lists
-    KD_TRY(sc.vals.ensure((size_t)R2 * 2 * kEdgeWords * 4 + 64), "KD edges");
+    KD_TRY(ensure_after(sc.vals, (size_t)R2 * 2 * kEdgeWords * 4 + 64, st), "KD edges");
     EdgeLists eln{sc.vals.as<uint32_t>(), (size_t)R2 * 2};
     if (E2 && R2) {
       count_launch(3);
@@ -1026,7 +1034,6 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     }
     pool_used += leaf_refs;
     total += M;
-    KD_TRY(cudaStreamSynchronize(st), "KD level");
     std::swap(sc.m1, sc.kd_refs);  // the children's refs become the current refs
     std::swap(sc.keys, sc.vals);   // and their edge lists
     el = EdgeLists{sc.keys.as<uint32_t>(), (size_t)R2 * 2};
@@ -1040,7 +1047,7 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
   level_lo.push_back(total);
   Table T = table_at(tabbuf.as<char>(), table_cap);
   // size, pos, cnt, off: four arrays of total + 2 words
-  KD_TRY(sc.m7.ensure(((size_t)total + 2) * 16 + scan_tmp_words((uint64_t)total + 2) * 4 + 64), "KD layout");
+  KD_TRY(ensure_after(sc.m7, ((size_t)total + 2) * 16 + scan_tmp_words((uint64_t)total + 2) * 4 + 64, st), "KD layout");
   uint32_t* size = sc.m7.as<uint32_t>();
   uint32_t* pos = size + (total + 1);
   uint32_t* cnt = pos + (total + 1);
