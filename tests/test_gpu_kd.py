@@ -105,3 +105,19 @@ def test_kd_degenerate_inputs(engine, oracle, rqm):
         nodes, pidx, root, info = engine.export_kd(acc)
         ref = oracle.build_kd(oracle.sphere_prims(sph)[0])
         _check_nodes(nodes, pidx, ref.nodes, ref.prim_idx)
+
+
+def test_kd_full_size_terrain_matches_oracle(engine, oracle, rqm):
+    """The benchmark's 998,000-triangle terrain: about 30 levels, up to 2.4M refs
+    a level, so the edge-list partition runs with more than 1024 tiles a list and
+    every pass of the level loop at full width.  Rebuilt once more: same tree."""
+    v, f = scenes.heightfield(1001, 500, amplitude=0.3, octaves=5, seed=1)
+    s = engine.scene_triangles(v, f)
+    acc = engine.build(s, rqm.KDTREE)
+    nodes, pidx, root, info = engine.export_kd(acc)
+    _, aabb, _ = oracle.tri_prims(v, f)
+    ref = oracle.build_kd(aabb)
+    _check_nodes(nodes, pidx, ref.nodes, ref.prim_idx)
+    acc.rebuild()
+    nodes2, pidx2, _, _ = engine.export_kd(acc)
+    assert np.array_equal(nodes2, nodes) and np.array_equal(pidx2, pidx)

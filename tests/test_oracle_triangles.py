@@ -66,3 +66,22 @@ def test_stable_sort_order(oracle):
     k, v = oracle.sort_pairs(keys)
     assert np.array_equal(v, np.argsort(keys, kind="stable"))
     assert np.array_equal(k, keys[v])
+
+
+def test_lbvh_closest_equals_brute_force_on_terrain(oracle):
+    """A flat terrain seen by a camera and by diffuse bounce rays: thin boxes and
+    hits just inside a box's entry face, where a box bound that is not the slab
+    test's own widened bound drops hits.  The FAST walk must still equal brute
+    force bit for bit."""
+    v, f = scenes.heightfield(161, 80, amplitude=0.3, octaves=5, seed=5)
+    prims, aabb, cen = oracle.tri_prims(v, f)
+    lo, hi = oracle.bounds3(v)
+    codes = oracle.morton_centroids(cen, lo, hi)
+    bvh = oracle.build_lbvh(codes, aabb)
+    cam = scenes.pinhole_rays(160, 120, 2, eye=(0.5, -1.2, 1.0), target=(0.5, 0.25, 0.0), seed=6)
+    hc = oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, prims, cam)
+    bounce = scenes.cosine_rays(v, f, cam, hc, seed=7)
+    for rays, want in ((cam, hc), (bounce, oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST,
+                                                              prims, bounce))):
+        got = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, bvh, prims, rays)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
