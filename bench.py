@@ -947,8 +947,10 @@ def run_case(args):
     """Profiling driver (no bench line): one query class of the benchmark
     workload run warmup + steps times, for ncu captures of a single kernel.
     Cases: primary, secondary, shadow (the LBVH traversal kernels, with
-    --ray-sort 0/1), build (the LBVH rebuild), batched (the many-structure
-    persistent query on the many-scene workload, 32 scenes with --small)."""
+    --ray-sort 0/1), build (the LBVH rebuild), build-bvh / build-kd (the median
+    BVH and SAH KD rebuilds of the same mesh), batched (the many-structure
+    persistent query on the many-scene workload, 32 scenes with --small),
+    build-batched (the batched LBVH rebuild of the same scenes)."""
     import torch
     import rq
     import scenes
@@ -959,7 +961,7 @@ def run_case(args):
     eng = rq.Engine(0)
     eng.set_stream(stream.cuda_stream)
     eng.configure(morton=rq.MORTON_SCENE_CUBE)  # the tuner's build choice (see --no-tune)
-    if args.case == "batched":
+    if args.case in ("batched", "build-batched"):
         rng = np.random.default_rng(SEED + 40)
         n_sc = 32 if args.small else 256
         tri_t = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_sc))
@@ -974,12 +976,14 @@ def run_case(args):
         d_rays = batch_rays(torch, dev, meshes, ray_n.tolist(), SEED + 41)
         d_hits = torch.empty(int(offs[-1]) * HIT_BYTES, dtype=torch.uint8, device=dev)
         call = lambda: eng.trace_batched(accs, d_rays, offs, out=d_hits)  # noqa: E731
+        if args.case == "build-batched":
+            call = lambda: eng.rebuild_batched(accs)  # noqa: E731
     else:
         verts, idx, primary = make_inputs(args.small)
         scene = eng.scene_triangles(verts, idx)
         acc = eng.build(scene, rq.LBVH)
         hits_p = eng.trace_closest(acc, primary)
-        rays = {"primary": primary, "build": primary,
+        rays = {"primary": primary, "build": primary, "build-bvh": primary, "build-kd": primary,
                 "secondary": scenes.cosine_rays(verts, idx, primary, hits_p, seed=SEED + 2),
                 "shadow": scenes.shadow_rays(verts, idx, primary, hits_p, LIGHT)}[args.case]
         d_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8)).to(dev)
@@ -987,6 +991,9 @@ def run_case(args):
         eng.configure(ray_sort=args.ray_sort, scheduling=args.scheduling)
         if args.case == "build":
             call = acc.rebuild
+        elif args.case in ("build-bvh", "build-kd"):
+            other = eng.build(scene, rq.BVH if args.case == "build-bvh" else rq.KDTREE)
+            call = other.rebuild
         elif args.case == "shadow":
             call = lambda: eng.trace_any(acc, d_rays, d_out)  # noqa: E731
         else:
@@ -1012,7 +1019,8 @@ def main():
     ap.add_argument("--skip-render", action="store_true", help="skip the render-step legs")
     ap.add_argument("--skip-batch", action="store_true", help="skip the many-scene leg")
     ap.add_argument("--skip-serve", action="store_true", help="skip the serving-loop leg")
-    ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "batched"],
+    ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "build-bvh", "build-kd",
+                                       "batched", "build-batched"],
                     help="profiling driver: run one query class, print no bench line")
     ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
     ap.add_argument("--scheduling", type=int, default=0, help="--case: settings.scheduling (0-3)")
