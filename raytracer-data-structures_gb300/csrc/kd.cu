@@ -8,15 +8,16 @@
 // traversalCost = 1, emptyBonus = 0 (the global `char emptyBonus = 0.5f`
 // truncates, accelerators.h:767-770); maxDepth = round(8 + 1.3 log2 N).
 //
-// Per level, for every node still splitting:
-//  * its primitive list is kept sorted by id, so a stable sort of its edges by
-//    (node, t, start-before-end) orders ties by primitive id;
-//  * two prefix sums give nBelow / nAbove at every edge and the SAH cost is
-//    evaluated with the reference's float operations (no fused multiply-add);
-//  * a 64-bit atomicMin of (cost, edge index) per node takes the first
-//    cheapest edge (buildTree's strict <);
-//  * a node with no candidate on its longest axis retries the next axis, up
-//    to twice (:915-919), in further passes over only those nodes;
+// Edges are sorted once: at the root, one list per axis, ordered by (t,
+// start before end, primitive id), the order of buildTree's edge sort
+// (:872-879) with ties in id order.  A node's edges are a contiguous segment
+// of each list, and a stable partition hands every child its segments still
+// sorted.  Per level, for every node still splitting:
+//  * the SAH cost of every edge on every axis, with the reference's float
+//    operations (no fused multiply-add); nBelow is carried with each edge;
+//  * per node and axis, a 64-bit atomicMin of (cost, edge offset) takes the
+//    first cheapest edge (buildTree's strict <); the axis is the first from
+//    the longest on with a candidate edge, as the retries (:915-919) choose;
 //  * the leaf rules (maxPrims, depth, 4x old cost under 16 primitives, three
 //    bad refines, :843, :920-925) decide; primitives whose start edge precedes
 //    the split go below, those whose end edge follows it go above (:928-934).
