@@ -85,9 +85,15 @@ struct EdgeLists {
 };
 constexpr int kEdgeWords = 12;  // t, v, node and start-rank arrays of the three lists
 
-// Pre-leaf test and first axis (:843, :860).
-__global__ void k_node_init(LevelNodes L, uint32_t M) {
+// Pre-leaf test and first axis (:843, :860); also clears the level's ref
+// side flags (R + 1 each).
+__global__ void k_node_init(LevelNodes L, uint32_t M, uint32_t* __restrict__ below, uint32_t* __restrict__ above,
+                            uint32_t R) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k <= R) {
+    below[k] = 0u;
+    above[k] = 0u;
+  }
   if (k >= M) return;
   const float* b = L.box + 6 * (size_t)k;
   for (int a = 0; a < 3; ++a) L.best[3 * (size_t)k + a] = kNone;
@@ -214,9 +220,26 @@ __global__ void __launch_bounds__(kThreads) k_cost(EdgeLists el, uint32_t E2, ui
 
 // Split decision (:915-925): the first axis from the longest on with a
 // candidate edge; none -> leaf.
-__global__ void k_decide(EdgeLists el, LevelNodes L, uint32_t M, uint32_t E2, uint32_t* err) {
+__device__ void decide_node(EdgeLists el, LevelNodes L, uint32_t k, uint32_t E2, uint32_t* err);
+
+// Decides every undecided node, then writes each node's interior flag and
+// leaf ref count (M + 1 entries, the last 0) for the level's scans.
+__global__ void k_decide(EdgeLists el, LevelNodes L, uint32_t M, uint32_t E2, uint32_t* __restrict__ iflag,
+                         uint32_t* __restrict__ lcnt, uint32_t* err) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= M || L.state[k] != 0) return;
+  if (k > M) return;
+  if (k == M) {
+    iflag[k] = 0u;
+    lcnt[k] = 0u;
+    return;
+  }
+  if (L.state[k] == 0) decide_node(el, L, k, E2, err);
+  const int st = L.state[k];
+  iflag[k] = st == 2 ? 1u : 0u;
+  lcnt[k] = st == 1 ? L.rc[k] : 0u;
+}
+
+__device__ void decide_node(EdgeLists el, LevelNodes L, uint32_t k, uint32_t E2, uint32_t* err) {
   for (int q = 0; q < 3; ++q) {
     const int a = (L.axis0[k] + q) % 3;
     const unsigned long long b = L.best[3 * (size_t)k + a];
@@ -446,14 +469,6 @@ __global__ void __launch_bounds__(kThreads) k_partition(EdgeLists el, uint32_t E
   }
 }
 
-// Interior flag and leaf ref count of every node (M + 1 entries, last 0).
-__global__ void k_node_flags(LevelNodes L, uint32_t M, uint32_t* __restrict__ iflag, uint32_t* __restrict__ lcnt) {
-  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k > M) return;
-  const int st = k < M ? L.state[k] : 0;
-  iflag[k] = st == 2 ? 1u : 0u;
-  lcnt[k] = st == 1 ? L.rc[k] : 0u;
-}
 
 // Global node table (breadth-first ids).
 struct Table {
@@ -472,6 +487,7 @@ __global__ void k_spawn(LevelNodes L, uint32_t M, const uint32_t* __restrict__ i
                         uint32_t level_base, uint32_t next_base, Table T, LevelNodes N,
                         uint32_t* __restrict__ child_cnt, uint32_t M2, uint32_t* err) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0) child_cnt[M2] = 0u;  // the scan's last entry
   if (k >= M) return;
   const uint32_t g = level_base + k;
   const uint32_t rs = L.rs[k], rc = L.rc[k];
@@ -954,7 +970,6 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     uint32_t* sB = above + (R + 1);
     uint32_t* sA = sB + (R + 1);
     uint32_t* tmp = sA + (R + 1);
-    KD_TRY(cudaMemsetAsync(below, 0, ((size_t)R + 1) * 8, st), "KD flags");  // below + above
     // partition scratch: tile counts and the side flags as ballot words
     const uint32_t E2 = 2 * R;
     const uint32_t runs = (E2 + kEdgeRun - 1) / kEdgeRun, tiles = (E2 + kEdgeTile - 1) / kEdgeTile;
@@ -963,16 +978,6 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     unsigned long long* tile_cnt = sc.m4.as<unsigned long long>();
     uint32_t* sideB = reinterpret_cast<uint32_t*>(tile_cnt + (size_t)tiles * 3 * 2);
     uint32_t* sideA = sideB + words * 3;
-    count_launch();
-    k_node_init<<<grid(M), kThreads, 0, st>>>(L, M);
-    if (E2) {
-      count_launch();
-      k_cost<<<grid(3ull * runs * 32), kThreads, 0, st>>>(el, E2, runs, M, L, err);
-    }
-    count_launch(2);
-    k_decide<<<grid(M), kThreads, 0, st>>>(el, L, M, E2, err);
-    k_classify<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, M, aabb, L, below, above, err);
-    KD_TRY(cudaGetLastError(), "KD split");
     // interior ranks, leaf pool offsets, children's ref counts
     KD_TRY(ensure_after(sc.m7, ((size_t)M + 1) * 4 * 4 + scan_tmp_words((uint64_t)M + 1) * 8 + 64, st), "KD scratch");
     uint32_t* iflag = sc.m7.as<uint32_t>();
@@ -982,7 +987,15 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
     uint32_t* mtmp = lofs + (M + 1);
     uint32_t* mtot = mtmp + 2 * scan_tmp_words((uint64_t)M + 1) + 4;  // 4 totals
     count_launch();
-    k_node_flags<<<grid(M + 1), kThreads, 0, st>>>(L, M, iflag, lcnt);
+    k_node_init<<<grid(std::max<uint64_t>(M, (uint64_t)R + 1)), kThreads, 0, st>>>(L, M, below, above, R);
+    if (E2) {
+      count_launch();
+      k_cost<<<grid(3ull * runs * 32), kThreads, 0, st>>>(el, E2, runs, M, L, err);
+    }
+    count_launch(2);
+    k_decide<<<grid((uint64_t)M + 1), kThreads, 0, st>>>(el, L, M, E2, iflag, lcnt, err);
+    k_classify<<<grid(R), kThreads, 0, st>>>(ref_prim, ref_node, R, M, aabb, L, below, above, err);
+    KD_TRY(cudaGetLastError(), "KD split");
     launch_scan2_excl(iflag, irank, lcnt, lofs, (uint64_t)M + 1, mtmp, mtot, mtot + 1, st);
     launch_scan2_excl(below, sB, above, sA, (uint64_t)R + 1, tmp, mtot + 2, mtot + 3, st);
     uint32_t h_tot[4] = {0, 0, 0, 0};
@@ -1009,7 +1022,6 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth_cfg, AccelBuffers& a
                                           err);
     KD_TRY(cudaGetLastError(), "KD spawn");
     if (M2) {
-      KD_TRY(cudaMemsetAsync(ccnt + M2, 0, 4, st), "KD spawn");
       launch_scan_excl(ccnt, coff, (uint64_t)M2 + 1, ctmp, nullptr, st);
       count_launch();
       k_set_ref_starts<<<grid(M2), kThreads, 0, st>>>(N, M2, ccnt, coff);

@@ -74,7 +74,10 @@ __global__ void __launch_bounds__(kThreads) k_scan_local(ScanArgs<NA> A, uint64_
       if (i < n) A.out[q][i] = run;
       run += v[q][k];
     }
-    if (threadIdx.x == 0) A.tot[q][blockIdx.x] = total;
+    if (threadIdx.x == 0) {
+      A.tot[q][blockIdx.x] = total;
+      if (gridDim.x == 1 && A.grand[q]) *A.grand[q] = total;  // one block: no totals pass
+    }
   }
 }
 
@@ -125,10 +128,12 @@ __global__ void __launch_bounds__(kThreads) k_scan_add(ScanArgs<NA> A, uint64_t 
 template <int NA>
 void scan_launch(const ScanArgs<NA>& A, uint64_t n, cudaStream_t s) {
   const uint32_t nb = (uint32_t)((n + kBlock - 1) / kBlock);
-  count_launch(nb > 1 ? 3 : 2);
+  count_launch(nb > 1 ? 3 : 1);
   k_scan_local<NA><<<nb, kThreads, 0, s>>>(A, n);
-  k_scan_totals<NA><<<1, kThreads, 0, s>>>(A, nb);
-  if (nb > 1) k_scan_add<NA><<<nb, kThreads, 0, s>>>(A, n);
+  if (nb > 1) {
+    k_scan_totals<NA><<<1, kThreads, 0, s>>>(A, nb);
+    k_scan_add<NA><<<nb, kThreads, 0, s>>>(A, n);
+  }
 }
 
 }  // namespace
