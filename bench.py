@@ -983,6 +983,8 @@ def run_case(args):
         scene = eng.scene_triangles(verts, idx)
         acc = eng.build(scene, rq.LBVH)
         hits_p = eng.trace_closest(acc, primary)
+        if args.structure != "LBVH" and args.case in ("primary", "secondary", "shadow"):
+            acc = eng.build(scene, args.structure)  # the same rays through another structure
         rays = {"primary": primary, "build": primary, "build-bvh": primary, "build-kd": primary,
                 "secondary": scenes.cosine_rays(verts, idx, primary, hits_p, seed=SEED + 2),
                 "shadow": scenes.shadow_rays(verts, idx, primary, hits_p, LIGHT)}[args.case]
@@ -1022,6 +1024,8 @@ def main():
     ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "build-bvh", "build-kd",
                                        "batched", "build-batched"],
                     help="profiling driver: run one query class, print no bench line")
+    ap.add_argument("--structure", choices=["LBVH", "BVH", "KDTREE"], default="LBVH",
+                    help="structure traced by --case primary/secondary/shadow")
     ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
     ap.add_argument("--scheduling", type=int, default=0, help="--case: settings.scheduling (0-3)")
     ap.add_argument("--no-tune", action="store_true",
