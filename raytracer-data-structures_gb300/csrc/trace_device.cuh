@@ -75,6 +75,21 @@ __device__ __forceinline__ uint32_t test_count(const float4* __restrict__ prims,
   return (uint32_t)count;
 }
 
+// One 64-byte BVH2 node as two 256-bit loads (nodes are 64-byte aligned).
+__device__ __forceinline__ void load_node(const float4* nd, float4& a, float4& b, float4& z, int4& l) {
+  uint32_t r[16];
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "l"(nd));
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "l"(nd + 2));
+  a = make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]), __uint_as_float(r[3]));
+  b = make_float4(__uint_as_float(r[4]), __uint_as_float(r[5]), __uint_as_float(r[6]), __uint_as_float(r[7]));
+  z = make_float4(__uint_as_float(r[8]), __uint_as_float(r[9]), __uint_as_float(r[10]), __uint_as_float(r[11]));
+  l = make_int4((int)r[12], (int)r[13], (int)r[14], (int)r[15]);
+}
+
 // FAST walk of one ray through a BVH2: near child first, far child on a
 // per-thread stack of STACK entries, boxes clipped to [tmin, closest hit].
 // Returns true when an any-hit query found a hit.
@@ -95,9 +110,15 @@ __device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, C
   for (;;) {
     if (++steps > max_steps) { atomicOr(err, kErrCorrupt); return false; }
     if (cur >= 0) {
+      float4 a, b, z;
+      int4 l;
       const float4* nd = bvh.nodes + 4 * (size_t)cur;
-      float4 a = __ldg(nd), b = __ldg(nd + 1), z = __ldg(nd + 2);
-      int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+      if (ANY) {  // any hit measured 1% faster with four 128-bit loads, closest hit 2% slower
+        a = __ldg(nd); b = __ldg(nd + 1); z = __ldg(nd + 2);
+        l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+      } else {
+        load_node(nd, a, b, z, l);
+      }
       if (COUNT) ++visits;
       const float tfar = ANY ? ray.tmax : c.t;
       float tl, tr;
