@@ -207,9 +207,13 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ kin
 constexpr int kItems32 = 15;  // 3,840 keys per tile
 constexpr int kItems64 = 10;  // 2,560 keys per tile (64-bit keys)
 
+// Sorted pairs land back in keys / vals, unless vals_out is given: then the
+// final pass's buffers are left as they are and *vals_out names the one that
+// holds the sorted values (keys end in the matching key buffer).
 template <typename K, int ITEMS>
 void onesweep_passes(K* keys, uint32_t* vals, uint32_t n, int passes, K* keys_alt, uint32_t* vals_alt,
-                     const uint32_t* hist, uint32_t* status, uint32_t* counters, uint32_t* err, cudaStream_t s) {
+                     const uint32_t* hist, uint32_t* status, uint32_t* counters, uint32_t* err, cudaStream_t s,
+                     uint32_t** vals_out = nullptr) {
   using Smem = OnesweepSmem<K, ITEMS>;
   static_assert(sizeof(Smem) <= 48 * 1024, "onesweep shared memory over the default limit");
   const uint32_t tile = kThreads * ITEMS;
@@ -225,6 +229,10 @@ void onesweep_passes(K* keys, uint32_t* vals, uint32_t n, int passes, K* keys_al
                                                                counters + p, err);
     K* tk = src_k; src_k = dst_k; dst_k = tk;
     uint32_t* tv = src_v; src_v = dst_v; dst_v = tv;
+  }
+  if (vals_out) {
+    *vals_out = src_v;
+    return;
   }
   if (src_k != keys) {
     cudaMemcpyAsync(keys, src_k, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, s);
@@ -258,6 +266,15 @@ void launch_onesweep(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, con
   if (n <= 1) return;
   onesweep_passes<uint32_t, kItems32>(keys, vals, n, passes, sc.keys_alt, sc.vals_alt, sc.hist, sc.status,
                                       sc.counters, err, s);
+}
+
+uint32_t* launch_onesweep_vals(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
+                               uint32_t* err, cudaStream_t s) {
+  if (n <= 1) return vals;
+  uint32_t* out = vals;
+  onesweep_passes<uint32_t, kItems32>(keys, vals, n, passes, sc.keys_alt, sc.vals_alt, sc.hist, sc.status,
+                                      sc.counters, err, s, &out);
+  return out;
 }
 
 size_t sort_status_words64(uint32_t n, int passes) {

@@ -60,6 +60,10 @@ size_t sort_status_words(uint32_t n, int passes);
 void launch_histogram(const uint32_t* keys, uint32_t n, int passes, uint32_t* hist, cudaStream_t s);
 void launch_onesweep(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
                      uint32_t* err, cudaStream_t s);
+// As launch_onesweep, without copying the result back after an odd number of
+// passes: returns the buffer (vals or sc.vals_alt) that holds the sorted values.
+uint32_t* launch_onesweep_vals(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
+                               uint32_t* err, cudaStream_t s);
 
 // 64-bit keys, 32-bit values (tiles of 2,560 keys).  hist: 256 words per pass
 // (up to 8 passes); status: sort_status_words64 words; counters: one per pass.
