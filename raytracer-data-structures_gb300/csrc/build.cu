@@ -70,17 +70,16 @@ BuildResult sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, b
   return {};
 }
 
-// sort_pairs for a permutation: the sorted values stay in whichever buffer
-// the last pass wrote (no copy back); *perm names it.
+// sort_pairs for a permutation whose digit histogram is already in sc.zero
+// (zeroed with its look-back words before the histogram was counted): the
+// sorted values stay in whichever buffer the last pass wrote (no copy back);
+// *perm names it.
 BuildResult sort_perm(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, BuildScratch& sc, uint32_t* err,
                       cudaStream_t st, const uint32_t** perm) {
   *perm = vals;
   if (n <= 1) return {};
   RQ_B(sc.keys_alt.ensure((size_t)n * 4), "sort scratch");
   RQ_B(sc.vals_alt.ensure((size_t)n * 4), "sort scratch");
-  RQ_B(sc.zero.ensure(zero_words(n, passes) * 4), "sort scratch");
-  RQ_B(cudaMemsetAsync(sc.zero.p, 0, (1024 + 16 + sort_status_words(n, passes)) * 4, st), "memset");
-  launch_histogram(keys, n, passes, sc.zero.as<uint32_t>(), st);
   uint32_t* z = sc.zero.as<uint32_t>();
   SortScratch s{sc.keys_alt.as<uint32_t>(), sc.vals_alt.as<uint32_t>(), z, z + 1040, z + 1024};
   *perm = launch_onesweep_vals(keys, vals, n, passes, s, err, st);
@@ -216,9 +215,11 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
     RQ_B(sc.vals.ensure((size_t)q.n * 4), "ray sort scratch");
     uint32_t* keys = sc.keys.as<uint32_t>();
     uint32_t* p = sc.vals.as<uint32_t>();
-    launch_ray_keys(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, keys, p, st);
     const int passes = cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON12 ? 2
                        : (cfg.ray_sort == RQ_RAY_SORT_OCTANT || cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON3) ? 1 : 4;
+    RQ_B(sc.zero.ensure(zero_words(q.n, passes) * 4), "sort scratch");
+    RQ_B(cudaMemsetAsync(sc.zero.p, 0, (1024 + 16 + sort_status_words(q.n, passes)) * 4, st), "memset");
+    launch_ray_keys(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, keys, p, st, sc.zero.as<uint32_t>(), passes);
     BuildResult r = sort_perm(keys, p, q.n, passes, sc, err, st, &perm);
     if (!r.ok()) return r;
   }

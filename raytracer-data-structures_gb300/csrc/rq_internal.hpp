@@ -163,8 +163,10 @@ void launch_trace_bvh2_packet(int kind, bool any, const Bvh2View& v, const float
 void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
                             uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s);
 // Coherence sort keys (mode: rq_ray_sort_t other than NONE, 30 bits); vals = identity.
+// With hist (zeroed, 256 words per pass) it also counts the sort's `passes`
+// digits, as launch_histogram would.
 void launch_ray_keys(const float4* rays, uint32_t n, const float* root, int mode, uint32_t* keys, uint32_t* vals,
-                     cudaStream_t s);
+                     cudaStream_t s, uint32_t* hist = nullptr, int passes = 0);
 // FAST traversal that also sums internal-node visits and primitive tests
 // into counters[0..1] (the inputs of the traversal byte model).
 void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n,

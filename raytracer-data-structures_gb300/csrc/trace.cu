@@ -735,51 +735,94 @@ __device__ __forceinline__ uint32_t spread_bits(uint32_t v) {  // 10 bits -> eve
   return v;
 }
 
+// Sort keys of the optional ray order, and (when hist is given) the digit
+// histogram of the sort's `passes` 8-bit digits in the same read: a block
+// of 256 threads strides over the rays, counts in shared memory with one
+// atomic per distinct digit in a warp, and adds its counts to hist once.
+// The octant-only key reads just the direction.
 __global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ rays, uint32_t n,
                                                   const float* __restrict__ root, int mode,
-                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
-  const float o[3] = {a.x, a.y, a.z};
-  const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4
-                    : mode == RQ_RAY_SORT_OCTANT_MORTON3 ? 1 : mode == RQ_RAY_SORT_OCTANT ? 0 : 5;
-  const float cells = (float)(1u << obits);
-  uint32_t q[3];
-  for (int k = 0; k < 3; ++k) {
-    float lo = root[k], ext = root[3 + k] - root[k];
-    float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
-    u = fminf(fmaxf(u * cells, 0.f), cells - 1.f);
-    q[k] = (uint32_t)u;
+                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                  uint32_t* __restrict__ hist, int passes) {
+  __shared__ uint32_t sh[4][256];
+  if (hist) {
+    for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&sh[0][0])[k] = 0u;
+    __syncthreads();
   }
-  const uint32_t morton = (spread_bits(q[0]) << 2) | (spread_bits(q[1]) << 1) | spread_bits(q[2]);
-  const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
-  uint32_t key;
-  if (mode == RQ_RAY_SORT_OCTANT_MORTON) {
-    key = (oct << 27) | morton;
-  } else if (mode == RQ_RAY_SORT_OCTANT_MORTON12) {
-    key = (oct << 12) | morton;
-  } else if (mode == RQ_RAY_SORT_OCTANT_MORTON3) {
-    key = (oct << 3) | morton;
-  } else if (mode == RQ_RAY_SORT_OCTANT) {
-    key = oct;
-  } else {
-    const float len = sqrtf(b.x * b.x + b.y * b.y + b.z * b.z);
-    const float inv = len > 0.f ? 1.0f / len : 0.f;
-    const uint32_t dx = (uint32_t)fminf(fabsf(b.x) * inv * 64.f, 63.f);
-    const uint32_t dy = (uint32_t)fminf(fabsf(b.y) * inv * 64.f, 63.f);
-    const uint32_t dir = (dx << 6) | dy;
-    key = mode == RQ_RAY_SORT_ORIGIN_DIRECTION ? (oct << 27) | (morton << 12) | dir : (oct << 27) | (dir << 15) | morton;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t end = (n + 31u) & ~31u;  // whole warps take part in the histogram
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += stride) {
+    const bool live = i < n;
+    uint32_t key = 0;
+    if (live) {
+      const float4 b = __ldg(rays + 2 * (size_t)i + 1);
+      const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
+      if (mode == RQ_RAY_SORT_OCTANT) {
+        key = oct;
+      } else {
+        const float4 a = __ldg(rays + 2 * (size_t)i);
+        const float o[3] = {a.x, a.y, a.z};
+        const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4
+                          : mode == RQ_RAY_SORT_OCTANT_MORTON3 ? 1 : 5;
+        const float cells = (float)(1u << obits);
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) {
+          float lo = root[k], ext = root[3 + k] - root[k];
+          float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
+          u = fminf(fmaxf(u * cells, 0.f), cells - 1.f);
+          q[k] = (uint32_t)u;
+        }
+        const uint32_t morton = (spread_bits(q[0]) << 2) | (spread_bits(q[1]) << 1) | spread_bits(q[2]);
+        if (mode == RQ_RAY_SORT_OCTANT_MORTON) {
+          key = (oct << 27) | morton;
+        } else if (mode == RQ_RAY_SORT_OCTANT_MORTON12) {
+          key = (oct << 12) | morton;
+        } else if (mode == RQ_RAY_SORT_OCTANT_MORTON3) {
+          key = (oct << 3) | morton;
+        } else {
+          const float len = sqrtf(b.x * b.x + b.y * b.y + b.z * b.z);
+          const float inv = len > 0.f ? 1.0f / len : 0.f;
+          const uint32_t dx = (uint32_t)fminf(fabsf(b.x) * inv * 64.f, 63.f);
+          const uint32_t dy = (uint32_t)fminf(fabsf(b.y) * inv * 64.f, 63.f);
+          const uint32_t dir = (dx << 6) | dy;
+          key = mode == RQ_RAY_SORT_ORIGIN_DIRECTION ? (oct << 27) | (morton << 12) | dir
+                                                     : (oct << 27) | (dir << 15) | morton;
+        }
+      }
+      keys[i] = key;
+      vals[i] = i;
+    }
+    if (hist) {
+      const uint32_t lanes = __ballot_sync(0xffffffffu, live);
+      if (live) {
+        for (int p = 0; p < passes; ++p) {
+          const uint32_t d = (key >> (8 * p)) & 255u;
+          const uint32_t same = __match_any_sync(lanes, d);
+          if ((same & ((1u << lane) - 1u)) == 0u) atomicAdd(&sh[p][d], (uint32_t)__popc(same));
+        }
+      }
+    }
   }
-  keys[i] = key;
-  vals[i] = i;
+  if (hist) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < passes * 256; k += blockDim.x) {
+      const uint32_t v = (&sh[0][0])[k];
+      if (v) atomicAdd(hist + k, v);
+    }
+  }
 }
 
 void launch_ray_keys(const float4* rays, uint32_t n, const float* root, int mode, uint32_t* keys, uint32_t* vals,
-                     cudaStream_t s) {
+                     cudaStream_t s, uint32_t* hist, int passes) {
   if (n == 0) return;
   count_launch();
-  k_ray_keys<<<(n + 255) / 256, 256, 0, s>>>(rays, n, root, mode, keys, vals);
+  uint32_t g = (n + 255) / 256;
+  if (hist) {
+    const uint32_t cap = 4u * (uint32_t)device_sm_count();  // few blocks: few global histogram atomics
+    if (g > cap) g = cap;
+  }
+  k_ray_keys<<<g, 256, 0, s>>>(rays, n, root, mode, keys, vals, hist, passes);
 }
 
 void launch_trace_brute(int kind, int traversal, bool any, const float4* prims, uint32_t n_prims,
