@@ -754,7 +754,7 @@ def run_serve_leg(args):
 
 
 def build_bytes_per_tri():
-    """Compulsory bytes per triangle of the LBVH build kernels (see DESIGN.md):
+    """Compulsory bytes per triangle of the LBVH build kernels:
     bounds 6 (12 B per vertex, 0.5 vertex per triangle) + Morton 26 (12 B indices,
     6 B vertices, 8 B code/index write) + 4 sort passes x 16 + Karras 28 (code
     read 4, links 16, parents 8) + refit 150 (order 4, indices 12, vertices 6,
