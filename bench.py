@@ -16,8 +16,8 @@ and L2 is additionally flushed (256 MB write) before every timed step.
   roofline: the step's dominant kernel against measured HBM bandwidth, with
            algorithmic bytes from the engine's traversal counters
   cpu_baseline: the CPU oracle (the reference's algorithms: median BVH build,
-           collect-all division-slab traversal, Moller-Trumbore) on a bounded
-           sample of the same rays, all host threads
+           collect-all division-slab traversal, Moller-Trumbore) on the whole
+           job (every ray of the step), all host threads
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -89,19 +89,24 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(kernel_key):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", "trace_lbvh_heightfield.md")
+def profile_value(name, kernel_key, path=os.path.join("profiles", "trace_lbvh_heightfield.md")):
+    """A figure `name[kernel_key]: value ...` recorded in a committed ncu summary, or None."""
+    p = os.path.join(ROOT, path)
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for line in f:
-            if line.startswith(f"dram_bytes_per_launch[{kernel_key}]:"):
+            if line.startswith(f"{name}[{kernel_key}]:"):
                 try:
                     return float(line.split(":", 1)[1].split()[0])
                 except ValueError:
                     return None
     return None
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch (full-size launch) from the committed ncu summary."""
+    return profile_value("dram_bytes_per_launch", kernel_key)
 
 
 class ClockSampler:
@@ -340,12 +345,28 @@ def run_ours(args):
     alg = {"build": build_bytes, "trace_primary": trace_bytes("primary", n_p),
            "trace_secondary": trace_bytes("secondary", n_s), "trace_shadow": trace_bytes("shadow", n_sh, False)}
     achieved = alg[dom] / (kern[dom] * 1e-3) / 1e9
+    traffic = profile_traffic(dom)
+    n_dom = {"trace_primary": n_p, "trace_secondary": n_s, "trace_shadow": n_sh}.get(dom)
+    step_work = sum(alg.values())
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": profile_traffic(dom), "algorithmic_bytes": int(alg[dom]),
-                "compulsory_frac": round((((n_p if dom == "trace_primary" else n_s if dom == "trace_secondary" else n_sh)
-                                           * (RAY_BYTES + HIT_BYTES)) / (kern[dom] * 1e-3) / 1e9) / peak, 4)
-                if dom != "build" else None}
+                "achieved_kind": ("L1/L2-inclusive work bytes: every node visit (node_bytes) and triangle test "
+                                  "(48 B) counted as a fetch, plus 32 B ray + hit; most of these fetches hit L1/L2"),
+                "traffic": traffic, "algorithmic_bytes": int(alg[dom]),
+                # What DRAM itself carries for this kernel (ncu, committed summary) against the
+                # live kernel time: the bandwidth actually used.
+                "dram_gbs": round(traffic / (kern[dom] * 1e-3) / 1e9, 1) if traffic else None,
+                "dram_frac": round(traffic / (kern[dom] * 1e-3) / 1e9 / peak, 4) if traffic else None,
+                "issue_active": profile_value("issue_active", dom),
+                "lanes_per_inst": profile_value("lanes_per_inst", dom),
+                "l2_hit_rate": profile_value("l2_hit_rate", dom),
+                "limiter": ("divergence and memory latency (lanes per instruction and long-scoreboard stalls), "
+                            "not DRAM bandwidth") if dom != "build" else None,
+                "compulsory_frac": round((n_dom * (RAY_BYTES + HIT_BYTES)) / (kern[dom] * 1e-3) / 1e9 / peak, 4)
+                if n_dom else None,
+                # The whole step's work bytes over the step time: above 1 means the model's
+                # fetches are served by the caches, not that DRAM ran above its peak.
+                "step_work_frac": round(step_work / (mean_ms * 1e-3) / 1e9 / peak, 4)}
 
     # The same step through the C ABI with host buffers, right after the
     # device-resident step (before the other legs leave memory and heat behind).
@@ -396,7 +417,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
-        cpu = cpu_baseline(verts, idx, primary, secondary, shadow, budget_s=args.cpu_budget)
+        cpu = cpu_baseline(verts, idx, primary, secondary, shadow)
 
     if rank == 0:
         out = {
@@ -406,6 +427,9 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "dataStructure": "LBVH", "triangles": n_tri, "primary_rays": n_p,
                        "secondary_rays": n_s, "shadow_rays": n_sh, "seed": SEED,
                        "l2": "flushed before every timed step (256 MB write); rays exceed L2",
+                       "ray_generation": ("primary rays generated once on the host; secondary (cosine) and shadow "
+                                          "rays generated once from the first primary trace's hits; each timed "
+                                          "step rebuilds the LBVH and traces all three sets"),
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "node_width": max(node_width, 2), "morton": morton_names[morton_mode],
                        "ray_sort": {k: sort_names[v[0]] for k, v in sort_choice.items()},
@@ -569,10 +593,25 @@ def batch_rays(torch, dev, meshes, counts, seed):
     return out.view(torch.uint8).reshape(-1)
 
 
+def c4_workload(n_sc=256):
+    """The many-scene workload: n_sc meshes with triangle counts log-uniform in
+    [1k, 500k], each a displaced icosphere or an fBm heightfield chosen by
+    seed, and per-scene ray counts log-uniform in [64k, 2M].  Returns
+    (meshes [(verts, idx)], ray counts, ray offsets (n_sc + 1, uint32))."""
+    import scenes
+    mixed = scenes.mixed_meshes(n_sc, 1e3, 5e5, SEED + 40)
+    rng = np.random.default_rng(SEED + 41)
+    ray_n = np.exp(rng.uniform(np.log(64e3), np.log(2e6), n_sc)).astype(np.int64)
+    offs = np.zeros(n_sc + 1, np.uint32)
+    offs[1:] = np.cumsum(ray_n)
+    return [(v, f) for v, f, _ in mixed], ray_n, offs
+
+
 def run_batch_leg(eng, stream, dev, args):
-    """Many scenes at once: 256 terrain meshes with triangle counts
-    log-uniform in [1k, 500k] and ray counts log-uniform in [64k, 2M] (origins
-    on each scene's bounding sphere, directions into its box).  One step =
+    """Many scenes at once: 256 meshes (displaced icospheres or fBm
+    heightfields, chosen by seed) with triangle counts log-uniform in [1k,
+    500k] and ray counts log-uniform in [64k, 2M] (origins on each scene's
+    bounding sphere, directions into its box).  One step =
     rebuild every structure + closest hit for every ray.  'plain' does it one
     scene per launch (rq_accel_rebuild + rq_trace_closest per scene); 'batched'
     replays one plan: the batched LBVH rebuild + one persistent many-structure
@@ -584,20 +623,12 @@ def run_batch_leg(eng, stream, dev, args):
 
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    rng = np.random.default_rng(SEED + 40)
     n_sc = 32 if args.small else 256
-    tri_t = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_sc))
-    ray_n = np.exp(rng.uniform(np.log(64e3), np.log(2e6), n_sc)).astype(np.int64)
-    meshes = []
-    for k in range(n_sc):
-        nx = max(2, int(round(np.sqrt(tri_t[k] / 2)))) + 1
-        meshes.append(scenes.wave_heightfield(nx, nx, seed=SEED + 100 + k))
+    meshes, ray_n, offs = c4_workload(n_sc)
     n_tri = int(sum(len(f) for _, f in meshes))
     saved = eng.settings
     eng.configure(ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
     sc = [eng.scene_triangles(v, f) for v, f in meshes]
-    offs = np.zeros(n_sc + 1, np.uint32)
-    offs[1:] = np.cumsum(ray_n)
     n_rays = int(offs[-1])
     d_rays = batch_rays(torch, dev, meshes, ray_n.tolist(), SEED + 41)
     d_hits = torch.empty(n_rays * HIT_BYTES, dtype=torch.uint8, device=dev)
@@ -681,7 +712,7 @@ def run_batch_leg(eng, stream, dev, args):
 
 def run_serve_leg(args):
     """The serving loop under load: Poisson arrivals at 400 requests/s for a
-    few seconds; 32 resident terrain meshes of 10k-2M triangles (log-uniform)
+    few seconds; 32 resident displaced icospheres of 10k-2M triangles (log-uniform)
     plus new meshes (5% of requests name a mesh never seen before: upload +
     LBVH build on demand); resolution uniform over 320x240, 640x480, 1280x720,
     1920x1080, spp over 1, 2, 4, 8, 16; HBM budget 80 GB with LRU eviction.
@@ -694,13 +725,10 @@ def run_serve_leg(args):
     rate, secs = 400.0, (1.0 if args.small else 4.0)
     n_res, n_new_max = 32, 64
 
-    def mesh(seed):
-        t = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
-        nx = max(2, int(round(np.sqrt(t / 2)))) + 1
-        return scenes.wave_heightfield(nx, nx, seed=seed)
-
-    lib = {k: mesh(SEED + 200 + k) for k in range(n_res)}
-    fresh = {1000 + k: mesh(SEED + 400 + k) for k in range(n_new_max)}
+    # seeded displaced icospheres, 10k-2M triangles (log-uniform target, nearest subdivision level)
+    pool = scenes.mixed_meshes(n_res + n_new_max, 1e4, 2e6, SEED + 200, kinds=("icosphere",))
+    lib = {k: pool[k][:2] for k in range(n_res)}
+    fresh = {1000 + k: pool[n_res + k][:2] for k in range(n_new_max)}
     arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * secs * 1.2)))
     arrivals = arrivals[arrivals < secs]
     res = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
@@ -712,9 +740,11 @@ def run_serve_leg(args):
         w, h = res[int(rng.integers(4))]
         spp = int(rng.choice([1, 2, 4, 8, 16]))
         az = rng.uniform(0, 6.283)
-        view = rq.make_view(eye=(float(2.2 * np.cos(az)), float(2.2 * np.sin(az)), float(rng.uniform(0.5, 1.5))),
-                            target=(0.0, 0.0, 0.0), up=(0.0, 0.0, 1.0), fov_deg=float(rng.uniform(35, 60)),
-                            light=(1.0, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=int(SEED + k))
+        # an orbit around the mesh's centre (the meshes fill the unit cube)
+        view = rq.make_view(eye=(float(0.5 + 2.2 * np.cos(az)), float(0.5 + 2.2 * np.sin(az)),
+                                 float(0.5 + rng.uniform(-0.8, 0.8))),
+                            target=(0.5, 0.5, 0.5), up=(0.0, 0.0, 1.0), fov_deg=float(rng.uniform(35, 60)),
+                            light=(1.5, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=int(SEED + k))
         sched.append((float(t), mid, view, w, h, spp))
     out = {"requests": len(sched), "rate_per_s": rate, "seconds": secs,
            "resident_meshes": n_res, "new_mesh_requests": sum(1 for s in sched if s[1] >= 1000),
@@ -815,63 +845,65 @@ def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_
 class CpuBaseline:
     """The reference's algorithms on the host cores (the oracle port): median
     BVH build (constructBVHNew's partition + nth_element, one thread as the
-    reference runs it), collect-all division-slab traversal (boxIntersect)
-    with Moller-Trumbore closest hit and any hit for shadow rays, on all host
-    threads.  A bounded, seeded sample of each ray class is traced; the
-    whole-job time is the build time plus the measured per-ray cost times the
-    full ray counts."""
+    reference runs it), then every ray of the job through the collect-all
+    division-slab traversal (boxIntersect) with Moller-Trumbore closest hit
+    (primary, secondary) and any hit (shadow), rays in their own order split
+    over all host threads in chunks of 256 consecutive rays.  One step = the
+    build + all three ray classes: the whole job, nothing extrapolated."""
 
-    def __init__(self, verts, idx, samples, counts, budget_s=20.0):
+    def __init__(self, verts, idx, classes):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle_py as O
         self.O = O
         self.cores = os.cpu_count() or 1
-        self.prims, aabb, cen = O.tri_prims(verts, idx)
-        t0 = time.perf_counter()
+        self.prims, self.aabb, self.cen = O.tri_prims(verts, idx)
+        self.n_tri = len(idx)
+        self.classes = classes  # name -> (rays, query)
+        self.rays = sum(len(r) for r, _ in classes.values())
+
+    def build(self):
         # The reference's partition + nth_element median build; on meshes its
         # degenerate nodes (all centroids at or above the midpoint) would recurse
         # forever, so the oracle's rule (such a node becomes one leaf) is used.
-        self.bvh = O.build_median(aabb, cen, compat=False)
-        self.build_s = time.perf_counter() - t0
-        self.n_tri = len(idx)
-        self.counts = counts
-        self.pool = samples  # name -> (rays, query)
-        rng = np.random.default_rng(SEED + 9)
-        self.sample = 256
-        while True:
-            self.sel = {k: rng.choice(len(r), size=min(self.sample, len(r)), replace=False)
-                        for k, (r, q) in self.pool.items()}
-            per = self.measure()
-            spent = sum(per[k] * len(self.sel[k]) for k in per)
-            if spent > budget_s / 10 or self.sample >= 1 << 15:
-                break
-            self.sample *= 4
+        t0 = time.perf_counter()
+        bvh = self.O.build_median(self.aabb, self.cen, compat=False)
+        return bvh, time.perf_counter() - t0
 
-    def measure(self, threads=None, limit=None):
+    def step(self, threads=None, rows=None):
+        """Build + trace; rows (optional): a contiguous slice of each class.
+        Returns (total seconds, build seconds, {class: seconds})."""
         O = self.O
+        bvh, tb = self.build()
         per = {}
-        for k, (rays, q) in self.pool.items():
-            r = rays[self.sel[k][:limit]]
+        for k, (rays, q) in self.classes.items():
+            r = rays if rows is None else rays[rows(len(rays))]
             t1 = time.perf_counter()
-            O.trace_bvh2(O.TRIANGLES, O.REFERENCE, q, self.bvh, self.prims, r, nthreads=threads or self.cores)
-            per[k] = (time.perf_counter() - t1) / len(r)
-        return per
+            O.trace_bvh2(O.TRIANGLES, O.REFERENCE, q, bvh, self.prims, r, nthreads=threads or self.cores)
+            per[k] = time.perf_counter() - t1
+        return tb + sum(per.values()), tb, per
 
-    def whole_job(self, per):
-        return sum(self.counts.values()) / (self.build_s + sum(per[k] * self.counts[k] for k in per)) / 1e9
+    def record(self, total_s, build_s, per, one_core=True):
+        out = {"value": self.rays / total_s / 1e9, "unit": UNIT, "cores": self.cores, "kind": "port",
+               "sample": (f"full job: median-BVH build of all {self.n_tri} triangles (1 thread) + all "
+                          f"{self.rays} rays (primary/secondary/shadow) through the reference's collect-all "
+                          f"traversal on {self.cores} threads, rays in their own order"),
+               "build_s": round(build_s, 3), "trace_s": {k: round(v, 3) for k, v in per.items()},
+               "step_s": round(total_s, 3), "nproc": self.cores, "cpu_model": cpu_model()}
+        if one_core:
+            # One thread on a contiguous 1/64 of each class (pixel tiles in order),
+            # scaled to the class; the build is the same single-threaded build.
+            frac = 64
 
-    def record(self, per):
-        one_n = max(256, self.sample // 8)
-        one = self.measure(threads=1, limit=one_n)  # the same rays' first eighth on one thread
-        return {"value": self.whole_job(per), "unit": UNIT, "cores": self.cores, "kind": "port",
-                "sample": (f"median-BVH build of all {self.n_tri} triangles (1 thread, {self.build_s:.2f} s) + "
-                           f"{self.sample} seeded rays per class (primary/secondary/shadow) traced with the "
-                           f"reference's collect-all traversal on {self.cores} threads; whole job = build + "
-                           f"per-ray cost x full ray counts"),
-                "build_s": round(self.build_s, 3), "per_ray_us": {k: round(v * 1e6, 3) for k, v in per.items()},
-                "nproc": self.cores, "cpu_model": cpu_model(),
-                "one_core": {"value": self.whole_job(one), "rays_per_class": min(one_n, self.sample),
-                             "per_ray_us": {k: round(v * 1e6, 3) for k, v in one.items()}}}
+            def rows(n):
+                a = n // 2
+                return slice(a, a + max(1, n // frac))
+            _, tb, part = self.step(threads=1, rows=rows)
+            whole = build_s + sum(part[k] * len(self.classes[k][0]) / max(1, len(self.classes[k][0]) // frac)
+                                  for k in part)
+            out["one_core"] = {"value": self.rays / whole / 1e9,
+                               "sample": f"1 thread, a contiguous 1/{frac} of each ray class from its middle, "
+                                         "scaled to the class; build as above"}
+        return out
 
 
 def cpu_model():
@@ -895,15 +927,20 @@ def cpu_model():
     return platform.machine()
 
 
-def cpu_baseline(verts, idx, primary, secondary, shadow, budget_s=20.0):
+def cpu_baseline(verts, idx, primary, secondary, shadow):
     O_any, O_closest = 1, 0
     cb = CpuBaseline(verts, idx, {"primary": (primary, O_closest), "secondary": (secondary, O_closest),
-                                  "shadow": (shadow, O_any)},
-                     {"primary": len(primary), "secondary": len(secondary), "shadow": len(shadow)}, budget_s)
-    return cb.record(cb.measure())
+                                  "shadow": (shadow, O_any)})
+    return cb.record(*cb.step())
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores (the oracle port: the
+    reference compiled from its sources needs its source tree, which only the
+    build container has).  Secondary and shadow rays start at this arm's own
+    primary hits (closest hit on its median BVH, equal to the GPU arm's hits:
+    the closest hit does not depend on the tree), so the rays are the GPU
+    arm's rays.  Every step is the whole job: build + all rays."""
     ws, rank, _ = dist_env()
     if ws > 1 and rank != 0:
         return
@@ -911,30 +948,25 @@ def run_reference(args):
     import scenes
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as O
-    # Secondary and shadow rays start at primary hits: find the hits of a
-    # seeded subset of primary rays with the oracle, and scale the counts by
-    # the subset's hit fraction.
     prims, aabb, cen = O.tri_prims(verts, idx)
     bvh = O.build_median(aabb, cen)
-    rng = np.random.default_rng(SEED + 7)
-    sub = primary[rng.choice(len(primary), size=min(100_000, len(primary)), replace=False)]
-    h = O.trace_bvh2(O.TRIANGLES, O.FAST, O.CLOSEST, bvh, prims, sub)
-    secondary = scenes.cosine_rays(verts, idx, sub, h, seed=SEED + 2)
-    shadow = scenes.shadow_rays(verts, idx, sub, h, LIGHT)
-    n_hit = int(round(len(primary) * len(secondary) / len(sub)))
-    counts = {"primary": len(primary), "secondary": n_hit, "shadow": n_hit}
-    cb = CpuBaseline(verts, idx, {"primary": (sub, O.CLOSEST), "secondary": (secondary, O.CLOSEST),
-                                  "shadow": (shadow, O.ANY)}, counts, budget_s=args.cpu_budget)
-    vals, rec = [], None
+    h = O.trace_bvh2(O.TRIANGLES, O.FAST, O.CLOSEST, bvh, prims, primary)
+    secondary = scenes.cosine_rays(verts, idx, primary, h, seed=SEED + 2)
+    shadow = scenes.shadow_rays(verts, idx, primary, h, LIGHT)
+    counts = {"primary": len(primary), "secondary": len(secondary), "shadow": len(shadow)}
+    cb = CpuBaseline(verts, idx, {"primary": (primary, O.CLOSEST), "secondary": (secondary, O.CLOSEST),
+                                  "shadow": (shadow, O.ANY)})
+    times, last = [], None
     for k in range(args.warmup + args.steps):
-        rec = cb.record(cb.measure())
+        last = cb.step()
         if k >= args.warmup:
-            vals.append(rec["value"])
-    v = float(np.mean(vals))
-    rec["value"] = v
+            times.append(last[0])
+    t = float(np.mean(times))
+    rec = cb.record(t, last[1], last[2], one_core=False)
+    v = rec["value"]
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
-           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 1), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
            "config": {"workload": WORKLOAD, "dataStructure": "BVH (the reference's median builder)",
                       "triangles": len(idx), "primary_rays": counts["primary"],
                       "secondary_rays": counts["secondary"], "shadow_rays": counts["shadow"], "seed": SEED},
@@ -962,17 +994,9 @@ def run_case(args):
     eng.set_stream(stream.cuda_stream)
     eng.configure(morton=rq.MORTON_SCENE_CUBE)  # the tuner's build choice (see --no-tune)
     if args.case in ("batched", "build-batched"):
-        rng = np.random.default_rng(SEED + 40)
-        n_sc = 32 if args.small else 256
-        tri_t = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_sc))
-        ray_n = np.exp(rng.uniform(np.log(64e3), np.log(2e6), n_sc)).astype(np.int64)
-        meshes = [scenes.wave_heightfield(max(2, int(round(np.sqrt(t / 2)))) + 1,
-                                          max(2, int(round(np.sqrt(t / 2)))) + 1, seed=SEED + 100 + k)
-                  for k, t in enumerate(tri_t)]
+        meshes, ray_n, offs = c4_workload(32 if args.small else 256)
         sc = [eng.scene_triangles(v, f) for v, f in meshes]
         accs = eng.build_batched(sc, rq.LBVH)
-        offs = np.zeros(n_sc + 1, np.uint32)
-        offs[1:] = np.cumsum(ray_n)
         d_rays = batch_rays(torch, dev, meshes, ray_n.tolist(), SEED + 41)
         d_hits = torch.empty(int(offs[-1]) * HIT_BYTES, dtype=torch.uint8, device=dev)
         call = lambda: eng.trace_batched(accs, d_rays, offs, out=d_hits)  # noqa: E731
@@ -1013,7 +1037,6 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline work")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--small", action="store_true", help="960x540x4 rays (profiling case)")

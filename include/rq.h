@@ -272,6 +272,42 @@ rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t accel, int32_t* nodes, i
  * count -1.  No reference counterpart: the reference's trees are binary. */
 rq_status_t rq_accel_export_bvh4(rq_ctx_t ctx, rq_accel_t accel, float* nodes, uint32_t* n_nodes);
 
+/* A BVH2 structure from host arrays in rq_accel_export_bvh2's layout (nodes =
+ * n_nodes * 16 words, order = n_slots primitive ids of `scene`, root_bounds =
+ * min xyz, max xyz), for trees built elsewhere or edited by the caller.  Every
+ * link is checked to stay inside the arrays (internal child < n_nodes, leaf
+ * slots within n_slots, counts >= 1) and every box to be finite; the shape
+ * itself is not checked: a cycle makes queries end with
+ * RQ_ERROR_INVALID_ARGUMENT ("malformed acceleration structure") once a walk
+ * exceeds the steps a valid tree allows, and boxes that miss their primitives
+ * lose those hits.  The structure reports type RQ_BVH, is walked with binary
+ * nodes whatever settings.node_width says, and cannot be rebuilt
+ * (rq_accel_rebuild: RQ_ERROR_UNSUPPORTED).  No reference counterpart: the
+ * reference builds its trees in process (constructBVHNew, accelerators.h:246). */
+rq_status_t rq_accel_import_bvh2(rq_ctx_t ctx, rq_scene_t scene, const float* nodes, uint32_t n_nodes,
+                                 const uint32_t* order, uint32_t n_slots, const float* root_bounds,
+                                 rq_accel_t* out);
+
+/* Test hooks that make the engine's device-side guards fire on purpose,
+ * without a fault, so a test can check the status a caller then sees and that
+ * the context keeps working.  All fields 0 (the default) is normal operation.
+ * No reference counterpart (the reference reports no errors at all,
+ * main.cpp:656-660). */
+typedef struct rq_debug_t {
+  /* 1: in rq_sort_pairs of this context with at least 3,841 pairs, one tile
+   * of the first digit pass waits on a device word that nothing ever sets; its
+   * bounded wait gives up (some microseconds) and the call returns
+   * RQ_ERROR_TIMEOUT with keys and values undefined. */
+  uint32_t sort_stall;
+  /* 1: FAST thread-per-ray binary-BVH queries (rq_trace_closest / any, BVH and
+   * LBVH, node_width 2, scheduling THREAD_PER_RAY) run with a traversal
+   * stack of 8 entries instead of 64, so trees deep enough along a ray end in
+   * RQ_ERROR_STACK_OVERFLOW. */
+  uint32_t small_stack;
+} rq_debug_t;
+/* debug may be NULL (all hooks off). */
+rq_status_t rq_set_debug(rq_ctx_t ctx, const rq_debug_t* debug);
+
 /* ---------------------------------------------------------------- queries */
 
 /* Closest hit per ray: replaces boxIntersect + castRay's candidate loop
@@ -394,11 +430,15 @@ rq_status_t rq_sort_pairs(rq_ctx_t ctx, uint32_t* keys, uint32_t* values, uint32
  *    9.5 MB that every GPU loading this library holds until the process exits.
  *    It bounds n to RQ_SORT_NOALLOC_MAX_PAIRS; larger n returns
  *    RQ_ERROR_INVALID_ARGUMENT.
- *  - The first call on each device looks up the array's device address; make
- *    that first call before any stream capture.
+ *  - Every call looks up the array's device address on the current device
+ *    (cuda_stream must belong to that device: RQ_ERROR_INVALID_ARGUMENT
+ *    otherwise).  The first call on a device may load the library's device
+ *    code there; make that first call before any stream capture.
  *  - All calls on a device share the array, so calls that overlap on the GPU
  *    (other streams, other host threads) race and must be serialized by the
- *    caller. */
+ *    caller.
+ *  - RQ_ERROR_TIMEOUT (a bounded device-side wait gave up) leaves keys and
+ *    values undefined: later digit passes still run and write into them. */
 #define RQ_SORT_NOALLOC_MAX_PAIRS (1u << 20)
 rq_status_t rq_sort_pairs_noalloc(uint32_t* keys, uint32_t* values, uint32_t n, uint32_t key_bits,
                                   void* cuda_stream);

@@ -184,11 +184,19 @@ inline bool box_ref(V3 o, V3 d, const float* lo, const float* hi, float& tMin, f
 // (one correctly rounded fused multiply-add, as the engine's kernels do),
 // NaN-ignoring fminf/fmaxf, interval clipped to [tmin, tfar], far end widened
 // by the relative 1 + 2*gamma(3) (Ize 2013) and the absolute eps, so that no
-// box the ray truly meets is rejected because of rounding.  The engine's
-// kernels perform exactly these operations in this order.
+// box the ray truly meets is rejected because of rounding.
+// The fused form needs o * inv finite on every axis.  Rays where it is not (a
+// direction component zero, or so small that 1/d or o/d overflows) use the
+// exact form: per axis (b - o) * inv, and an axis along which the ray does not
+// move (inv infinite) constrains nothing when lo <= o <= hi and rejects the
+// box otherwise; far end widened by 1 + 2^-20.  The engine's kernels perform
+// exactly these operations in this order.
+constexpr float kWidenExact = 0x1.00001p+0f;
 struct SlabRay {
   V3 inv, noi;
   float eps;
+  V3 o;
+  bool exact;
 };
 inline SlabRay slab_ray(V3 o, V3 d) {
   SlabRay s;
@@ -200,23 +208,52 @@ inline SlabRay slab_ray(V3 o, V3 d) {
   if (std::fabs(oy) <= FLT_MAX) m = fmaxf(m, std::fabs(oy));
   if (std::fabs(oz) <= FLT_MAX) m = fmaxf(m, std::fabs(oz));
   s.eps = m * 0x1p-21f;
+  s.o = o;
+  s.exact = !(std::fabs(s.noi.x) <= FLT_MAX && std::fabs(s.noi.y) <= FLT_MAX && std::fabs(s.noi.z) <= FLT_MAX);
   return s;
+}
+inline void slab_axis_exact(float l, float h, float o, float inv, float& near_t, float& far_t) {
+  const float a = l - o, b = h - o;
+  if (std::fabs(inv) > FLT_MAX) {  // the ray does not move along this axis
+    const bool in = a <= 0.f && b >= 0.f;
+    near_t = in ? -INFINITY : INFINITY;
+    far_t = in ? INFINITY : -INFINITY;
+  } else {
+    const float t0 = a * inv, t1 = b * inv;
+    near_t = fminf(t0, t1);
+    far_t = fmaxf(t0, t1);
+  }
+}
+// Per-axis entry and exit distances of one box.
+inline void slab_axes(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz, float n[3],
+                      float f[3]) {
+  if (r.exact) {
+    slab_axis_exact(lx, hx, r.o.x, r.inv.x, n[0], f[0]);
+    slab_axis_exact(ly, hy, r.o.y, r.inv.y, n[1], f[1]);
+    slab_axis_exact(lz, hz, r.o.z, r.inv.z, n[2], f[2]);
+    return;
+  }
+  const float tx0 = std::fmaf(lx, r.inv.x, r.noi.x), tx1 = std::fmaf(hx, r.inv.x, r.noi.x);
+  const float ty0 = std::fmaf(ly, r.inv.y, r.noi.y), ty1 = std::fmaf(hy, r.inv.y, r.noi.y);
+  const float tz0 = std::fmaf(lz, r.inv.z, r.noi.z), tz1 = std::fmaf(hz, r.inv.z, r.noi.z);
+  n[0] = fminf(tx0, tx1); f[0] = fmaxf(tx0, tx1);
+  n[1] = fminf(ty0, ty1); f[1] = fmaxf(ty0, ty1);
+  n[2] = fminf(tz0, tz1); f[2] = fmaxf(tz0, tz1);
 }
 inline float slab_exit(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
                        float tfar_in) {
-  float tx0 = std::fmaf(lx, r.inv.x, r.noi.x), tx1 = std::fmaf(hx, r.inv.x, r.noi.x);
-  float ty0 = std::fmaf(ly, r.inv.y, r.noi.y), ty1 = std::fmaf(hy, r.inv.y, r.noi.y);
-  float tz0 = std::fmaf(lz, r.inv.z, r.noi.z), tz1 = std::fmaf(hz, r.inv.z, r.noi.z);
-  return fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar_in));
+  float n[3], f[3];
+  slab_axes(r, lx, hx, ly, hy, lz, hz, n, f);
+  return fminf(fminf(f[0], f[1]), fminf(f[2], tfar_in));
 }
+inline float slab_widen(const SlabRay& r) { return r.exact ? kWidenExact : kWiden; }
 inline bool box_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz, float hz,
                      float tmin, float tfar_in, float& tnear_out) {
-  float tx0 = std::fmaf(lx, r.inv.x, r.noi.x), tx1 = std::fmaf(hx, r.inv.x, r.noi.x);
-  float ty0 = std::fmaf(ly, r.inv.y, r.noi.y), ty1 = std::fmaf(hy, r.inv.y, r.noi.y);
-  float tz0 = std::fmaf(lz, r.inv.z, r.noi.z), tz1 = std::fmaf(hz, r.inv.z, r.noi.z);
-  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar_in));
-  tf = std::fmaf(tf, kWiden, r.eps);
+  float n[3], f[3];
+  slab_axes(r, lx, hx, ly, hy, lz, hz, n, f);
+  float tn = fmaxf(fmaxf(n[0], n[1]), fmaxf(n[2], tmin));
+  float tf = fminf(fminf(f[0], f[1]), fminf(f[2], tfar_in));
+  tf = std::fmaf(tf, slab_widen(r), r.eps);
   tnear_out = tn;
   return tn <= tf;
 }
@@ -368,7 +405,7 @@ void trace_one_kd(int kind, int mode, int query, const KdView& kd, const int32_t
     if (!box_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, best, tn)) return;
     // exit distance of the root box, clipped and widened the same way
     tMin = tn;
-    tMax = std::fmaf(slab_exit(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], best), kWiden, sr.eps);
+    tMax = std::fmaf(slab_exit(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], best), slab_widen(sr), sr.eps);
   }
   KdTodo todo[64];
   int todoPos = 0;

@@ -64,7 +64,7 @@ BuildResult sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, b
     launch_histogram(keys, n, passes, sc.zero.as<uint32_t>(), st);
   }
   uint32_t* z = sc.zero.as<uint32_t>();
-  SortScratch s{sc.keys_alt.as<uint32_t>(), sc.vals_alt.as<uint32_t>(), z, z + 1040, z + 1024};
+  SortScratch s{sc.keys_alt.as<uint32_t>(), sc.vals_alt.as<uint32_t>(), z, z + 1040, z + 1024, sc.stall};
   launch_onesweep(keys, vals, n, passes, s, err, st);
   RQ_B(cudaGetLastError(), "radix sort launch");
   return {};
@@ -190,7 +190,7 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
   } else {
     Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
                a.root.as<const float>(), a.n_nodes, a.n_slots};
-    launch_trace_bvh2(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
+    launch_trace_bvh2(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, nullptr, q.small_stack);
   }
 }
 
@@ -242,7 +242,7 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
     return {};
   }
   if (a.node_width == 4) launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
-  else launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm);
+  else launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm, q.small_stack);
   RQ_B(cudaGetLastError(), "trace launch");
   return {};
 }

@@ -646,9 +646,14 @@ __global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, c
     } else {
       float tn;
       const SlabRay sr = slab_ray(o, d);
-      in = slab_fast(sr, R[0], R[3], R[1], R[4], R[2], R[5], rtmin, best, tn);
+      if (zero_dir(sr)) {  // the exact box test (rq_device.cuh)
+        in = slab_box<true>(sr, o, R[0], R[3], R[1], R[4], R[2], R[5], rtmin, best, tn);
+        tMax = __fmaf_rn(slab_exit<true>(sr, o, R[0], R[3], R[1], R[4], R[2], R[5], best), kWidenExact, sr.eps);
+      } else {
+        in = slab_box<false>(sr, o, R[0], R[3], R[1], R[4], R[2], R[5], rtmin, best, tn);
+        tMax = __fmaf_rn(slab_exit<false>(sr, o, R[0], R[3], R[1], R[4], R[2], R[5], best), kWiden, sr.eps);
+      }
       tMin = tn;
-      tMax = __fmaf_rn(slab_exit(sr, R[0], R[3], R[1], R[4], R[2], R[5], best), kWiden, sr.eps);
     }
     if (in) {
       Todo todo[kStackSize];

@@ -24,6 +24,7 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kFlagAbort = 3u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
 constexpr uint32_t kSpinLimit = 1u << 20;  // polls of one predecessor word before giving up
+constexpr uint32_t kStallSpin = 256;       // polls of the test hook's never-set word
 
 template <typename K>
 __global__ void __launch_bounds__(kThreads) k_histogram(const K* __restrict__ keys, uint32_t n,
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ kin
                                                        uint32_t* __restrict__ vout, uint32_t n,
                                                        int shift, const uint32_t* __restrict__ hist,
                                                        uint32_t* status, uint32_t* tile_counter,
-                                                       uint32_t* err) {
+                                                       uint32_t* err, const uint32_t* stall) {
   constexpr int kTile = kThreads * kItems;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   OnesweepSmem<K, kItems>& sm = *reinterpret_cast<OnesweepSmem<K, kItems>*>(smem_raw);
@@ -156,7 +157,11 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ kin
   uint32_t excl = 0;
   bool failed = false;
   if (tile > 0) {
-    for (int64_t j = (int64_t)tile - 1; j >= 0; --j) {
+    // Test hook (stall != null): tile 1 first waits on a word that nothing
+    // sets, so its bounded wait gives up as a lost predecessor's would.
+    if (stall && tile == 1)
+      failed = !spin_until([&] { return *reinterpret_cast<const volatile uint32_t*>(stall) != 0u; }, kStallSpin);
+    for (int64_t j = (int64_t)tile - 1; j >= 0 && !failed; --j) {
       uint32_t s = 0;
       bool ok = spin_until([&] { s = st[(size_t)j * 256 + t]; return (s & ~kValueMask) != 0; },
                            kSpinLimit);
@@ -213,7 +218,7 @@ constexpr int kItems64 = 10;  // 2,560 keys per tile (64-bit keys)
 template <typename K, int ITEMS>
 void onesweep_passes(K* keys, uint32_t* vals, uint32_t n, int passes, K* keys_alt, uint32_t* vals_alt,
                      const uint32_t* hist, uint32_t* status, uint32_t* counters, uint32_t* err, cudaStream_t s,
-                     uint32_t** vals_out = nullptr) {
+                     uint32_t** vals_out = nullptr, const uint32_t* stall = nullptr) {
   using Smem = OnesweepSmem<K, ITEMS>;
   static_assert(sizeof(Smem) <= 48 * 1024, "onesweep shared memory over the default limit");
   const uint32_t tile = kThreads * ITEMS;
@@ -226,7 +231,7 @@ void onesweep_passes(K* keys, uint32_t* vals, uint32_t n, int passes, K* keys_al
     count_launch();
     k_onesweep<K, ITEMS><<<tiles, kThreads, sizeof(Smem), s>>>(src_k, src_v, dst_k, dst_v, n, 8 * p,
                                                                hist + 256 * p, status + (size_t)p * tiles * 256,
-                                                               counters + p, err);
+                                                               counters + p, err, p == 0 ? stall : nullptr);
     K* tk = src_k; src_k = dst_k; dst_k = tk;
     uint32_t* tv = src_v; src_v = dst_v; dst_v = tv;
   }
@@ -265,7 +270,7 @@ void launch_onesweep(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, con
                      uint32_t* err, cudaStream_t s) {
   if (n <= 1) return;
   onesweep_passes<uint32_t, kItems32>(keys, vals, n, passes, sc.keys_alt, sc.vals_alt, sc.hist, sc.status,
-                                      sc.counters, err, s);
+                                      sc.counters, err, s, nullptr, sc.stall);
 }
 
 uint32_t* launch_onesweep_vals(uint32_t* keys, uint32_t* vals, uint32_t n, int passes, const SortScratch& sc,
@@ -273,7 +278,7 @@ uint32_t* launch_onesweep_vals(uint32_t* keys, uint32_t* vals, uint32_t n, int p
   if (n <= 1) return vals;
   uint32_t* out = vals;
   onesweep_passes<uint32_t, kItems32>(keys, vals, n, passes, sc.keys_alt, sc.vals_alt, sc.hist, sc.status,
-                                      sc.counters, err, s, &out);
+                                      sc.counters, err, s, &out, sc.stall);
   return out;
 }
 

@@ -139,8 +139,10 @@ rq_status_t rq_create(const rq_settings_t* settings, int device, rq_ctx_t* out) 
   else rq_settings_default(&ctx->settings);
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 4);
-  if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 4);
+  // d_err[0]: the device error word; d_err[1]: a word that nothing writes
+  // (the sort test hook of rq_set_debug waits on it).
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 8);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 8);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
     rq_status_t st = e == cudaErrorMemoryAllocation ? RQ_ERROR_OUT_OF_MEMORY : RQ_ERROR_CUDA;
@@ -402,7 +404,78 @@ rq_status_t rq_build(rq_ctx_t ctx, rq_scene_t scene, int32_t acc_type, rq_accel_
 rq_status_t rq_accel_rebuild(rq_ctx_t ctx, rq_accel_t a) {
   if (!a) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel");
   RQ_TRY(bind(ctx));
+  if (a->imported) return fail(ctx, RQ_ERROR_UNSUPPORTED, "an imported structure has no builder to rerun");
   return do_build(ctx, a);
+}
+
+rq_status_t rq_accel_import_bvh2(rq_ctx_t ctx, rq_scene_t scene, const float* nodes, uint32_t n_nodes,
+                                 const uint32_t* order, uint32_t n_slots, const float* root_bounds,
+                                 rq_accel_t* out) {
+  if (!out) return RQ_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  RQ_TRY(bind(ctx));
+  if (!scene || !order || !root_bounds || (n_nodes && !nodes))
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null scene, nodes, order or root bounds");
+  if (n_slots == 0 || n_slots > (1u << 30)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "n_slots must be 1..2^30");
+  if (n_nodes >= n_slots + (1u << 30)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "too many nodes");
+  if (!finite3(root_bounds, 6)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "root bounds not finite");
+  for (uint32_t k = 0; k < n_slots; ++k)
+    if (order[k] >= scene->n) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "order entry is not a primitive id");
+  // Every link must stay inside the arrays, so a walk never reads outside
+  // them; what is left unchecked (cycles, boxes that do not bound their
+  // primitives) is caught or tolerated by the walks' own bounds.
+  for (uint32_t i = 0; i < n_nodes; ++i) {
+    const float* nd = nodes + 16 * (size_t)i;
+    if (!finite3(nd, 12)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "node box not finite");
+    int32_t l[4];
+    std::memcpy(l, nd + 12, 16);
+    for (int c = 0; c < 2; ++c) {
+      const int32_t link = l[c], count = l[2 + c];
+      if (link >= 0 ? (uint32_t)link >= n_nodes
+                    : (count < 1 || (uint64_t)(uint32_t)(~link) + (uint64_t)count > n_slots))
+        return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "node link outside the node or slot arrays");
+    }
+  }
+  rq_accel* a = new (std::nothrow) rq_accel();
+  if (!a) return RQ_ERROR_OUT_OF_MEMORY;
+  a->ctx = ctx;
+  a->scene = scene;
+  a->type = RQ_BVH;
+  a->imported = true;
+  AccelBuffers& b = a->buf;
+  cudaError_t e = b.nodes.ensure((size_t)n_nodes * 64);
+  if (e == cudaSuccess) e = b.order.ensure((size_t)n_slots * 4);
+  if (e == cudaSuccess) e = b.root.ensure(32);
+  if (e == cudaSuccess) e = b.prims.ensure((size_t)n_slots * (scene->kind == kTriangles ? 48 : 16));
+  if (e == cudaSuccess && n_nodes)
+    e = cudaMemcpyAsync(b.nodes.p, nodes, (size_t)n_nodes * 64, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.order.p, order, (size_t)n_slots * 4, cudaMemcpyHostToDevice, ctx->stream);
+  float root8[8] = {root_bounds[0], root_bounds[1], root_bounds[2], root_bounds[3], root_bounds[4], root_bounds[5], 0.f, 0.f};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.root.p, root8, 32, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    const SceneView sv = scene_view(scene);
+    launch_prims_gather(sv.kind, sv.verts, sv.idx, sv.sph, b.order.as<const uint32_t>(), n_slots,
+                        b.prims.as<float4>(), ctx->stream);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // root8 lives on this stack frame
+  if (e != cudaSuccess) {
+    b.release();
+    delete a;
+    return cuda_fail(ctx, e, "import");
+  }
+  b.n_nodes = n_nodes;
+  b.n_slots = n_slots;
+  b.node_width = 2;
+  *out = a;
+  return RQ_SUCCESS;
+}
+
+rq_status_t rq_set_debug(rq_ctx_t ctx, const rq_debug_t* debug) {
+  if (!ctx) return RQ_ERROR_INVALID_ARGUMENT;
+  if (debug) ctx->debug = *debug;
+  else ctx->debug = rq_debug_t{};
+  return RQ_SUCCESS;
 }
 
 rq_status_t rq_accel_destroy(rq_accel_t a) {
@@ -702,6 +775,7 @@ static rq_status_t trace(rq_ctx_t ctx, rq_accel_t a, const rq_ray_t* rays, uint3
   q.n = n;
   q.hits = any ? nullptr : static_cast<float4*>(d_out);
   q.occ = any ? static_cast<uint32_t*>(d_out) : nullptr;
+  q.small_stack = ctx->debug.small_stack != 0;
   BuildResult br = launch_query_sorted(a->type, scene_view(a->scene), a->buf, ctx->settings, any, q, ctx->scratch,
                                        ctx->d_err, ctx->stream);
   if (br.cuda != cudaSuccess) return cuda_fail(ctx, br.cuda, br.what);
@@ -1188,7 +1262,9 @@ rq_status_t rq_sort_pairs(rq_ctx_t ctx, uint32_t* keys, uint32_t* values, uint32
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dk, keys, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(dv, values, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
   }
+  ctx->scratch.stall = ctx->debug.sort_stall ? ctx->d_err + 1 : nullptr;
   BuildResult r = sort_pairs(dk, dv, n, (int)((key_bits + 7) / 8), true, ctx->scratch, ctx->d_err, ctx->stream);
+  ctx->scratch.stall = nullptr;
   if (r.cuda != cudaSuccess) return cuda_fail(ctx, r.cuda, r.what);
   RQ_TRY(check_launch(ctx, "sort launch"));
   if (!dev) {

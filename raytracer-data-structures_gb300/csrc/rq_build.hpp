@@ -55,6 +55,7 @@ struct BuildScratch {
   DevBuf m0, m1, m2, m3, m4, m5, m6, m7;  // median / KD working arrays
   DevBuf kd_refs;             // KD: next level's primitive references
   DevBuf work;                // work counter of lane-refill traversal
+  const uint32_t* stall = nullptr;  // sort test hook (SortScratch::stall); null in normal use
   void release() {
     work.release();
     keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); mark.release(); lohi.release();
@@ -137,6 +138,7 @@ struct QueryTarget {
   uint32_t n = 0;
   float4* hits = nullptr;
   uint32_t* occ = nullptr;
+  bool small_stack = false;  // test hook: FAST BVH2 walk with a traversal stack of kDebugStack entries
 };
 // Batches of at least this many rays are reordered when settings.ray_sort asks.
 constexpr uint32_t kRaySortMin = 65536;

@@ -111,28 +111,85 @@ __device__ __forceinline__ SlabRay slab_ray(F3 o, F3 d) {
   return s;
 }
 
+// The fused plane distance fma(b, inv, -o*inv) needs o*inv finite.  A
+// direction component that is zero (or so small that 1/d or o/d overflows)
+// breaks it: inf - inf, or an infinite near distance, which rejects every
+// box.  Such rays take the exact form instead (callers pick the form once per
+// ray, so ordinary rays pay nothing): per axis (b - o) * inv, whose sign is
+// the sign of b - o, and an axis along which the ray does not move (inv
+// infinite) constrains nothing when lo <= o <= hi and rejects the box
+// otherwise.
+constexpr float kWidenExact = 0x1.00001p+0f;  // 1 + 2^-20: covers the roundings of (b - o) * inv
+__device__ __forceinline__ bool zero_dir(const SlabRay& r) {
+  return !(fabsf(r.noi.x) <= 3.402823466e38f && fabsf(r.noi.y) <= 3.402823466e38f &&
+           fabsf(r.noi.z) <= 3.402823466e38f);
+}
+__device__ __forceinline__ void slab_axis_exact(float l, float h, float o, float inv, float& near, float& far) {
+  const float a = __fsub_rn(l, o), b = __fsub_rn(h, o);
+  if (fabsf(inv) > 3.402823466e38f) {  // the ray does not move along this axis
+    const bool in = a <= 0.f && b >= 0.f;
+    near = __int_as_float(in ? (int)0xFF800000u : 0x7F800000);
+    far = __int_as_float(in ? 0x7F800000 : (int)0xFF800000u);
+  } else {
+    const float t0 = __fmul_rn(a, inv), t1 = __fmul_rn(b, inv);
+    near = fminf(t0, t1);
+    far = fmaxf(t0, t1);
+  }
+}
+
 // Engine slab test on one box: plane distances b*inv - o*inv with one fused
-// multiply-add each, NaN-ignoring min/max, clipped to [tmin, tfar].  The far
-// end is widened by kWiden (relative rounding) and eps (the absolute error
-// of the fused form, proportional to |o*inv|), so no box that the ray truly
-// meets is rejected.
-__device__ __forceinline__ bool slab_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz,
-                                          float hz, float tmin, float tfar, float& tnear) {
-  float tx0 = __fmaf_rn(lx, r.inv.x, r.noi.x), tx1 = __fmaf_rn(hx, r.inv.x, r.noi.x);
-  float ty0 = __fmaf_rn(ly, r.inv.y, r.noi.y), ty1 = __fmaf_rn(hy, r.inv.y, r.noi.y);
-  float tz0 = __fmaf_rn(lz, r.inv.z, r.noi.z), tz1 = __fmaf_rn(hz, r.inv.z, r.noi.z);
-  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar));
-  tf = __fmaf_rn(tf, kWiden, r.eps);
+// multiply-add each (EXACT: (b - o) * inv), NaN-ignoring min/max, clipped to
+// [tmin, tfar].  The far end is widened by kWiden (relative rounding) and eps
+// (the absolute error of the fused form, proportional to |o*inv|), so no box
+// that the ray truly meets is rejected.
+template <bool EXACT>
+__device__ __forceinline__ bool slab_box(const SlabRay& r, F3 o, float lx, float hx, float ly, float hy, float lz,
+                                         float hz, float tmin, float tfar, float& tnear) {
+  float tn, tf;
+  if (EXACT) {
+    float nx, fx, ny, fy, nz, fz;
+    slab_axis_exact(lx, hx, o.x, r.inv.x, nx, fx);
+    slab_axis_exact(ly, hy, o.y, r.inv.y, ny, fy);
+    slab_axis_exact(lz, hz, o.z, r.inv.z, nz, fz);
+    tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, tmin));
+    tf = fminf(fminf(fx, fy), fminf(fz, tfar));
+    tf = __fmaf_rn(tf, kWidenExact, r.eps);
+  } else {
+    const float tx0 = __fmaf_rn(lx, r.inv.x, r.noi.x), tx1 = __fmaf_rn(hx, r.inv.x, r.noi.x);
+    const float ty0 = __fmaf_rn(ly, r.inv.y, r.noi.y), ty1 = __fmaf_rn(hy, r.inv.y, r.noi.y);
+    const float tz0 = __fmaf_rn(lz, r.inv.z, r.noi.z), tz1 = __fmaf_rn(hz, r.inv.z, r.noi.z);
+    tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar));
+    tf = __fmaf_rn(tf, kWiden, r.eps);
+  }
   tnear = tn;
   return tn <= tf;
 }
+// The fused form (rays without a zero direction component).
+__device__ __forceinline__ bool slab_fast(const SlabRay& r, float lx, float hx, float ly, float hy, float lz,
+                                          float hz, float tmin, float tfar, float& tnear) {
+  return slab_box<false>(r, F3{0.f, 0.f, 0.f}, lx, hx, ly, hy, lz, hz, tmin, tfar, tnear);
+}
+// Either form, chosen per call (kernels whose lanes walk together).
+__device__ __forceinline__ bool slab_any(bool exact, const SlabRay& r, F3 o, float lx, float hx, float ly, float hy,
+                                         float lz, float hz, float tmin, float tfar, float& tnear) {
+  return exact ? slab_box<true>(r, o, lx, hx, ly, hy, lz, hz, tmin, tfar, tnear)
+               : slab_box<false>(r, o, lx, hx, ly, hy, lz, hz, tmin, tfar, tnear);
+}
 // Exit distance of the same box (before widening).
-__device__ __forceinline__ float slab_exit(const SlabRay& r, float lx, float hx, float ly, float hy, float lz,
+template <bool EXACT>
+__device__ __forceinline__ float slab_exit(const SlabRay& r, F3 o, float lx, float hx, float ly, float hy, float lz,
                                            float hz, float tfar) {
-  float tx0 = __fmaf_rn(lx, r.inv.x, r.noi.x), tx1 = __fmaf_rn(hx, r.inv.x, r.noi.x);
-  float ty0 = __fmaf_rn(ly, r.inv.y, r.noi.y), ty1 = __fmaf_rn(hy, r.inv.y, r.noi.y);
-  float tz0 = __fmaf_rn(lz, r.inv.z, r.noi.z), tz1 = __fmaf_rn(hz, r.inv.z, r.noi.z);
+  if (EXACT) {
+    float nx, fx, ny, fy, nz, fz;
+    slab_axis_exact(lx, hx, o.x, r.inv.x, nx, fx);
+    slab_axis_exact(ly, hy, o.y, r.inv.y, ny, fy);
+    slab_axis_exact(lz, hz, o.z, r.inv.z, nz, fz);
+    return fminf(fminf(fx, fy), fminf(fz, tfar));
+  }
+  const float tx0 = __fmaf_rn(lx, r.inv.x, r.noi.x), tx1 = __fmaf_rn(hx, r.inv.x, r.noi.x);
+  const float ty0 = __fmaf_rn(ly, r.inv.y, r.noi.y), ty1 = __fmaf_rn(hy, r.inv.y, r.noi.y);
+  const float tz0 = __fmaf_rn(lz, r.inv.z, r.noi.z), tz1 = __fmaf_rn(hz, r.inv.z, r.noi.z);
   return fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tfar));
 }
 

@@ -82,6 +82,7 @@ struct rq_context {
   DevBuf batch_table;  // views + ray offsets + work counter of rq_trace_batched
   DevBuf ref_jitter;   // the reference render's default-seeded jitter, generated once per sample count
   uint64_t ref_jitter_n = 0;
+  rq_debug_t debug{};  // test hooks (rq_set_debug); all off by default
 };
 
 struct rq_plan {
@@ -117,5 +118,6 @@ struct rq_accel {
   AccelBuffers buf;
   std::shared_ptr<BatchStore> batch;  // set when buf borrows a batched build's arrays
   uint32_t batch_index = 0;
+  bool imported = false;  // made by rq_accel_import_bvh2: nothing to rebuild from
 };
 

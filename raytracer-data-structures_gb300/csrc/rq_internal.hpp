@@ -51,6 +51,9 @@ struct SortScratch {
   uint32_t* hist;      // 4 * 256 digit counts
   uint32_t* status;    // passes * tiles * 256 look-back words
   uint32_t* counters;  // one tile counter per pass
+  // Test hook: non-null makes tile 1 of the first pass wait (bounded) on this
+  // device word, which nothing sets, so the sort reports a timeout.
+  const uint32_t* stall = nullptr;
 };
 uint32_t sort_tiles(uint32_t n);
 size_t sort_status_words(uint32_t n, int passes);
@@ -142,9 +145,12 @@ struct Bvh2View {
   uint32_t n_slots;
 };
 // perm (optional): trace ray perm[i] in thread i (results stay in caller order).
+// small_stack (a test hook): the FAST walk's stack holds kDebugStack entries,
+// so moderately deep trees overflow it.
+constexpr int kDebugStack = 8;
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
                        uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
-                       const uint32_t* perm = nullptr);
+                       const uint32_t* perm = nullptr, bool small_stack = false);
 // boxIntersect's candidate lists: ids == null counts per ray into counts;
 // otherwise writes each ray's ids at offs[r] (and checks the counts).
 // Count pass (ids null): counts[r] and *total (64-bit sum, zeroed by the

@@ -11,8 +11,6 @@
 // library is loaded.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "rq_device.cuh"
 #include "rq_internal.hpp"
 
@@ -37,30 +35,26 @@ constexpr size_t kWords = kErrOff + 16;
 // One array per GPU that loads the library (about 9.5 MB), shared by every call.
 static __device__ __align__(256) uint32_t g_sort_scratch[kWords];
 
-// Device address of g_sort_scratch per device ordinal.  Host code must not use
-// the symbol itself as a pointer: on the host it names a stand-in, not device
-// memory.
-std::mutex g_mutex;
-uint32_t* g_addr[64] = {};
-
+// Device address of g_sort_scratch on the current device, looked up on every
+// call.  Host code must not use the symbol itself as a pointer: on the host it
+// names a stand-in, not device memory.  The lookup is not cached: after a
+// cudaDeviceReset (or a primary context released and created again) the
+// module is loaded anew and the array may sit at another address.  Once the
+// module is loaded on a device the lookup is cheap; the first one on a device
+// may load the module, which is why that first call must precede any capture.
 rq_status_t scratch_for_current_device(uint32_t** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
     return RQ_ERROR_NO_DEVICE;
   }
-  if (dev < 0 || dev >= 64) return RQ_ERROR_UNSUPPORTED;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return RQ_ERROR_CUDA;
-    }
-    g_addr[dev] = static_cast<uint32_t*>(p);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return RQ_ERROR_CUDA;
   }
-  *out = g_addr[dev];
+  *out = static_cast<uint32_t*>(p);
   return RQ_SUCCESS;
 }
 
@@ -79,11 +73,23 @@ extern "C" rq_status_t rq_sort_pairs_noalloc(uint32_t* keys, uint32_t* values, u
   if (st != RQ_SUCCESS) return st;
   if (n == 1) return RQ_SUCCESS;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  if (s) {  // the array's address is the current device's: the stream must belong to it
+    int cur = 0, sdev = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+      cudaGetLastError();
+      return RQ_ERROR_INVALID_ARGUMENT;
+    }
+    if (sdev != cur) return RQ_ERROR_INVALID_ARGUMENT;
+  }
   const int passes = (int)((key_bits + 7) / 8);
-  if (sort_status_words(n, passes) > kStatusWords) return RQ_ERROR_UNSUPPORTED;  // tile size mismatch
-  // Histograms, tile counters, look-back words and the error word must start
-  // at zero; the array keeps whatever the previous call left there.
-  if (cudaMemsetAsync(base + kHistOff, 0, (kWords - kHistOff) * sizeof(uint32_t), s) != cudaSuccess) {
+  const size_t status_words = sort_status_words(n, passes);
+  if (status_words > kStatusWords) return RQ_ERROR_UNSUPPORTED;  // tile size mismatch
+  // Histograms, tile counters, the look-back words of this sort's passes
+  // (contiguous from kStatusOff) and the error word must start at zero; the
+  // array keeps whatever the previous call left there.
+  if (cudaMemsetAsync(base + kHistOff, 0, (kStatusOff - kHistOff + status_words) * sizeof(uint32_t), s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(base + kErrOff, 0, sizeof(uint32_t), s) != cudaSuccess) {
     cudaGetLastError();
     return RQ_ERROR_CUDA;
   }

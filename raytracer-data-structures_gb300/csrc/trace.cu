@@ -27,7 +27,7 @@ constexpr int kThreads = 128;
 // expects it).  With perm, any-hit bits are set with atomicOr on a zeroed array.
 // At most 48 registers (10 blocks of 128 per SM): measured 3-4% faster on
 // the closest-hit triangle walk than the unconstrained 52.
-template <int KIND, bool ANY, bool COUNT = false>
+template <int KIND, bool ANY, bool COUNT = false, int STACK = kStackSize>
 __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const float4* __restrict__ rays,
                                                          uint32_t n, float4* __restrict__ hits,
                                                          uint32_t* __restrict__ occ, uint32_t* err,
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const
   if (i < n) {
     Ray ray = load_ray(rays, r);
     Closest c = {ray.tmax, kMiss, 0.f, 0.f};
-    occluded = walk_bvh2<KIND, ANY, COUNT, kStackSize>(bvh, ray, c, visits, tests, err);
+    occluded = walk_bvh2<KIND, ANY, COUNT, STACK>(bvh, ray, c, visits, tests, err);
     if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
   }
   if (ANY) {
@@ -115,9 +115,10 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_packet(Bvh2View bvh, con
   Ray ray = live ? load_ray(rays, r) : Ray{{0.f, 0.f, 0.f}, {0.f, 0.f, 1.f}, 0.f, 0.f};
   Closest c = {ray.tmax, kMiss, 0.f, 0.f};
   const SlabRay sr = slab_ray(ray.o, ray.d);
+  const bool ex = zero_dir(sr);
   const float* rb = bvh.root;
   float tn;
-  const bool in_root = live && slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn);
+  const bool in_root = live && slab_any(ex, sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn);
   uint32_t mask = __ballot_sync(0xffffffffu, in_root);
   uint32_t alive = mask;  // lanes still searching (any hit: not yet occluded)
   bool occluded = false;
@@ -139,8 +140,8 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_packet(Bvh2View bvh, con
       float tl = 0.f, tr = 0.f;
       if (act) {
         const float tfar = ANY ? ray.tmax : c.t;
-        hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
-        hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+        hl = slab_any(ex, sr, ray.o, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+        hr = slab_any(ex, sr, ray.o, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
       }
       const uint32_t ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
       if (ml && mr) {
@@ -207,9 +208,10 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_spec(Bvh2View bvh, const
     const Ray ray = load_ray(rays, r);
     Closest c = {ray.tmax, kMiss, 0.f, 0.f};
     const SlabRay sr = slab_ray(ray.o, ray.d);
+    const bool ex = zero_dir(sr);
     float tn;
     const float* rb = bvh.root;
-    if (slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
+    if (slab_any(ex, sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
       int2 stack[kStackSize];
       int sp = 0;
       int cur = bvh.n_internal ? 0 : -1;
@@ -227,8 +229,8 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_spec(Bvh2View bvh, const
           int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
           const float tfar = ANY ? ray.tmax : c.t;
           float tl, tr;
-          bool hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
-          bool hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+          bool hl = slab_any(ex, sr, ray.o, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+          bool hr = slab_any(ex, sr, ray.o, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
           if (hl && hr) {
             int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
             if (tr < tl) { int2 t = nearE; nearE = farE; farE = t; }
@@ -320,6 +322,7 @@ __global__ void __launch_bounds__(kThreads) k_trace_refill(Bvh2View bvh, const f
   int2 stack[kStackSize];
   Ray ray = {{0.f, 0.f, 0.f}, {0.f, 0.f, 1.f}, 0.f, 0.f};
   SlabRay sr = slab_ray(ray.o, ray.d);
+  bool ex = false;
   Closest c = {0.f, kMiss, 0.f, 0.f};
   int cur = 0, cnt = 0, sp = 0;
   uint32_t r = 0, steps = 0;
@@ -339,9 +342,10 @@ __global__ void __launch_bounds__(kThreads) k_trace_refill(Bvh2View bvh, const f
           ray = load_ray(rays, r);
           c = {ray.tmax, kMiss, 0.f, 0.f};
           sr = slab_ray(ray.o, ray.d);
+          ex = zero_dir(sr);
           float tn;
           const float* rb = bvh.root;
-          if (slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
+          if (slab_any(ex, sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) {
             active = true;
             sp = 0;
             steps = 0;
@@ -366,8 +370,8 @@ __global__ void __launch_bounds__(kThreads) k_trace_refill(Bvh2View bvh, const f
       int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
       const float tfar = ANY ? ray.tmax : c.t;
       float tl, tr;
-      bool hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
-      bool hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+      bool hl = slab_any(ex, sr, ray.o, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+      bool hr = slab_any(ex, sr, ray.o, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
       if (hl && hr) {
         int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
         if (tr < tl) { int2 t = nearE; nearE = farE; farE = t; }
@@ -595,10 +599,12 @@ __global__ void __launch_bounds__(kThreads) k_brute(const float4* __restrict__ p
 
 template <int KIND, bool ANY>
 void dispatch_bvh2(int traversal, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
-                   uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s) {
+                   uint32_t* occ, uint32_t* err, const uint32_t* perm, bool small_stack, cudaStream_t s) {
   uint32_t g = (n + kThreads - 1) / kThreads;
   if (traversal == RQ_TRAVERSAL_REFERENCE)
     k_trace_ref<KIND, ANY><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err);
+  else if (small_stack)
+    k_trace_fast<KIND, ANY, false, kDebugStack><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr, perm);
   else
     k_trace_fast<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr, perm);
 }
@@ -638,17 +644,17 @@ void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const floa
 
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
                        uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
-                       const uint32_t* perm) {
+                       const uint32_t* perm, bool small_stack) {
   if (n == 0) return;
   count_launch();
   if (traversal == RQ_TRAVERSAL_REFERENCE) perm = nullptr;
   if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
   if (kind == kTriangles) {
-    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, perm, s);
-    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, perm, s);
+    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
+    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
   } else {
-    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, perm, s);
-    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, perm, s);
+    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
+    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
   }
 }
 

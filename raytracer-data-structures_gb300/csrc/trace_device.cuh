@@ -92,14 +92,15 @@ __device__ __forceinline__ void load_node(const float4* nd, float4& a, float4& b
 
 // FAST walk of one ray through a BVH2: near child first, far child on a
 // per-thread stack of STACK entries, boxes clipped to [tmin, closest hit].
+// EXACT: the exact-sign box test (rays with a zero direction component).
 // Returns true when an any-hit query found a hit.
-template <int KIND, bool ANY, bool COUNT, int STACK>
-__device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
-                                          uint32_t& tests, uint32_t* err) {
+template <int KIND, bool ANY, bool COUNT, int STACK, bool EXACT>
+__device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                               uint32_t& tests, uint32_t* err) {
   const SlabRay sr = slab_ray(ray.o, ray.d);
   float tn;
   const float* rb = bvh.root;
-  if (!slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
+  if (!slab_box<EXACT>(sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
   int2 stack[STACK];
   int sp = 0;
   int cur = bvh.n_internal ? 0 : -1;
@@ -122,8 +123,8 @@ __device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, C
       if (COUNT) ++visits;
       const float tfar = ANY ? ray.tmax : c.t;
       float tl, tr;
-      bool hl = slab_fast(sr, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
-      bool hr = slab_fast(sr, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+      bool hl = slab_box<EXACT>(sr, ray.o, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+      bool hr = slab_box<EXACT>(sr, ray.o, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
       if (hl && hr) {
         int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
         if (tr < tl) { int2 t = nearE; nearE = farE; farE = t; }
@@ -144,6 +145,14 @@ __device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, C
     cur = e.x;
     cnt = e.y;
   }
+}
+
+// walk_bvh2_form with the box test each ray needs.
+template <int KIND, bool ANY, bool COUNT, int STACK>
+__device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* err) {
+  return zero_dir(slab_ray(ray.o, ray.d)) ? walk_bvh2_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, c, visits, tests, err)
+                         : walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
 }
 
 // Sum the per-thread visit / test counts of a warp into counters[0..1].
@@ -186,13 +195,13 @@ __device__ __forceinline__ int pick(const int4& v, uint32_t k) {
 
 // FAST walk of one ray through the collapsed 4-wide BVH.  Returns true when
 // an any-hit query found a hit.
-template <int KIND, bool ANY, bool COUNT, int STACK>
-__device__ __forceinline__ bool walk_bvh4(const Bvh4View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
-                                          uint32_t& tests, uint32_t* err) {
+template <int KIND, bool ANY, bool COUNT, int STACK, bool EXACT>
+__device__ __forceinline__ bool walk_bvh4_form(const Bvh4View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                               uint32_t& tests, uint32_t* err) {
   const SlabRay sr = slab_ray(ray.o, ray.d);
   float tn;
   const float* rb = bvh.root;
-  if (!slab_fast(sr, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
+  if (!slab_box<EXACT>(sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
   int2 stack[STACK];
   int sp = 0;
   int cur = bvh.n_binary ? 0 : -1;
@@ -212,13 +221,13 @@ __device__ __forceinline__ bool walk_bvh4(const Bvh4View& bvh, const Ray& ray, C
       const float tfar = ANY ? ray.tmax : c.t;
       float t0, t1, t2, t3;
       uint32_t k0 = 0xFFFFFFFFu, k1 = 0xFFFFFFFFu, k2 = 0xFFFFFFFFu, k3 = 0xFFFFFFFFu;
-      if (ct.x >= 0 && slab_fast(sr, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, ray.tmin, tfar, t0))
+      if (ct.x >= 0 && slab_box<EXACT>(sr, ray.o, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, ray.tmin, tfar, t0))
         k0 = (order_key(t0) & ~3u) | 0u;
-      if (ct.y >= 0 && slab_fast(sr, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, ray.tmin, tfar, t1))
+      if (ct.y >= 0 && slab_box<EXACT>(sr, ray.o, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, ray.tmin, tfar, t1))
         k1 = (order_key(t1) & ~3u) | 1u;
-      if (ct.z >= 0 && slab_fast(sr, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, ray.tmin, tfar, t2))
+      if (ct.z >= 0 && slab_box<EXACT>(sr, ray.o, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, ray.tmin, tfar, t2))
         k2 = (order_key(t2) & ~3u) | 2u;
-      if (ct.w >= 0 && slab_fast(sr, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, ray.tmin, tfar, t3))
+      if (ct.w >= 0 && slab_box<EXACT>(sr, ray.o, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, ray.tmin, tfar, t3))
         k3 = (order_key(t3) & ~3u) | 3u;
       // A hit key is at most order_key(+inf) | 3 < 0xFFFFFFFF, so misses sort last.
       const int m = (k0 != 0xFFFFFFFFu) + (k1 != 0xFFFFFFFFu) + (k2 != 0xFFFFFFFFu) + (k3 != 0xFFFFFFFFu);
@@ -247,5 +256,11 @@ __device__ __forceinline__ bool walk_bvh4(const Bvh4View& bvh, const Ray& ray, C
   }
 }
 
+template <int KIND, bool ANY, bool COUNT, int STACK>
+__device__ __forceinline__ bool walk_bvh4(const Bvh4View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* err) {
+  return zero_dir(slab_ray(ray.o, ray.d)) ? walk_bvh4_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, c, visits, tests, err)
+                         : walk_bvh4_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
+}
 
 }  // namespace rq

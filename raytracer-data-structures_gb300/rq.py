@@ -222,6 +222,8 @@ def load(build_if_missing=True):
         "rq_accel_export_bvh2": (i32, [vp, vp, vp, vp, vp]),
         "rq_accel_export_kd": (i32, [vp, vp, vp, vp]),
         "rq_accel_export_bvh4": (i32, [vp, vp, vp, vp]),
+        "rq_accel_import_bvh2": (i32, [vp, vp, vp, u32, vp, u32, vp, vp]),
+        "rq_set_debug": (i32, [vp, vp]),
         "rq_trace_closest": (i32, [vp, vp, vp, u32, vp, u32]),
         "rq_trace_any": (i32, [vp, vp, vp, u32, vp, u32]),
         "rq_morton_codes": (i32, [vp, vp, vp, u32]),
@@ -529,6 +531,22 @@ class Engine:
         self._check(load().rq_accel_export_bvh2(self.ctx, accel.handle, nodes.ctypes.data, order.ctypes.data,
                                                 codes.ctypes.data if codes is not None else None))
         return nodes, order, codes, np.array(inf.root_bounds, np.float32), inf
+
+    def import_bvh2(self, scene, nodes, order, root_bounds):
+        """rq_accel_import_bvh2: a BVH2 structure from host arrays in export_bvh2's layout."""
+        nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1, 16)
+        order = np.ascontiguousarray(order, np.uint32)
+        root = np.ascontiguousarray(root_bounds, np.float32).reshape(6)
+        h = C.c_void_p()
+        self._check(load().rq_accel_import_bvh2(self.ctx, scene.handle, nodes.ctypes.data if len(nodes) else None,
+                                                len(nodes), order.ctypes.data, len(order), root.ctypes.data,
+                                                C.byref(h)))
+        return Accel(self, h, scene, BVH)
+
+    def set_debug(self, sort_stall=0, small_stack=0):
+        """rq_set_debug: test hooks that make device-side guards fire (all 0: off)."""
+        d = (C.c_uint32 * 2)(int(sort_stall), int(small_stack))
+        self._check(load().rq_set_debug(self.ctx, C.byref(d)))
 
     def export_bvh4(self, accel):
         """Collapsed 4-wide nodes, (n, 32) float32 (structures built with node_width 4)."""

@@ -17,6 +17,8 @@ Value noise: pseudo-random values on the integer lattice, blended with
 smoothstep weights; fBm sums octaves with lacunarity 2 and gain 0.5.  Lattice
 values come from a 32-bit integer hash of (ix, iy, iz, seed).
 """
+import functools
+
 import numpy as np
 
 from rq import RAY_DTYPE, MISS
@@ -70,7 +72,17 @@ def fbm3(p, octaves, seed, base_freq=1.0):
 
 # ------------------------------------------------------------------ meshes
 
+@functools.lru_cache(maxsize=None)
 def icosphere(level):
+    """Unit icosphere subdivided `level` times: 20 * 4^level triangles.  Cached
+    per level; the arrays are read-only (callers derive new arrays from them)."""
+    v, f = _icosphere(level)
+    v.flags.writeable = False
+    f.flags.writeable = False
+    return v, f
+
+
+def _icosphere(level):
     t = (1.0 + 5 ** 0.5) / 2.0
     v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t],
                   [0, 1, -t], [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
@@ -160,6 +172,28 @@ def heightfield(nx=1001, ny=500, amplitude=0.3, octaves=5, seed=2):
     a, b, c, d = i, i + 1, i + nx, i + nx + 1
     f = np.concatenate([np.stack([a, b, d], 1), np.stack([a, d, c], 1)]).astype(np.uint32)
     return verts, f
+
+
+def mixed_meshes(n, tri_lo, tri_hi, seed, kinds=("icosphere", "heightfield")):
+    """n seeded meshes whose target triangle counts are log-uniform in
+    [tri_lo, tri_hi]; each is, by seed, a displaced icosphere (3-octave value
+    noise, amplitude 0.15, in the unit cube; the subdivision level nearest the
+    target on a log scale, so counts are 20 * 4^level) or an fBm heightfield
+    (5 octaves, amplitude 0.3; a square vertex grid of about the target
+    count).  Returns [(verts, idx, kind)]; callers record the actual counts."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        t = float(np.exp(rng.uniform(np.log(tri_lo), np.log(tri_hi))))
+        kind = kinds[int(rng.integers(len(kinds)))]
+        if kind == "icosphere":
+            level = int(np.clip(np.round(np.log(t / 20.0) / np.log(4.0)), 2, 8))
+            v, f = displaced_icosphere(level, seed=seed + 1000 + k)
+        else:
+            nx = max(2, int(round(np.sqrt(t / 2.0)))) + 1
+            v, f = heightfield(nx, nx, amplitude=0.3, octaves=5, seed=seed + 1000 + k)
+        out.append((v, f, kind))
+    return out
 
 
 def chain_clusters(grid=16, group=32, levels=30):

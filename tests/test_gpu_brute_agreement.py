@@ -29,3 +29,39 @@ def test_fast_closest_hit_equals_brute_force_on_terrain(engine, rqm, acc_name):
     for rays, want in ((cam, want_c), (bounce, want_b)):
         got = engine.trace_closest(acc, rays)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def _grid_aligned_axis_rays(v):
+    """Rays straight down (direction (0, 0, -1)) from above every vertex of a
+    grid, plus rays along x and y through the grid's rows at vertex height:
+    every ray has zero direction components and sits exactly on box planes,
+    where the fused plane distance fma(b, inv, -o*inv) breaks down."""
+    import oracle_py as O
+    down = O.make_rays(np.stack([v[:, 0], v[:, 1], np.full(len(v), 2.0, np.float32)], 1).astype(np.float32),
+                       np.tile(np.array([[0, 0, -1]], np.float32), (len(v), 1)))
+    row = v[:: 7]
+    along_x = O.make_rays(np.stack([np.full(len(row), -3.0, np.float32), row[:, 1], row[:, 2]], 1),
+                          np.tile(np.array([[1, 0, 0]], np.float32), (len(row), 1)))
+    along_y = O.make_rays(np.stack([row[:, 0], np.full(len(row), 3.0, np.float32), row[:, 2]], 1),
+                          np.tile(np.array([[0, -1, 0]], np.float32), (len(row), 1)))
+    return np.concatenate([down, along_x, along_y])
+
+
+@pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])
+@pytest.mark.parametrize("width", [2, 4])
+def test_axis_aligned_rays_on_box_planes_equal_brute_force(engine, rqm, oracle, acc_name, width):
+    v, f = scenes.heightfield(81, 41, amplitude=0.3, octaves=5, seed=13)
+    rays = _grid_aligned_axis_rays(v)
+    s = engine.scene_triangles(v, f)
+    brute = engine.build(s, rqm.NONE)
+    want = engine.trace_closest(brute, rays)
+    want_any = engine.trace_any(brute, rays)
+    assert (want["prim"] != rqm.MISS).mean() > 0.95  # the downward rays all land on the terrain
+    engine.configure(node_width=width)
+    acc = engine.build(s, acc_name)
+    got = engine.trace_closest(acc, rays)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(engine.trace_any(acc, rays), want_any)
+    prims, _, _ = oracle.tri_prims(v, f)
+    assert np.array_equal(want.view(np.uint32),
+                          oracle.trace_brute(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, prims, rays).view(np.uint32))

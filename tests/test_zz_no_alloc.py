@@ -24,7 +24,11 @@ def _sorted_by_existing_entry_point(engine, keys, vals, bits):
 def test_noalloc_sort_matches_rq_sort_pairs_on_two_calls_in_a_row(engine, rqm):
     import torch
     stream = torch.cuda.current_stream()
-    cases = [(rqm.SORT_NOALLOC_MAX_PAIRS, 30, 1), (100_003, 32, 2)]  # second call is smaller: stale scratch
+    # Key widths of 4, 1 and 3 digit passes: after an odd number of passes the
+    # result is copied back from the fixed array into the caller's buffers.
+    # Each call is smaller than the one before, so stale contents of the
+    # shared array would show.
+    cases = [(rqm.SORT_NOALLOC_MAX_PAIRS, 30, 1), (100_003, 32, 2), (77_777, 7, 3), (50_001, 24, 4)]
     for n, bits, seed in cases:
         rng = np.random.default_rng(seed)
         keys = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
@@ -48,3 +52,11 @@ def test_noalloc_sort_rejects_sizes_beyond_its_array(rqm):
     dk = torch.zeros(n, dtype=torch.int32, device="cuda")
     dv = torch.zeros(n, dtype=torch.int32, device="cuda")
     assert rqm.sort_pairs_noalloc(dk.data_ptr(), dv.data_ptr(), n, 32, None) == 1  # INVALID_ARGUMENT
+
+
+def test_noalloc_sort_single_pair_is_left_unchanged(rqm):
+    import torch
+    dk = torch.tensor([123456789], dtype=torch.int32, device="cuda")
+    dv = torch.tensor([42], dtype=torch.int32, device="cuda")
+    assert rqm.sort_pairs_noalloc(dk.data_ptr(), dv.data_ptr(), 1, 32, None) == 0
+    assert int(dk.item()) == 123456789 and int(dv.item()) == 42
