@@ -245,7 +245,7 @@ def run_ours(args):
     morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
     tuning = {}
     best = None
-    candidates = [(w, m) for w in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4) for m in morton_names]
+    candidates = [(w, m) for w in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4, rq.NODE_WIDTH_8) for m in morton_names]
     if args.no_tune:  # the live tuner's choice on a GB300, for profiling the same kernel mix
         candidates = [(rq.NODE_WIDTH_2, rq.MORTON_SCENE_CUBE)]
     for width, morton in candidates:
@@ -282,7 +282,7 @@ def run_ours(args):
     _, acc, (node_width, morton_mode), sort_choice = best
     eng.configure(node_width=node_width, morton=morton_mode, ray_sort=rq.RAY_SORT_NONE,
                   scheduling=rq.SCHEDULING_THREAD_PER_RAY)
-    node_bytes = 128 if node_width == rq.NODE_WIDTH_4 else NODE_BYTES
+    node_bytes = 128 if node_width in (rq.NODE_WIDTH_4, rq.NODE_WIDTH_8) else NODE_BYTES
     log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}, morton {morton_names[morton_mode]}")
 
     # Traversal work of each query on these exact rays (the byte model's inputs).
@@ -711,8 +711,8 @@ def run_batch_leg(eng, stream, dev, args):
 
 
 def run_serve_leg(args):
-    """The serving loop under load: Poisson arrivals at 400 requests/s for a
-    few seconds; 32 resident displaced icospheres of 10k-2M triangles (log-uniform)
+    """The serving loop under load: Poisson arrivals at 400 requests/s (and
+    at 1,200/s, more than either path serves) for a few seconds; 32 resident displaced icospheres of 10k-2M triangles (log-uniform)
     plus new meshes (5% of requests name a mesh never seen before: upload +
     LBVH build on demand); resolution uniform over 320x240, 640x480, 1280x720,
     1920x1080, spp over 1, 2, 4, 8, 16; HBM budget 80 GB with LRU eviction.
@@ -721,39 +721,39 @@ def run_serve_leg(args):
     import rq
     import scenes
 
-    rng = np.random.default_rng(SEED + 50)
-    rate, secs = 400.0, (1.0 if args.small else 4.0)
+    secs = 1.0 if args.small else 4.0
     n_res, n_new_max = 32, 64
-
     # seeded displaced icospheres, 10k-2M triangles (log-uniform target, nearest subdivision level)
     pool = scenes.mixed_meshes(n_res + n_new_max, 1e4, 2e6, SEED + 200, kinds=("icosphere",))
     lib = {k: pool[k][:2] for k in range(n_res)}
     fresh = {1000 + k: pool[n_res + k][:2] for k in range(n_new_max)}
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * secs * 1.2)))
-    arrivals = arrivals[arrivals < secs]
     res = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
-    sched, new_ids = [], iter(sorted(fresh))
-    for k, t in enumerate(arrivals):
-        mid = next(new_ids, None) if rng.random() < 0.05 else None
-        if mid is None:
-            mid = int(rng.integers(n_res))
-        w, h = res[int(rng.integers(4))]
-        spp = int(rng.choice([1, 2, 4, 8, 16]))
-        az = rng.uniform(0, 6.283)
-        # an orbit around the mesh's centre (the meshes fill the unit cube)
-        view = rq.make_view(eye=(float(0.5 + 2.2 * np.cos(az)), float(0.5 + 2.2 * np.sin(az)),
-                                 float(0.5 + rng.uniform(-0.8, 0.8))),
-                            target=(0.5, 0.5, 0.5), up=(0.0, 0.0, 1.0), fov_deg=float(rng.uniform(35, 60)),
-                            light=(1.5, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=int(SEED + k))
-        sched.append((float(t), mid, view, w, h, spp))
-    out = {"requests": len(sched), "rate_per_s": rate, "seconds": secs,
-           "resident_meshes": n_res, "new_mesh_requests": sum(1 for s in sched if s[1] >= 1000),
-           "triangles_resident": int(sum(len(f) for _, f in lib.values()))}
-    for mode, batching in (("batched", True), ("one_per_step", False)):
-        srv = rq.Server(batching=batching, hbm_budget=80 << 30)
+
+    def schedule(rate, seed):
+        rng = np.random.default_rng(seed)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * secs * 1.3) + 16))
+        arrivals = arrivals[arrivals < secs]
+        sched, new_ids = [], iter(sorted(fresh))
+        for k, t in enumerate(arrivals):
+            mid = next(new_ids, None) if rng.random() < 0.05 else None
+            if mid is None:
+                mid = int(rng.integers(n_res))
+            w, h = res[int(rng.integers(4))]
+            spp = int(rng.choice([1, 2, 4, 8, 16]))
+            az = rng.uniform(0, 6.283)
+            # an orbit around the mesh's centre (the meshes fill the unit cube)
+            view = rq.make_view(eye=(float(0.5 + 2.2 * np.cos(az)), float(0.5 + 2.2 * np.sin(az)),
+                                     float(0.5 + rng.uniform(-0.8, 0.8))),
+                                target=(0.5, 0.5, 0.5), up=(0.0, 0.0, 1.0), fov_deg=float(rng.uniform(35, 60)),
+                                light=(1.5, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=int(seed + k))
+            sched.append((float(t), mid, view, w, h, spp))
+        return sched
+
+    def serve(sched, batching, budget):
+        srv = rq.Server(batching=batching, hbm_budget=budget)
         for mid, (v, f) in list(lib.items()) + list(fresh.items()):
             srv.add_mesh(mid, v, f)
-        for mid in lib:  # the library starts resident
+        for mid in lib:  # the library starts resident (as far as the budget allows)
             srv.wait(srv.submit(mid, sched[0][2], 32, 32, 1, keep_pixels=False), want_pixels=False)
         srv.reset_stats()
         t0 = time.perf_counter()
@@ -767,19 +767,40 @@ def run_serve_leg(args):
         wall = time.perf_counter() - t0
         st = srv.stats()
         rays = int(st.camera_rays + st.shadow_rays)
-        out[mode] = {"completed": int(st.completed), "rejected": int(st.rejected), "steps": int(st.batches),
-                     "builds": int(st.builds), "evictions": int(st.evictions),
-                     "p50_ms": round(st.latency_ms_p50, 3), "p99_ms": round(st.latency_ms_p99, 3),
-                     "mean_ms": round(st.latency_ms_mean, 3), "max_ms": round(st.latency_ms_max, 3),
-                     "wall_s": round(wall, 3), "busy_s": round(st.busy_s, 3), "rays": rays,
-                     "grays_s_wall": round(rays / wall / 1e9, 4), "grays_s_busy": round(rays / max(st.busy_s, 1e-9) / 1e9, 4)}
+        r = {"completed": int(st.completed), "rejected": int(st.rejected), "steps": int(st.batches),
+             "builds": int(st.builds), "evictions": int(st.evictions),
+             "p50_ms": round(st.latency_ms_p50, 3), "p99_ms": round(st.latency_ms_p99, 3),
+             "mean_ms": round(st.latency_ms_mean, 3), "max_ms": round(st.latency_ms_max, 3),
+             "wall_s": round(wall, 3), "busy_s": round(st.busy_s, 3), "rays": rays,
+             "grays_s_wall": round(rays / wall / 1e9, 4), "grays_s_busy": round(rays / max(st.busy_s, 1e-9) / 1e9, 4),
+             "resident_gb": round(st.resident_bytes / 1e9, 3)}
         for tk in tickets:
             srv.wait(tk, want_pixels=False)
         srv.close()
-        log(f"[bench] serve {mode}: {out[mode]}")
-    b, o = out["batched"], out["one_per_step"]
-    out["busy_rays_ratio"] = round(b["grays_s_busy"] / max(o["grays_s_busy"], 1e-9), 3)
-    out["p99_ratio"] = round(o["p99_ms"] / max(b["p99_ms"], 1e-9), 3)
+        return r
+
+    out = {"seconds": secs, "resident_meshes": n_res, "new_meshes": n_new_max,
+           "triangles_resident": int(sum(len(f) for _, f in lib.values())),
+           "triangles_library": int(sum(len(f) for _, f in list(lib.values()) + list(fresh.values()))),
+           "hbm_budget_gb": 80}
+    # the configured load, then an overloaded one (arrivals faster than either path serves them)
+    for rate in (400.0, 1200.0):
+        sched = schedule(rate, SEED + 50 + int(rate))
+        leg = {"requests": len(sched), "rate_per_s": rate, "new_mesh_requests": sum(1 for x in sched if x[1] >= 1000)}
+        for mode, batching in (("batched", True), ("one_per_step", False)):
+            leg[mode] = serve(sched, batching, 80 << 30)
+            log(f"[bench] serve {int(rate)}/s {mode}: {leg[mode]}")
+        b, o = leg["batched"], leg["one_per_step"]
+        leg["busy_rays_ratio"] = round(b["grays_s_busy"] / max(o["grays_s_busy"], 1e-9), 3)
+        leg["wall_rays_ratio"] = round(b["grays_s_wall"] / max(o["grays_s_wall"], 1e-9), 3)
+        leg["p99_ratio"] = round(o["p99_ms"] / max(b["p99_ms"], 1e-9), 3)
+        out[f"load_{int(rate)}"] = leg
+    # LRU residency under load: the overloaded schedule with a 4 GB budget
+    # (the library needs about 6.5 GB on the device): meshes are evicted and rebuilt
+    tight = serve(schedule(1200.0, SEED + 1250), True, 4 << 30)
+    tight["hbm_budget_gb"] = 4
+    out["tight_budget"] = tight
+    log(f"[bench] serve tight budget: {tight}")
     return out
 
 

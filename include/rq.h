@@ -95,12 +95,17 @@ typedef enum rq_scheduling_t {
 /* Node fan-out of BVH structures (RQ_BVH, RQ_LBVH), fixed when the structure
  * is built.  RQ_NODE_WIDTH_4 adds a collapsed 4-wide copy of the binary tree
  * (every even-depth node merged with its internal children: one 128-byte
- * node holds up to four child boxes) that FAST queries walk instead.  Hits
- * and occlusion bits are those of the binary tree; REFERENCE queries and
- * rq_accel_export_bvh2 keep using the binary nodes. */
+ * node holds up to four child boxes) that FAST queries walk instead.
+ * RQ_NODE_WIDTH_8 adds a compressed 8-wide copy (every node at a depth
+ * divisible by 3 holds its descendants three levels down: one 128-byte node
+ * with eight child boxes quantised to bytes, rounded outward, and the children
+ * placed by direction so each ray visits them in an order set by its
+ * direction's signs).  Hits and occlusion bits are those of the binary tree;
+ * REFERENCE queries and rq_accel_export_bvh2 keep using the binary nodes. */
 typedef enum rq_node_width_t {
   RQ_NODE_WIDTH_2 = 0, /* binary nodes (2 is accepted too) */
-  RQ_NODE_WIDTH_4 = 4
+  RQ_NODE_WIDTH_4 = 4,
+  RQ_NODE_WIDTH_8 = 8
 } rq_node_width_t;
 
 /* Ray reordering before FAST BVH2 traversal of batches of at least 65,536
@@ -264,12 +269,17 @@ rq_status_t rq_accel_get_info(rq_accel_t accel, rq_accel_info_t* info);
 rq_status_t rq_accel_export_bvh2(rq_ctx_t ctx, rq_accel_t accel, float* nodes, uint32_t* order,
                                  uint32_t* sorted_codes);
 rq_status_t rq_accel_export_kd(rq_ctx_t ctx, rq_accel_t accel, int32_t* nodes, int32_t* prim_idx);
-/* The collapsed 4-wide nodes of a structure built with RQ_NODE_WIDTH_4:
- * n_nodes receives the count; nodes (may be NULL) receives n_nodes * 32 words
- * [lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] link[4] count[4]].  A
- * child with link >= 0 is a 4-wide node, link < 0 a leaf holding slots
+/* The wide nodes of a structure built with RQ_NODE_WIDTH_4 or _8: n_nodes
+ * receives the count; nodes (may be NULL) receives n_nodes * 32 words.
+ * 4-wide: [lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] link[4] count[4]];
+ * a child with link >= 0 is a 4-wide node, link < 0 a leaf holding slots
  * [~link, ~link + count) of the binary tree's order; unused children have
- * count -1.  No reference counterpart: the reference's trees are binary. */
+ * count -1.  8-wide: [pm.x pm.y pm.z E] [qlo.x[8] qhi.x[8] as bytes] (y) (z)
+ * [(link, count) x 8]: E packs three biased exponents (bits 0-23) and the
+ * mask of used slots (bits 24-31); child plane = fma(2^(E_a - 127),
+ * 1 + q * 2^-15, pm_a); count 0 -> 8-wide node `link`, count > 0 -> leaf of
+ * slots [link, link + count).  No reference counterpart: the reference's
+ * trees are binary. */
 rq_status_t rq_accel_export_bvh4(rq_ctx_t ctx, rq_accel_t accel, float* nodes, uint32_t* n_nodes);
 
 /* A BVH2 structure from host arrays in rq_accel_export_bvh2's layout (nodes =

@@ -158,10 +158,12 @@ BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, 
   if (s.n == 0) return BuildResult::error(RQ_ERROR_EMPTY_SCENE, "empty scene");
   a.node_width = 2;
   if (type == RQ_LBVH || type == RQ_BVH) {
-    if (cfg.node_width != RQ_NODE_WIDTH_2 && cfg.node_width != 2 && cfg.node_width != RQ_NODE_WIDTH_4)
-      return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "node_width must be 2 or 4");
+    if (cfg.node_width != RQ_NODE_WIDTH_2 && cfg.node_width != 2 && cfg.node_width != RQ_NODE_WIDTH_4 &&
+        cfg.node_width != RQ_NODE_WIDTH_8)
+      return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "node_width must be 2, 4 or 8");
     BuildResult r = type == RQ_LBVH ? build_lbvh(s, cfg, a, sc, err, st) : build_median_bvh(s, a, sc, err, st);
     if (r.ok() && cfg.node_width == RQ_NODE_WIDTH_4) r = collapse_bvh4(a, sc, err, st);
+    if (r.ok() && cfg.node_width == RQ_NODE_WIDTH_8) r = collapse_bvh8(a, sc, err, st);
     return r;
   }
   switch (type) {
@@ -172,6 +174,11 @@ BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, 
 }
 
 static Bvh4View bvh4_view(const AccelBuffers& a) {
+  return {a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+          a.root.as<const float>(), a.n_nodes, a.n_slots};
+}
+
+static Bvh8View bvh8_view(const AccelBuffers& a) {
   return {a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
           a.root.as<const float>(), a.n_nodes, a.n_slots};
 }
@@ -187,6 +194,8 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
     launch_trace_kd(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
   } else if (a.node_width == 4 && traversal == RQ_TRAVERSAL_FAST) {
     launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st);
+  } else if (a.node_width == 8 && traversal == RQ_TRAVERSAL_FAST) {
+    launch_trace_bvh8(s.kind, any, bvh8_view(a), q.rays, q.n, q.hits, q.occ, err, st);
   } else {
     Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
                a.root.as<const float>(), a.n_nodes, a.n_slots};
@@ -199,9 +208,10 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   const bool bvh2 = type == RQ_LBVH || type == RQ_BVH;
   const bool fast = bvh2 && cfg.traversal == RQ_TRAVERSAL_FAST;
   const bool sorted = fast && cfg.ray_sort != RQ_RAY_SORT_NONE && q.n >= kRaySortMin;
-  const bool refill = fast && cfg.scheduling == RQ_SCHEDULING_LANE_REFILL && a.node_width != 4;
-  const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && a.node_width != 4;
-  const bool packet = fast && cfg.scheduling == RQ_SCHEDULING_WARP_PACKET && a.node_width != 4;
+  const bool wide = a.node_width == 4 || a.node_width == 8;
+  const bool refill = fast && cfg.scheduling == RQ_SCHEDULING_LANE_REFILL && !wide;
+  const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && !wide;
+  const bool packet = fast && cfg.scheduling == RQ_SCHEDULING_WARP_PACKET && !wide;
   if (!sorted && !refill && !spec && !packet) {
     launch_query(type, s, a, cfg.traversal, any, q, err, st);
     RQ_B(cudaGetLastError(), "trace launch");
@@ -242,6 +252,7 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
     return {};
   }
   if (a.node_width == 4) launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
+  else if (a.node_width == 8) launch_trace_bvh8(s.kind, any, bvh8_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
   else launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm, q.small_stack);
   RQ_B(cudaGetLastError(), "trace launch");
   return {};
@@ -253,6 +264,11 @@ BuildResult trace_counted(int type, const SceneView& s, const AccelBuffers& a, b
     return BuildResult::error(RQ_ERROR_UNSUPPORTED, "traversal counters exist for BVH2 structures");
   if (a.node_width == 4) {
     launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, nullptr, counters);
+    RQ_B(cudaGetLastError(), "counted trace launch");
+    return {};
+  }
+  if (a.node_width == 8) {
+    launch_trace_bvh8(s.kind, any, bvh8_view(a), q.rays, q.n, q.hits, q.occ, err, st, nullptr, counters);
     RQ_B(cudaGetLastError(), "counted trace launch");
     return {};
   }

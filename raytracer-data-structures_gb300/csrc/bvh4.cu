@@ -157,6 +157,11 @@ __global__ void __launch_bounds__(kThreads) k_fill4(const float4* __restrict__ n
 
 }  // namespace
 
+void launch_parents(const float4* nodes, uint32_t n, uint32_t* parent, uint32_t* err, cudaStream_t st) {
+  count_launch();
+  k_parents<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(nodes, n, parent, err);
+}
+
 // Upper bound of the 4-wide node count: every even-depth node but the root
 // has an odd-depth parent with at most two children, so even <= 1 + 2 * odd
 // and even <= (2n + 1) / 3.

@@ -187,8 +187,9 @@ rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.traversal must be FAST or REFERENCE");
   if (s->morton != RQ_MORTON_SCENE_BOUNDS && s->morton != RQ_MORTON_REFERENCE && s->morton != RQ_MORTON_SCENE_CUBE)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.morton must be SCENE_BOUNDS, REFERENCE or SCENE_CUBE");
-  if (s->node_width != RQ_NODE_WIDTH_2 && s->node_width != 2 && s->node_width != RQ_NODE_WIDTH_4)
-    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.node_width must be 2 or 4");
+  if (s->node_width != RQ_NODE_WIDTH_2 && s->node_width != 2 && s->node_width != RQ_NODE_WIDTH_4 &&
+      s->node_width != RQ_NODE_WIDTH_8)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.node_width must be 2, 4 or 8");
   if (s->ray_sort < RQ_RAY_SORT_NONE || s->ray_sort > RQ_RAY_SORT_OCTANT_MORTON3)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.ray_sort out of range");
   if (s->scheduling < RQ_SCHEDULING_THREAD_PER_RAY || s->scheduling > RQ_SCHEDULING_WARP_PACKET)
@@ -544,8 +545,10 @@ rq_status_t rq_build_batched(rq_ctx_t ctx, const rq_scene_t* scenes, uint32_t n,
     a->batch = store;
     a->batch_index = k;
     out[k] = a;
-    if (ctx->settings.node_width == RQ_NODE_WIDTH_4) {
-      BuildResult r = collapse_bvh4(a->buf, ctx->scratch, ctx->d_err, ctx->stream);
+    if (ctx->settings.node_width == RQ_NODE_WIDTH_4 || ctx->settings.node_width == RQ_NODE_WIDTH_8) {
+      BuildResult r = ctx->settings.node_width == RQ_NODE_WIDTH_4
+                          ? collapse_bvh4(a->buf, ctx->scratch, ctx->d_err, ctx->stream)
+                          : collapse_bvh8(a->buf, ctx->scratch, ctx->d_err, ctx->stream);
       if (!r.ok()) {
         undo(k + 1);
         return r.cuda != cudaSuccess ? cuda_fail(ctx, r.cuda, r.what) : fail(ctx, r.status, r.what);
@@ -575,8 +578,9 @@ rq_status_t rq_accel_rebuild_batched(rq_ctx_t ctx, const rq_accel_t* accels, uin
   for (uint32_t k = 0; k < n; ++k) {
     AccelBuffers& b = accels[k]->buf;
     b.node_width = 2;
-    if (ctx->settings.node_width == RQ_NODE_WIDTH_4) {
-      BuildResult r = collapse_bvh4(b, ctx->scratch, ctx->d_err, ctx->stream);
+    if (ctx->settings.node_width == RQ_NODE_WIDTH_4 || ctx->settings.node_width == RQ_NODE_WIDTH_8) {
+      BuildResult r = ctx->settings.node_width == RQ_NODE_WIDTH_4 ? collapse_bvh4(b, ctx->scratch, ctx->d_err, ctx->stream)
+                                                                  : collapse_bvh8(b, ctx->scratch, ctx->d_err, ctx->stream);
       if (!r.ok()) return r.cuda != cudaSuccess ? cuda_fail(ctx, r.cuda, r.what) : fail(ctx, r.status, r.what);
     }
   }
@@ -602,7 +606,7 @@ rq_status_t rq_accel_get_info(rq_accel_t a, rq_accel_info_t* info) {
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(words, a->buf.root.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
     RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     std::memcpy(info->root_bounds, words, 24);
-    if (bvh2 && a->buf.node_width == 4) std::memcpy(&info->n_wide_nodes, words + 6, 4);
+    if (bvh2 && (a->buf.node_width == 4 || a->buf.node_width == 8)) std::memcpy(&info->n_wide_nodes, words + 6, 4);
   }
   return RQ_SUCCESS;
 }
@@ -626,12 +630,12 @@ rq_status_t rq_accel_export_bvh2(rq_ctx_t ctx, rq_accel_t a, float* nodes, uint3
 rq_status_t rq_accel_export_bvh4(rq_ctx_t ctx, rq_accel_t a, float* nodes, uint32_t* n_nodes) {
   if (!a || !n_nodes) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null accel or count");
   RQ_TRY(bind(ctx));
-  if ((a->type != RQ_BVH && a->type != RQ_LBVH) || a->buf.node_width != 4)
-    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "not built with node_width 4");
+  if ((a->type != RQ_BVH && a->type != RQ_LBVH) || (a->buf.node_width != 4 && a->buf.node_width != 8))
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "not built with node_width 4 or 8");
   uint32_t n4 = 0;
   RQ_TRY_CUDA(ctx, cudaMemcpyAsync(&n4, a->buf.root.as<uint32_t>() + 6, 4, cudaMemcpyDeviceToHost, ctx->stream));
   RQ_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (n4 > a->buf.n4_cap) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed 4-wide node count");
+  if (n4 > a->buf.n4_cap) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed wide node count");
   *n_nodes = n4;
   if (nodes && n4) {
     RQ_TRY_CUDA(ctx, cudaMemcpyAsync(nodes, a->buf.nodes4.p, (size_t)n4 * 128, cudaMemcpyDeviceToHost, ctx->stream));
@@ -956,7 +960,7 @@ static rq_status_t batch_tables(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t
       return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "structures mix primitive kinds or node widths");
     if (ray_offsets[k + 1] < ray_offsets[k]) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "ray_offsets decrease");
     const AccelBuffers& b = a->buf;
-    views[k] = {b.node_width == 4 ? b.nodes4.as<const float4>() : b.nodes.as<const float4>(), b.prims.as<const float4>(),
+    views[k] = {b.node_width != 2 ? b.nodes4.as<const float4>() : b.nodes.as<const float4>(), b.prims.as<const float4>(),
                 b.order.as<const uint32_t>(), b.root.as<const float>(), b.n_nodes, b.n_slots};
   }
   if (ray_offsets[n] >= (1u << 31)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "2^31 or more rays");
@@ -970,7 +974,7 @@ static rq_status_t batch_tables(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t
   t = BatchedTrace();
   t.kind = accels[0]->scene->kind;
   t.any = any;
-  t.width = accels[0]->buf.node_width == 4 ? 4 : 2;
+  t.width = (int)accels[0]->buf.node_width;
   t.views = reinterpret_cast<const Bvh2View*>(base);
   t.roff = reinterpret_cast<const uint32_t*>(base + vbytes);
   t.n_views = n;
@@ -1131,6 +1135,7 @@ rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_ac
     br = build_batch(*p->store, ctx->settings.morton, ctx->d_err, cap);
     for (uint32_t k = 0; br.ok() && k < n_accels; ++k)
       if (accels[k]->buf.node_width == 4) br = collapse_bvh4(accels[k]->buf, ctx->scratch, ctx->d_err, cap);
+      else if (accels[k]->buf.node_width == 8) br = collapse_bvh8(accels[k]->buf, ctx->scratch, ctx->d_err, cap);
   }
   BatchedTrace qt = p->trace;
   if (ce == cudaSuccess && br.ok() && p->ordered)

@@ -27,11 +27,11 @@ struct AccelBuffers {
   DevBuf root;         // 8 floats: root box (min xyz, max xyz)
   DevBuf kd_nodes;     // KD: int4 per node
   DevBuf kd_idx;       // KD: primitive indices
-  DevBuf nodes4;       // collapsed 4-wide nodes, 128 B each (node_width 4)
+  DevBuf nodes4;       // wide nodes, 128 B each: collapsed 4-wide (node_width 4) or compressed 8-wide (8)
   uint32_t n_nodes = 0;
   uint32_t n_slots = 0;
   uint32_t max_depth = 0;
-  uint32_t node_width = 2;  // BVH2 structures: 2, or 4 when nodes4 holds the collapsed tree
+  uint32_t node_width = 2;  // BVH2 structures: 2, or 4 / 8 when nodes4 holds a wide copy
   uint32_t n4_cap = 0;      // bound of the 4-wide node count (exact count: root word 6)
   void release() {
     nodes.release(); prims.release(); order.release(); codes.release(); root.release();
@@ -103,6 +103,10 @@ BuildResult build_kd_tree(const SceneView& s, int max_depth, AccelBuffers& a, Bu
 // into the root buffer's word 6).
 uint32_t bvh4_node_cap(uint32_t n_internal);
 BuildResult collapse_bvh4(AccelBuffers& a, BuildScratch& sc, uint32_t* err, cudaStream_t st);
+// Compressed 8-wide copy of the binary nodes (in a.nodes4, 128 B per node;
+// node count in root word 6; bvh8.cu).
+uint32_t bvh8_node_cap(uint32_t n_internal);
+BuildResult collapse_bvh8(AccelBuffers& a, BuildScratch& sc, uint32_t* err, cudaStream_t st);
 
 // ---------------------------------------------------------- batched build
 struct BatchDesc {  // device copy per scene: its geometry

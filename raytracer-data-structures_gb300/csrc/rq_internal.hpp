@@ -195,6 +195,19 @@ void launch_trace_bvh4(int kind, bool any, const Bvh4View& v, const float4* rays
                        uint32_t* occ, uint32_t* err, cudaStream_t s, const uint32_t* perm = nullptr,
                        unsigned long long* counters = nullptr);
 
+// Compressed 8-wide BVH over the same slot-ordered payload (layout in bvh8.cu).
+struct Bvh8View {
+  const float4* nodes;    // 8 float4 per node
+  const float4* prims;
+  const uint32_t* order;
+  const float* root;
+  uint32_t n_binary;      // binary internal nodes (0: the root is one leaf)
+  uint32_t n_slots;
+};
+void launch_trace_bvh8(int kind, bool any, const Bvh8View& v, const float4* rays, uint32_t n, float4* hits,
+                       uint32_t* occ, uint32_t* err, cudaStream_t s, const uint32_t* perm = nullptr,
+                       unsigned long long* counters = nullptr);
+
 // Rays of many BVH structures in one persistent launch (trace_batched.cu).
 // views: device array of n_views structures (nodes = 4-wide nodes when
 // width == 4); roff: device array of n_views + 1 ray offsets; work: one

@@ -1,27 +1,37 @@
 // Serving loop (rq_server_*): render requests against a library of meshes,
-// served by one worker thread that owns its own context.
+// served by one worker thread that owns its own contexts.
 //
 //  * Admission: a request must name a registered mesh and fit the ray limit
 //    of one batch; its mesh must fit the HBM budget.  Others complete at once
 //    with an error status.
 //  * Residency: meshes live on the host; a request's mesh is uploaded and its
-//    LBVH built when needed.  Resident scenes + structures stay within the
-//    HBM budget by evicting the least recently used meshes that the batch
-//    being formed does not need.
-//  * Continuous batching: each step takes the waiting requests in arrival
-//    order up to the batch limits and renders all of them as one wavefront:
-//    camera rays of every request, one persistent many-structure closest-hit
-//    query, shading, one many-structure shadow query, the light terms and
-//    every request's pixels, then one download.  batching = 0 serves one
-//    request per step (the one-request-per-launch comparison).
+//    LBVH built when needed, through a second context on its own stream, so
+//    uploads and builds run on the GPU beside the rendering already in
+//    flight.  Resident scenes + structures and the wavefront buffers stay
+//    within the HBM budget: the least recently used meshes that neither the
+//    batch being formed nor a batch in flight needs are evicted.
+//  * Continuous batching (batching = 1): two wavefront slots, each with its
+//    own stream and buffers.  While one slot's step runs on the GPU, the
+//    requests that arrive are formed into the next step (everything waiting,
+//    in arrival order, up to the batch limits and the memory budget) and
+//    launched on the other slot, so consecutive steps overlap on the device.
+//    A step renders all its requests as one wavefront: camera rays of every
+//    request, one persistent many-structure closest-hit query, shading, one
+//    many-structure shadow query, the light terms and every request's pixels,
+//    then one download; a host callback on the slot's stream tells the worker
+//    when it has landed.  batching = 0 serves one request per step on one
+//    slot, each step waited for before the next (the one-request-per-launch
+//    comparison).
 //  * Latency: from rq_server_submit to the moment the request's pixels are
 //    in host memory; the worker keeps every completed request's latency for
-//    the percentile statistics.
+//    the percentile statistics.  Busy time is the time at least one step is
+//    in flight.
 //
 // A request renders exactly what rq_render renders for the same view with
 // bounces = 0 (the same per-sample device code), whether it is served alone
 // or among others.  The reference has no serving path; this is the engine's.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -33,7 +43,6 @@
 
 #include "rq_handles.hpp"
 #include "view_device.cuh"
-
 namespace rq {
 namespace {
 
@@ -93,13 +102,18 @@ __global__ void __launch_bounds__(kThreads) k_serve_pixels(const ServeReq* __res
 
 using Clock = std::chrono::steady_clock;
 
+// Wavefront bytes per camera sample: camera/mirror ray 32, shadow ray 32,
+// hit 16, colour + weight 16, pending light term 16, occlusion bit.
+constexpr uint64_t kSampleBytes = 112;
+
 struct Mesh {
   std::vector<float> verts;
   std::vector<uint32_t> idx;
   rq_scene_t scene = nullptr;
   rq_accel_t accel = nullptr;
-  uint64_t bytes = 0;     // device bytes while resident
+  uint64_t bytes = 0;     // device bytes while resident (scene copies + structure)
   uint64_t last_use = 0;  // batch counter of the last use
+  int in_flight = 0;      // steps in flight that read it (never evicted then)
 };
 
 struct Pending {
@@ -111,6 +125,50 @@ struct Pending {
   std::vector<uint8_t> pixels;
 };
 
+// One wavefront slot: a stream, its buffers and the step in flight on it.
+struct Slot {
+  cudaStream_t stream = nullptr;
+  DevBuf rays, shadow, hits, cw, pend, bits, pix, table, counters, err;
+  uint8_t* host = nullptr;  // pinned: pixels, then 16 bytes of shadow count and error word
+  size_t host_cap = 0;
+  bool busy = false;
+  uint64_t seq = 0;
+  std::atomic<bool> landed{false};
+  std::vector<Pending*> batch;
+  std::vector<rq_status_t> status;
+  std::vector<Mesh*> mesh;
+  std::vector<uint32_t> poff;
+  std::vector<size_t> which;
+  uint32_t npix = 0;
+  uint64_t nray = 0;
+  uint64_t device_bytes() const {
+    return rays.cap + shadow.cap + hits.cap + cw.cap + pend.cap + bits.cap + pix.cap + table.cap + counters.cap +
+           err.cap;
+  }
+  void release() {
+    rays.release(); shadow.release(); hits.release(); cw.release(); pend.release(); bits.release();
+    pix.release(); table.release(); counters.release(); err.release();
+    if (host) cudaFreeHost(host);
+    host = nullptr;
+    host_cap = 0;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+};
+
+uint64_t mesh_estimate_bytes(const Mesh& m) {
+  const uint64_t nt = m.idx.size() / 3, nv = m.verts.size() / 3;
+  // scene (vertices, indices and their 16-byte copies) + LBVH (nodes, payload,
+  // order, codes, root)
+  return nv * (12 + 16) + nt * (12 + 16) + (nt > 1 ? nt - 1 : 1) * 64 + nt * (48 + 4 + 4) + 512;
+}
+
+uint64_t scratch_bytes(const BuildScratch& sc) {
+  return sc.keys_alt.cap + sc.vals_alt.cap + sc.zero.cap + sc.parent.cap + sc.mark.cap + sc.lohi.cap +
+         sc.keys.cap + sc.vals.cap + sc.m0.cap + sc.m1.cap + sc.m2.cap + sc.m3.cap + sc.m4.cap + sc.m5.cap +
+         sc.m6.cap + sc.m7.cap + sc.kd_refs.cap + sc.work.cap;
+}
+
 }  // namespace
 }  // namespace rq
 
@@ -118,7 +176,8 @@ using namespace rq;
 
 struct rq_server {
   rq_server_config_t cfg{};
-  rq_ctx_t ctx = nullptr;
+  rq_ctx_t ctx = nullptr;        // rendering (slot streams)
+  rq_ctx_t build_ctx = nullptr;  // uploads and LBVH builds, on its own stream
   std::mutex m;
   std::condition_variable cv_work, cv_done;
   std::deque<Pending*> queue;
@@ -128,68 +187,94 @@ struct rq_server {
   bool stop = false;
   std::thread worker;
   // worker-only state
-  uint64_t batch_no = 0;
+  Slot slots[2];
+  int n_slots = 1;
+  uint64_t batch_no = 0, launch_no = 0;
   uint64_t resident = 0;
-  DevBuf rays, shadow, hits, cw, pend, bits, pix, table, counters;
-  uint8_t* host_pix = nullptr;  // pinned download buffer
-  size_t host_pix_cap = 0;
+  Clock::time_point busy_since;
   // statistics (under m)
   rq_server_stats_t st{};
   std::vector<double> lat_ms;
   std::string worker_error;
 
   void run();
-  void serve(std::vector<Pending*>& batch);
-  rq_status_t make_resident(Mesh& mesh, const std::vector<Mesh*>& keep);
+  Slot* free_slot();
+  Slot* oldest_busy();
+  bool launch(Slot& sl, std::vector<Pending*>& batch);
+  void retire(Slot& sl);
+  uint64_t engine_bytes() const;
+  rq_status_t make_resident(Mesh& mesh, const std::vector<Mesh*>& keep, uint64_t wavefront);
+  bool evict_one(const std::vector<Mesh*>& keep);
   void finish(std::vector<Pending*>& batch, const std::vector<rq_status_t>& status);
 };
 
 namespace {
 
-uint64_t mesh_device_bytes(const Mesh& m) {
-  const uint64_t nt = m.idx.size() / 3, nv = m.verts.size() / 3;
-  // scene (vertices + indices) + LBVH (nodes, payload, order, codes, root)
-  return nv * 12 + nt * 12 + (nt > 1 ? nt - 1 : 1) * 64 + nt * 48 + nt * 8 + 256;
+void CUDART_CB on_landed(void* arg) {
+  // Runs on a CUDA callback thread: no CUDA calls here, only the flag.
+  auto* pr = static_cast<std::pair<rq_server*, Slot*>*>(arg);
+  {
+    std::lock_guard<std::mutex> g(pr->first->m);
+    pr->second->landed.store(true);
+  }
+  pr->first->cv_work.notify_one();
+  delete pr;
 }
 
 }  // namespace
 
-rq_status_t rq_server::make_resident(Mesh& mesh, const std::vector<Mesh*>& keep) {
-  if (mesh.accel) return RQ_SUCCESS;
-  const uint64_t need = mesh_device_bytes(mesh);
-  if (need > cfg.hbm_budget) return RQ_ERROR_OUT_OF_MEMORY;
-  // least recently used first, never a mesh the current batch needs
-  while (resident + need > cfg.hbm_budget) {
-    Mesh* lru = nullptr;
-    {
-      std::lock_guard<std::mutex> g(m);
-      for (auto& kv : meshes) {
-        Mesh* c = kv.second.get();
-        if (!c->accel || std::find(keep.begin(), keep.end(), c) != keep.end()) continue;
-        if (!lru || c->last_use < lru->last_use) lru = c;
-      }
-    }
-    if (!lru) return RQ_ERROR_OUT_OF_MEMORY;
-    rq_accel_destroy(lru->accel);
-    rq_scene_destroy(lru->scene);
-    lru->accel = nullptr;
-    lru->scene = nullptr;
-    resident -= lru->bytes;
-    lru->bytes = 0;
+// Device memory the server holds besides resident meshes: the slots'
+// wavefront buffers and the two contexts' build and render scratch.
+uint64_t rq_server::engine_bytes() const {
+  uint64_t b = 0;
+  for (int k = 0; k < n_slots; ++k) b += slots[k].device_bytes();
+  b += scratch_bytes(ctx->scratch) + scratch_bytes(build_ctx->scratch);
+  b += build_ctx->stage_in.cap + build_ctx->stage_out.cap + build_ctx->stage_aux.cap;
+  return b;
+}
+
+bool rq_server::evict_one(const std::vector<Mesh*>& keep) {
+  Mesh* lru = nullptr;
+  {
     std::lock_guard<std::mutex> g(m);
-    ++st.evictions;
+    for (auto& kv : meshes) {
+      Mesh* c = kv.second.get();
+      if (!c->accel || c->in_flight > 0 || std::find(keep.begin(), keep.end(), c) != keep.end()) continue;
+      if (!lru || c->last_use < lru->last_use) lru = c;
+    }
   }
-  rq_status_t s = rq_scene_create_triangles(ctx, mesh.verts.data(), (uint32_t)(mesh.verts.size() / 3),
+  if (!lru) return false;
+  rq_accel_destroy(lru->accel);
+  rq_scene_destroy(lru->scene);
+  lru->accel = nullptr;
+  lru->scene = nullptr;
+  resident -= lru->bytes;
+  lru->bytes = 0;
+  std::lock_guard<std::mutex> g(m);
+  ++st.evictions;
+  return true;
+}
+
+// Upload + build `mesh` if needed, evicting least recently used meshes (not in
+// `keep`, not in flight) until resident meshes, the engine's buffers and
+// `wavefront` more bytes fit the budget.
+rq_status_t rq_server::make_resident(Mesh& mesh, const std::vector<Mesh*>& keep, uint64_t wavefront) {
+  if (mesh.accel) return RQ_SUCCESS;
+  const uint64_t need = mesh_estimate_bytes(mesh);
+  while (resident + engine_bytes() + wavefront + need > cfg.hbm_budget)
+    if (!evict_one(keep)) return RQ_ERROR_OUT_OF_MEMORY;
+  rq_status_t s = rq_scene_create_triangles(build_ctx, mesh.verts.data(), (uint32_t)(mesh.verts.size() / 3),
                                             mesh.idx.data(), (uint32_t)(mesh.idx.size() / 3), 0, &mesh.scene);
   if (s != RQ_SUCCESS) return s;
-  s = rq_build(ctx, mesh.scene, RQ_LBVH, &mesh.accel);
+  s = rq_build(build_ctx, mesh.scene, RQ_LBVH, &mesh.accel);  // returns once the build has finished
   if (s != RQ_SUCCESS) {
     rq_scene_destroy(mesh.scene);
     mesh.scene = nullptr;
     return s;
   }
-  mesh.bytes = need;
-  resident += need;
+  const rq_scene_t sc = mesh.scene;
+  mesh.bytes = sc->verts.cap + sc->idx.cap + sc->verts4.cap + sc->idx4.cap + mesh.accel->buf.device_bytes();
+  resident += mesh.bytes;
   std::lock_guard<std::mutex> g(m);
   ++st.builds;
   return RQ_SUCCESS;
@@ -214,31 +299,61 @@ void rq_server::finish(std::vector<Pending*>& batch, const std::vector<rq_status
   cv_done.notify_all();
 }
 
-void rq_server::serve(std::vector<Pending*>& batch) {
+Slot* rq_server::free_slot() {
+  for (int k = 0; k < n_slots; ++k)
+    if (!slots[k].busy) return &slots[k];
+  return nullptr;
+}
+
+Slot* rq_server::oldest_busy() {
+  Slot* o = nullptr;
+  for (int k = 0; k < n_slots; ++k)
+    if (slots[k].busy && (!o || slots[k].seq < o->seq)) o = &slots[k];
+  return o;
+}
+
+// Resolve meshes, make them resident, build the step's tables and enqueue the
+// whole wavefront on the slot's stream.  Returns true when a step went in
+// flight; requests that cannot go ahead are finished at once.
+bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
   const size_t n = batch.size();
-  std::vector<rq_status_t> status(n, RQ_SUCCESS);
-  std::vector<Mesh*> mesh(n, nullptr);
+  sl.batch = batch;
+  sl.status.assign(n, RQ_SUCCESS);
+  sl.mesh.assign(n, nullptr);
   ++batch_no;
   {
     std::lock_guard<std::mutex> g(m);
     for (size_t k = 0; k < n; ++k) {
       auto it = meshes.find(batch[k]->req.mesh_id);
-      if (it == meshes.end()) status[k] = RQ_ERROR_INVALID_ARGUMENT;
-      else mesh[k] = it->second.get();
+      if (it == meshes.end()) sl.status[k] = RQ_ERROR_INVALID_ARGUMENT;
+      else sl.mesh[k] = it->second.get();
     }
   }
+  // Wavefront growth this step would add to the slot's buffers.
+  uint64_t rays_all = 0, pix_all = 0;
   for (size_t k = 0; k < n; ++k) {
-    if (status[k] != RQ_SUCCESS) continue;
-    status[k] = make_resident(*mesh[k], mesh);
-    if (status[k] == RQ_SUCCESS) mesh[k]->last_use = batch_no;
+    const rq_request_t& r = batch[k]->req;
+    rays_all += (uint64_t)r.width * r.height * r.spp;
+    pix_all += (uint64_t)r.width * r.height;
+  }
+  const uint64_t want = rays_all * kSampleBytes + pix_all * 3 + 4096;
+  const uint64_t have = sl.device_bytes();
+  const uint64_t grow = want > have ? want - have : 0;
+  for (size_t k = 0; k < n; ++k) {
+    if (sl.status[k] != RQ_SUCCESS) continue;
+    sl.status[k] = make_resident(*sl.mesh[k], sl.mesh, grow);
+    if (sl.status[k] == RQ_SUCCESS) sl.mesh[k]->last_use = batch_no;
+  }
+  while (resident + engine_bytes() + grow > cfg.hbm_budget && evict_one(sl.mesh)) {
   }
   // Tables of the requests that go ahead.
   std::vector<ServeReq> sreq;
   std::vector<Bvh2View> views;
-  std::vector<uint32_t> roff(1, 0), poff(1, 0);
-  std::vector<size_t> which;
+  std::vector<uint32_t> roff(1, 0);
+  sl.poff.assign(1, 0);
+  sl.which.clear();
   for (size_t k = 0; k < n; ++k) {
-    if (status[k] != RQ_SUCCESS) continue;
+    if (sl.status[k] != RQ_SUCCESS) continue;
     const rq_request_t& r = batch[k]->req;
     const float tan_half = (float)std::tan((double)r.view.fov_deg * 3.141592653589793 / 360.0);
     rq_view_t view = r.view;
@@ -246,7 +361,7 @@ void rq_server::serve(std::vector<Pending*>& batch) {
     view.window[0] = view.window[1] = view.window[2] = view.window[3] = 0;
     ServeReq q;
     q.v = make_view_dev(view, r.width, r.height, r.spp, r.background, ctx->settings.bias, tan_half);
-    rq_scene_t sc = mesh[k]->scene;
+    rq_scene_t sc = sl.mesh[k]->scene;
     q.sc.kind = kTriangles;
     q.sc.n = sc->n;
     q.sc.nv = sc->nv;
@@ -256,148 +371,210 @@ void rq_server::serve(std::vector<Pending*>& batch) {
     q.sc.verts4 = sc->verts4.as<const float4>();
     q.sc.idx4 = sc->idx4.as<const uint4>();
     sreq.push_back(q);
-    const AccelBuffers& b = mesh[k]->accel->buf;
+    const AccelBuffers& b = sl.mesh[k]->accel->buf;
     views.push_back({b.nodes.as<const float4>(), b.prims.as<const float4>(), b.order.as<const uint32_t>(),
                      b.root.as<const float>(), b.n_nodes, b.n_slots});
     roff.push_back(roff.back() + r.width * r.height * r.spp);
-    poff.push_back(poff.back() + r.width * r.height);
-    which.push_back(k);
+    sl.poff.push_back(sl.poff.back() + r.width * r.height);
+    sl.which.push_back(k);
   }
-  const uint32_t nq = (uint32_t)which.size();
-  const uint32_t nray = roff.back(), npix = poff.back();
-  cudaStream_t s = ctx->stream;
+  const uint32_t nq = (uint32_t)sl.which.size();
+  if (nq == 0) {
+    finish(sl.batch, sl.status);
+    return false;
+  }
+  const uint32_t nray = roff.back(), npix = sl.poff.back();
+  cudaStream_t s = sl.stream;
   cudaError_t e = cudaSuccess;
-  if (nq > 0) {
-    // device table: [ServeReq n][Bvh2View n][roff n+1][poff n+1][work]
-    const size_t a0 = 0, a1 = (sizeof(ServeReq) * nq + 15) & ~size_t(15);
-    const size_t a2 = a1 + ((sizeof(Bvh2View) * nq + 15) & ~size_t(15));
-    const size_t a3 = a2 + ((4 * ((size_t)nq + 1) + 15) & ~size_t(15));
-    const size_t a4 = a3 + ((4 * ((size_t)nq + 1) + 15) & ~size_t(15));
-    std::vector<char> host(a4 + 16, 0);
-    std::memcpy(host.data() + a0, sreq.data(), sizeof(ServeReq) * nq);
-    std::memcpy(host.data() + a1, views.data(), sizeof(Bvh2View) * nq);
-    std::memcpy(host.data() + a2, roff.data(), 4 * ((size_t)nq + 1));
-    std::memcpy(host.data() + a3, poff.data(), 4 * ((size_t)nq + 1));
-    if (e == cudaSuccess) e = table.ensure(host.size());
-    if (e == cudaSuccess) e = rays.ensure((size_t)nray * 32);
-    if (e == cudaSuccess) e = shadow.ensure((size_t)nray * 32);
-    if (e == cudaSuccess) e = hits.ensure((size_t)nray * 16);
-    if (e == cudaSuccess) e = cw.ensure((size_t)nray * 16);
-    if (e == cudaSuccess) e = pend.ensure((size_t)nray * 16);
-    if (e == cudaSuccess) e = bits.ensure((((size_t)nray + 31) / 32) * 4);
-    if (e == cudaSuccess) e = pix.ensure((size_t)npix * 3);
-    if (e == cudaSuccess) e = counters.ensure(16);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(table.p, host.data(), host.size(), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(counters.p, 0, 16, s);
-    char* tb = table.as<char>();
-    const ServeReq* d_req = reinterpret_cast<const ServeReq*>(tb + a0);
-    const uint32_t* d_roff = reinterpret_cast<const uint32_t*>(tb + a2);
-    const uint32_t* d_poff = reinterpret_cast<const uint32_t*>(tb + a3);
-    const unsigned gr = (nray + kThreads - 1) / kThreads;
-    if (e == cudaSuccess) {
-      count_launch();
-      k_serve_rays<<<gr, kThreads, 0, s>>>(d_req, d_roff, nq, nray, rays.as<float4>(), cw.as<float4>());
-      e = cudaGetLastError();
-    }
-    BatchedTrace t;
-    t.kind = kTriangles;
-    t.width = 2;
-    t.views = reinterpret_cast<const Bvh2View*>(tb + a1);
-    t.roff = d_roff;
-    t.n_views = nq;
-    t.n = nray;
-    t.work = reinterpret_cast<uint32_t*>(tb + a4);
-    t.err = ctx->d_err;
-    if (e == cudaSuccess) {
-      t.any = false;
-      t.rays = rays.as<const float4>();
-      t.hits = hits.as<float4>();
-      e = launch_trace_batched(t, 128, 1, s);
-    }
-    if (e == cudaSuccess) {
-      count_launch();
-      k_serve_shade<<<gr, kThreads, 0, s>>>(d_req, d_roff, nq, nray, rays.as<float4>(), hits.as<const float4>(),
-                                            shadow.as<float4>(), cw.as<float4>(), pend.as<float4>(),
-                                            counters.as<unsigned long long>());
-      e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-      t.any = true;
-      t.rays = shadow.as<const float4>();
-      t.hits = nullptr;
-      t.occ = bits.as<uint32_t>();
-      e = launch_trace_batched(t, 128, 1, s);
-    }
-    if (e == cudaSuccess) {
-      count_launch(2);
-      k_serve_accum<<<gr, kThreads, 0, s>>>(nray, bits.as<const uint32_t>(), pend.as<const float4>(), cw.as<float4>());
-      k_serve_pixels<<<(npix + kThreads - 1) / kThreads, kThreads, 0, s>>>(d_req, d_roff, d_poff, nq, npix,
-                                                                            cw.as<const float4>(), pix.as<uint8_t>());
-      e = cudaGetLastError();
-    }
-    uint64_t shadow_rays = 0;
-    if (e == cudaSuccess && host_pix_cap < (size_t)npix * 3) {
-      if (host_pix) cudaFreeHost(host_pix);
-      host_pix = nullptr;
-      host_pix_cap = 0;
-      e = cudaMallocHost(&host_pix, (size_t)npix * 3);
-      if (e == cudaSuccess) host_pix_cap = (size_t)npix * 3;
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(host_pix, pix.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&shadow_rays, counters.p, 8, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    uint32_t derr = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&derr, ctx->d_err, 4, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && derr) e = cudaMemset(ctx->d_err, 0, 4);
-    if (e != cudaSuccess || derr) {
+  // device table: [ServeReq n][Bvh2View n][roff n+1][poff n+1][work]
+  const size_t a0 = 0, a1 = (sizeof(ServeReq) * nq + 15) & ~size_t(15);
+  const size_t a2 = a1 + ((sizeof(Bvh2View) * nq + 15) & ~size_t(15));
+  const size_t a3 = a2 + ((4 * ((size_t)nq + 1) + 15) & ~size_t(15));
+  const size_t a4 = a3 + ((4 * ((size_t)nq + 1) + 15) & ~size_t(15));
+  const size_t host_need = (((size_t)npix * 3 + 15) & ~size_t(15)) + 16 + a4 + 16;
+  if (sl.host_cap < host_need) {
+    if (sl.host) cudaFreeHost(sl.host);
+    sl.host = nullptr;
+    sl.host_cap = 0;
+    e = cudaMallocHost(&sl.host, host_need);
+    if (e == cudaSuccess) sl.host_cap = host_need;
+  }
+  const size_t pix_bytes = ((size_t)npix * 3 + 15) & ~size_t(15);
+  char* host_tab = reinterpret_cast<char*>(sl.host) + pix_bytes + 16;
+  if (e == cudaSuccess) {
+    std::memset(host_tab, 0, a4 + 16);
+    std::memcpy(host_tab + a0, sreq.data(), sizeof(ServeReq) * nq);
+    std::memcpy(host_tab + a1, views.data(), sizeof(Bvh2View) * nq);
+    std::memcpy(host_tab + a2, roff.data(), 4 * ((size_t)nq + 1));
+    std::memcpy(host_tab + a3, sl.poff.data(), 4 * ((size_t)nq + 1));
+  }
+  if (e == cudaSuccess) e = sl.table.ensure(a4 + 16);
+  if (e == cudaSuccess) e = sl.rays.ensure((size_t)nray * 32);
+  if (e == cudaSuccess) e = sl.shadow.ensure((size_t)nray * 32);
+  if (e == cudaSuccess) e = sl.hits.ensure((size_t)nray * 16);
+  if (e == cudaSuccess) e = sl.cw.ensure((size_t)nray * 16);
+  if (e == cudaSuccess) e = sl.pend.ensure((size_t)nray * 16);
+  if (e == cudaSuccess) e = sl.bits.ensure((((size_t)nray + 31) / 32) * 4);
+  if (e == cudaSuccess) e = sl.pix.ensure((size_t)npix * 3);
+  if (e == cudaSuccess) e = sl.counters.ensure(16);
+  if (e == cudaSuccess) e = sl.err.ensure(16);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sl.table.p, host_tab, a4 + 16, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(sl.counters.p, 0, 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(sl.err.p, 0, 16, s);
+  char* tb = sl.table.as<char>();
+  const ServeReq* d_req = reinterpret_cast<const ServeReq*>(tb + a0);
+  const uint32_t* d_roff = reinterpret_cast<const uint32_t*>(tb + a2);
+  const uint32_t* d_poff = reinterpret_cast<const uint32_t*>(tb + a3);
+  const unsigned gr = (nray + kThreads - 1) / kThreads;
+  if (e == cudaSuccess) {
+    count_launch();
+    k_serve_rays<<<gr, kThreads, 0, s>>>(d_req, d_roff, nq, nray, sl.rays.as<float4>(), sl.cw.as<float4>());
+    e = cudaGetLastError();
+  }
+  BatchedTrace t;
+  t.kind = kTriangles;
+  t.width = 2;
+  t.views = reinterpret_cast<const Bvh2View*>(tb + a1);
+  t.roff = d_roff;
+  t.n_views = nq;
+  t.n = nray;
+  t.work = reinterpret_cast<uint32_t*>(tb + a4);
+  t.err = sl.err.as<uint32_t>();
+  if (e == cudaSuccess) {
+    t.any = false;
+    t.rays = sl.rays.as<const float4>();
+    t.hits = sl.hits.as<float4>();
+    e = launch_trace_batched(t, 128, 1, s);
+  }
+  if (e == cudaSuccess) {
+    count_launch();
+    k_serve_shade<<<gr, kThreads, 0, s>>>(d_req, d_roff, nq, nray, sl.rays.as<float4>(), sl.hits.as<const float4>(),
+                                          sl.shadow.as<float4>(), sl.cw.as<float4>(), sl.pend.as<float4>(),
+                                          sl.counters.as<unsigned long long>());
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    t.any = true;
+    t.rays = sl.shadow.as<const float4>();
+    t.hits = nullptr;
+    t.occ = sl.bits.as<uint32_t>();
+    e = launch_trace_batched(t, 128, 1, s);
+  }
+  if (e == cudaSuccess) {
+    count_launch(2);
+    k_serve_accum<<<gr, kThreads, 0, s>>>(nray, sl.bits.as<const uint32_t>(), sl.pend.as<const float4>(),
+                                          sl.cw.as<float4>());
+    k_serve_pixels<<<(npix + kThreads - 1) / kThreads, kThreads, 0, s>>>(d_req, d_roff, d_poff, nq, npix,
+                                                                          sl.cw.as<const float4>(), sl.pix.as<uint8_t>());
+    e = cudaGetLastError();
+  }
+  uint8_t* tail = sl.host + pix_bytes;  // shadow-ray count (8 bytes) and error word (4 bytes)
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sl.host, sl.pix.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tail, sl.counters.p, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tail + 8, sl.err.p, 4, cudaMemcpyDeviceToHost, s);
+  sl.landed.store(false);
+  if (e == cudaSuccess) e = cudaLaunchHostFunc(s, on_landed, new std::pair<rq_server*, Slot*>(this, &sl));
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(s);
+    {
       std::lock_guard<std::mutex> g(m);
-      worker_error = e != cudaSuccess ? cudaGetErrorString(e) : "device error flag set during a batch";
-      cudaGetLastError();
+      worker_error = cudaGetErrorString(e);
     }
-    for (uint32_t j = 0; j < nq; ++j) {
-      const size_t k = which[j];
-      if (e != cudaSuccess || derr) {
-        status[k] = e != cudaSuccess ? RQ_ERROR_CUDA : RQ_ERROR_INVALID_ARGUMENT;
-        continue;
-      }
-      if (batch[k]->req.keep_pixels)
-        batch[k]->pixels.assign(host_pix + 3 * (size_t)poff[j], host_pix + 3 * (size_t)poff[j + 1]);
+    cudaGetLastError();
+    for (size_t j = 0; j < sl.which.size(); ++j) sl.status[sl.which[j]] = RQ_ERROR_CUDA;
+    finish(sl.batch, sl.status);
+    return false;
+  }
+  for (size_t j = 0; j < sl.which.size(); ++j) ++sl.mesh[sl.which[j]]->in_flight;
+  sl.npix = npix;
+  sl.nray = nray;
+  sl.busy = true;
+  sl.seq = ++launch_no;
+  return true;
+}
+
+// A landed step: hand out pixels and statuses, release its meshes.
+void rq_server::retire(Slot& sl) {
+  const size_t pix_bytes = ((size_t)sl.npix * 3 + 15) & ~size_t(15);
+  uint64_t shadow_rays = 0;
+  uint32_t derr = 0;
+  std::memcpy(&shadow_rays, sl.host + pix_bytes, 8);
+  std::memcpy(&derr, sl.host + pix_bytes + 8, 4);
+  if (derr) {
+    std::lock_guard<std::mutex> g(m);
+    worker_error = "device error flag set during a batch";
+  }
+  for (size_t j = 0; j < sl.which.size(); ++j) {
+    const size_t k = sl.which[j];
+    --sl.mesh[k]->in_flight;
+    if (derr) {
+      sl.status[k] = (derr & kErrStackOverflow) ? RQ_ERROR_STACK_OVERFLOW : RQ_ERROR_INVALID_ARGUMENT;
+      continue;
     }
+    if (sl.batch[k]->req.keep_pixels)
+      sl.batch[k]->pixels.assign(sl.host + 3 * (size_t)sl.poff[j], sl.host + 3 * (size_t)sl.poff[j + 1]);
+  }
+  sl.busy = false;
+  {
     std::lock_guard<std::mutex> g(m);
     ++st.batches;
-    st.camera_rays += nray;
+    st.camera_rays += sl.nray;
     st.shadow_rays += shadow_rays;
     st.resident_bytes = resident;
   }
-  finish(batch, status);
+  finish(sl.batch, sl.status);
 }
 
 void rq_server::run() {
   if (cudaSetDevice(cfg.device) != cudaSuccess) return;
   for (;;) {
-    std::vector<Pending*> batch;
-    {
-      std::unique_lock<std::mutex> lk(m);
-      cv_work.wait(lk, [&] { return stop || !queue.empty(); });
-      if (stop) return;
-      // continuous batching: everything waiting, in arrival order, up to the limits
-      uint64_t rays_in = 0;
-      while (!queue.empty()) {
-        Pending* p = queue.front();
-        const uint64_t r = (uint64_t)p->req.width * p->req.height * p->req.spp;
-        if (!batch.empty() && (!cfg.batching || batch.size() >= cfg.max_batch_requests ||
-                               rays_in + r > cfg.max_batch_rays))
-          break;
-        batch.push_back(p);
-        rays_in += r;
-        queue.pop_front();
+    // Retire every step that has landed, oldest first.
+    for (;;) {
+      Slot* o = oldest_busy();
+      if (!o || !o->landed.load()) break;
+      retire(*o);
+      if (!oldest_busy()) {
+        std::lock_guard<std::mutex> g(m);
+        st.busy_s += std::chrono::duration<double>(Clock::now() - busy_since).count();
       }
     }
+    std::vector<Pending*> batch;
+    Slot* sl = free_slot();
+    {
+      std::unique_lock<std::mutex> lk(m);
+      if (stop && !oldest_busy()) return;
+      if (sl && !queue.empty() && !stop) {
+        // everything waiting, in arrival order, up to the limits
+        uint64_t rays_in = 0;
+        while (!queue.empty()) {
+          Pending* p = queue.front();
+          const uint64_t r = (uint64_t)p->req.width * p->req.height * p->req.spp;
+          if (!batch.empty() && (!cfg.batching || batch.size() >= cfg.max_batch_requests ||
+                                 rays_in + r > cfg.max_batch_rays))
+            break;
+          batch.push_back(p);
+          rays_in += r;
+          queue.pop_front();
+        }
+      }
+      if (batch.empty()) {
+        // wait for an arrival (when a slot is free) or for a step to land
+        // (slot states change only on this thread; `landed` is set under m)
+        cv_work.wait(lk, [&] {
+          Slot* o = oldest_busy();
+          if (o && o->landed.load()) return true;
+          if (stop) return o == nullptr;
+          return free_slot() != nullptr && !queue.empty();
+        });
+        continue;
+      }
+    }
+    const bool was_idle = oldest_busy() == nullptr;
     const Clock::time_point t0 = Clock::now();
-    serve(batch);
-    const double dt = std::chrono::duration<double>(Clock::now() - t0).count();
-    std::lock_guard<std::mutex> g(m);
-    st.busy_s += dt;
+    if (launch(*sl, batch) && was_idle) busy_since = t0;
+    if (!cfg.batching) {  // the plain path: each step waited for before the next
+      cudaStreamSynchronize(sl->stream);
+    }
   }
 }
 
@@ -421,6 +598,21 @@ rq_status_t rq_server_create(const rq_server_config_t* cfg, rq_server_t* out) {
   settings.morton = RQ_MORTON_SCENE_CUBE;
   rq_status_t st = rq_create(&settings, s->cfg.device, &s->ctx);
   if (st != RQ_SUCCESS) return st;
+  st = rq_create(&settings, s->cfg.device, &s->build_ctx);
+  if (st != RQ_SUCCESS) {
+    rq_destroy(s->ctx);
+    return st;
+  }
+  s->n_slots = s->cfg.batching ? 2 : 1;
+  for (int k = 0; k < s->n_slots; ++k) {
+    if (cudaStreamCreateWithFlags(&s->slots[k].stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      for (int j = 0; j < k; ++j) s->slots[j].release();
+      rq_destroy(s->build_ctx);
+      rq_destroy(s->ctx);
+      return RQ_ERROR_CUDA;
+    }
+  }
   rq_server* raw = s.get();
   s->worker = std::thread([raw] { raw->run(); });
   *out = s.release();
@@ -551,9 +743,11 @@ rq_status_t rq_server_destroy(rq_server_t s) {
     if (kv.second->accel) rq_accel_destroy(kv.second->accel);
     if (kv.second->scene) rq_scene_destroy(kv.second->scene);
   }
-  s->rays.release(); s->shadow.release(); s->hits.release(); s->cw.release(); s->pend.release();
-  s->bits.release(); s->pix.release(); s->table.release(); s->counters.release();
-  if (s->host_pix) cudaFreeHost(s->host_pix);
+  for (int k = 0; k < s->n_slots; ++k) {
+    if (s->slots[k].stream) cudaStreamSynchronize(s->slots[k].stream);
+    s->slots[k].release();
+  }
+  rq_destroy(s->build_ctx);
   rq_destroy(s->ctx);
   delete s;
   return RQ_SUCCESS;

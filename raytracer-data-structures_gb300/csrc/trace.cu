@@ -83,6 +83,44 @@ __global__ void __launch_bounds__(kThreads) k_trace_bvh4(Bvh4View bvh, const flo
   if (COUNT) add_counts(counters, visits, tests);
 }
 
+template <int KIND, bool ANY, bool COUNT = false>
+__global__ void __launch_bounds__(kThreads) k_trace_bvh8(Bvh8View bvh, const float4* __restrict__ rays,
+                                                         uint32_t n, float4* __restrict__ hits,
+                                                         uint32_t* __restrict__ occ, uint32_t* err,
+                                                         const uint32_t* __restrict__ perm,
+                                                         unsigned long long* counters) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t r = (perm && i < n) ? __ldg(perm + i) : i;
+  bool occluded = false;
+  uint32_t visits = 0, tests = 0;
+  if (i < n) {
+    Ray ray = load_ray(rays, r);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    occluded = walk_bvh8<KIND, ANY, COUNT, kStack8>(bvh, ray, c, visits, tests, err);
+    if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  }
+  if (ANY) {
+    if (perm) {
+      if (occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+    } else {
+      uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+      uint32_t w0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+      if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+    }
+  }
+  if (COUNT) add_counts(counters, visits, tests);
+}
+
+template <int KIND, bool ANY>
+void dispatch_bvh8(const Bvh8View& v, const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
+                   uint32_t* err, const uint32_t* perm, unsigned long long* counters, cudaStream_t s) {
+  uint32_t g = (n + kThreads - 1) / kThreads;
+  if (counters)
+    k_trace_bvh8<KIND, ANY, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm, counters);
+  else
+    k_trace_bvh8<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, perm, nullptr);
+}
+
 template <int KIND, bool ANY>
 void dispatch_bvh4(const Bvh4View& v, const float4* rays, uint32_t n, float4* hits, uint32_t* occ,
                    uint32_t* err, const uint32_t* perm, unsigned long long* counters, cudaStream_t s) {
@@ -670,6 +708,21 @@ void launch_trace_bvh4(int kind, bool any, const Bvh4View& v, const float4* rays
   } else {
     if (any) dispatch_bvh4<kSpheres, true>(v, rays, n, hits, occ, err, perm, counters, s);
     else dispatch_bvh4<kSpheres, false>(v, rays, n, hits, occ, err, perm, counters, s);
+  }
+}
+
+void launch_trace_bvh8(int kind, bool any, const Bvh8View& v, const float4* rays, uint32_t n, float4* hits,
+                       uint32_t* occ, uint32_t* err, cudaStream_t s, const uint32_t* perm,
+                       unsigned long long* counters) {
+  if (n == 0) return;
+  count_launch();
+  if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
+  if (kind == kTriangles) {
+    if (any) dispatch_bvh8<kTriangles, true>(v, rays, n, hits, occ, err, perm, counters, s);
+    else dispatch_bvh8<kTriangles, false>(v, rays, n, hits, occ, err, perm, counters, s);
+  } else {
+    if (any) dispatch_bvh8<kSpheres, true>(v, rays, n, hits, occ, err, perm, counters, s);
+    else dispatch_bvh8<kSpheres, false>(v, rays, n, hits, occ, err, perm, counters, s);
   }
 }
 

@@ -44,6 +44,9 @@ __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restr
         if (W == 4) {
           const Bvh4View v4{v.nodes, v.prims, v.order, v.root, v.n_internal, v.n_slots};
           occluded = walk_bvh4<KIND, ANY, false, STACK>(v4, ray, c, visits, tests, err);
+        } else if (W == 8) {
+          const Bvh8View v8{v.nodes, v.prims, v.order, v.root, v.n_internal, v.n_slots};
+          occluded = walk_bvh8<KIND, ANY, false, STACK>(v8, ray, c, visits, tests, err);
         } else {
           occluded = walk_bvh2<KIND, ANY, false, STACK>(v, ray, c, visits, tests, err);
         }
@@ -119,7 +122,7 @@ __global__ void __launch_bounds__(256) k_batch_ray_keys(const Bvh2View* __restri
 
 template <int KIND, bool ANY, int W>
 cudaError_t dispatch_shape(const BatchedTrace& t, int block, int deep, cudaStream_t s) {
-  constexpr int kShallow = W == 4 ? 48 : 32, kDeep = W == 4 ? 96 : 64;
+  constexpr int kShallow = W == 4 ? 48 : W == 8 ? 16 : 32, kDeep = W == 4 ? 96 : W == 8 ? 32 : 64;
   if (block == 256) {
     return deep ? launch_shape<KIND, ANY, W, kDeep, 256>(t, s) : launch_shape<KIND, ANY, W, kShallow, 256>(t, s);
   }
@@ -128,12 +131,15 @@ cudaError_t dispatch_shape(const BatchedTrace& t, int block, int deep, cudaStrea
 
 template <int KIND, bool ANY>
 cudaError_t dispatch_width(const BatchedTrace& t, int block, int deep, cudaStream_t s) {
+  if (t.width == 8) return dispatch_shape<KIND, ANY, 8>(t, block, deep, s);
   return t.width == 4 ? dispatch_shape<KIND, ANY, 4>(t, block, deep, s) : dispatch_shape<KIND, ANY, 2>(t, block, deep, s);
 }
 
 }  // namespace
 
-int batched_stack_entries(int width, int deep) { return width == 4 ? (deep ? 96 : 48) : (deep ? 64 : 32); }
+int batched_stack_entries(int width, int deep) {
+  return width == 4 ? (deep ? 96 : 48) : width == 8 ? (deep ? 32 : 16) : (deep ? 64 : 32);
+}
 
 int batch_key_bits(uint32_t n_views) {
   int b = 0;

@@ -263,4 +263,101 @@ __device__ __forceinline__ bool walk_bvh4(const Bvh4View& bvh, const Ray& ray, C
                          : walk_bvh4_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
 }
 
+// ---------------------------------------------------------------- 8-wide
+// FAST traversal of the compressed 8-wide BVH (layout in bvh8.cu).  A node
+// visit decodes and tests its (up to) eight child boxes and keeps the hit
+// ones as a bit mask in the ray's visiting order (bit k = slot k ^ oct); the
+// walk takes children from the mask lowest bit first, and when it descends
+// it pushes the node with its remaining mask (one stack entry per level, at
+// most 22 for a tree 64 binary levels deep).
+constexpr int kStack8 = 32;
+
+// One child plane: fma(S, F(q), pm), F(q) = 1 + q * 2^-15 built by one byte
+// permute from byte k of `word` (the builder decodes with these operations).
+__device__ __forceinline__ float q8(uint32_t word, int k, float S, float pm) {
+  return __fmaf_rn(S, __uint_as_float(__byte_perm(word, 0x3F800000u, 0x7604u | (k << 4))), pm);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ uint32_t node8_hits(const float4* nd, const SlabRay& sr, F3 o, float tmin, float tfar,
+                                               uint32_t oct) {
+  uint32_t r[16];
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "l"(nd));
+  asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "l"(nd + 2));
+  const float pmx = __uint_as_float(r[0]), pmy = __uint_as_float(r[1]), pmz = __uint_as_float(r[2]);
+  const uint32_t hb = r[3];
+  const float Sx = __uint_as_float((hb & 0xFFu) << 23), Sy = __uint_as_float((hb & 0xFF00u) << 15),
+              Sz = __uint_as_float((hb & 0xFF0000u) << 7);
+  const uint32_t valid = hb >> 24;
+  uint32_t mask = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int k = i & 3, h = i >> 2;
+    const float lx = q8(r[4 + h], k, Sx, pmx), hx = q8(r[6 + h], k, Sx, pmx);
+    const float ly = q8(r[8 + h], k, Sy, pmy), hy = q8(r[10 + h], k, Sy, pmy);
+    const float lz = q8(r[12 + h], k, Sz, pmz), hz = q8(r[14 + h], k, Sz, pmz);
+    float tn;
+    const bool hit = slab_box<EXACT>(sr, o, lx, hx, ly, hy, lz, hz, tmin, tfar, tn);
+    mask |= (hit && (valid >> i & 1u)) ? 1u << (i ^ oct) : 0u;
+  }
+  return mask;
+}
+
+template <int KIND, bool ANY, bool COUNT, int STACK, bool EXACT>
+__device__ __forceinline__ bool walk_bvh8_form(const Bvh8View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                               uint32_t& tests, uint32_t* err) {
+  const SlabRay sr = slab_ray(ray.o, ray.d);
+  float tn;
+  const float* rb = bvh.root;
+  if (!slab_box<EXACT>(sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
+  if (bvh.n_binary == 0) {  // the root is one leaf
+    if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, 0u, (int)bvh.n_slots, ray);
+    return test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, 0u, (int)bvh.n_slots, ray, c);
+  }
+  const uint32_t oct = (ray.d.x < 0.f ? 1u : 0u) | (ray.d.y < 0.f ? 2u : 0u) | (ray.d.z < 0.f ? 4u : 0u);
+  uint2 stack[STACK];
+  int sp = 0;
+  uint32_t node = 0;
+  if (COUNT) ++visits;
+  uint32_t mask = node8_hits<EXACT>(bvh.nodes, sr, ray.o, ray.tmin, ANY ? ray.tmax : c.t, oct);
+  // A valid walk takes every child (node or leaf) at most once.
+  const uint32_t max_steps = 2u * (bvh.n_binary + bvh.n_slots) + 8u;
+  uint32_t steps = 0;
+  for (;;) {
+    if (mask == 0u) {
+      if (sp == 0) return false;
+      const uint2 e = stack[--sp];
+      node = e.x;
+      mask = e.y;
+    }
+    if (++steps > max_steps) { atomicOr(err, kErrCorrupt); return false; }
+    const uint32_t k = (uint32_t)__ffs(mask) - 1u;
+    mask &= mask - 1u;
+    const int2 lc = __ldg(reinterpret_cast<const int2*>(bvh.nodes + 8 * (size_t)node + 4) + (k ^ oct));
+    if (lc.y == 0) {
+      if (mask) {
+        if (sp >= STACK) { atomicOr(err, kErrStackOverflow); return false; }
+        stack[sp++] = make_uint2(node, mask);
+      }
+      node = (uint32_t)lc.x;
+      if (COUNT) ++visits;
+      mask = node8_hits<EXACT>(bvh.nodes + 8 * (size_t)node, sr, ray.o, ray.tmin, ANY ? ray.tmax : c.t, oct);
+    } else {
+      if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, (uint32_t)lc.x, lc.y, ray);
+      if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)lc.x, lc.y, ray, c)) return true;
+    }
+  }
+}
+
+template <int KIND, bool ANY, bool COUNT, int STACK>
+__device__ __forceinline__ bool walk_bvh8(const Bvh8View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* err) {
+  return zero_dir(slab_ray(ray.o, ray.d)) ? walk_bvh8_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, c, visits, tests, err)
+                                          : walk_bvh8_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
+}
+
 }  // namespace rq

@@ -166,6 +166,8 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
                       a.root.as<const float>(), a.n_nodes, a.n_slots};
     const Bvh4View b4{a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
                       a.root.as<const float>(), a.n_nodes, a.n_slots};
+    const Bvh8View b8{a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
+                      a.root.as<const float>(), a.n_nodes, a.n_slots};
     for (uint32_t depth = 0; depth <= v.bounces && n_live > 0; ++depth) {
       const bool last = depth == v.bounces;
       if (depth == 0) {
@@ -180,6 +182,8 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
         }
       } else if (a.node_width == 4) {
         launch_trace_bvh4(s.kind, false, b4, rays, n_live, hits, nullptr, err, st, live);
+      } else if (a.node_width == 8) {
+        launch_trace_bvh8(s.kind, false, b8, rays, n_live, hits, nullptr, err, st, live);
       } else {
         launch_trace_bvh2(s.kind, RQ_TRAVERSAL_FAST, false, bv, rays, n_live, hits, nullptr, err, st, live);
       }
@@ -202,6 +206,8 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
         if ((e = cudaMemsetAsync(bits, 0, ((nray + 31) / 32) * 4, st)) != cudaSuccess) return e;
         if (a.node_width == 4)
           launch_trace_bvh4(s.kind, true, b4, shadow, n_shadow, nullptr, bits, err, st, slist);
+        else if (a.node_width == 8)
+          launch_trace_bvh8(s.kind, true, b8, shadow, n_shadow, nullptr, bits, err, st, slist);
         else
           launch_trace_bvh2(s.kind, RQ_TRAVERSAL_FAST, true, bv, shadow, n_shadow, nullptr, bits, err, st, slist);
         count_launch();

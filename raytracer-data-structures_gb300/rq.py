@@ -20,7 +20,7 @@ TRAVERSAL_FAST, TRAVERSAL_REFERENCE = 0, 1
 RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON, RAY_SORT_ORIGIN_DIRECTION, RAY_SORT_DIRECTION_ORIGIN, RAY_SORT_OCTANT_MORTON12 = \
     0, 1, 2, 3, 4
 RAY_SORT_OCTANT, RAY_SORT_OCTANT_MORTON3 = 5, 6
-NODE_WIDTH_2, NODE_WIDTH_4 = 0, 4
+NODE_WIDTH_2, NODE_WIDTH_4, NODE_WIDTH_8 = 0, 4, 8
 SCHEDULING_THREAD_PER_RAY, SCHEDULING_LANE_REFILL, SCHEDULING_SPECULATIVE, SCHEDULING_WARP_PACKET = 0, 1, 2, 3
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE, MORTON_SCENE_CUBE = 0, 1, 2
 # SceneModel (settings.h:4)

@@ -56,7 +56,7 @@ def test_axis_aligned_rays_on_box_planes_equal_brute_force(engine, rqm, oracle, 
     brute = engine.build(s, rqm.NONE)
     want = engine.trace_closest(brute, rays)
     want_any = engine.trace_any(brute, rays)
-    assert (want["prim"] != rqm.MISS).mean() > 0.95  # the downward rays all land on the terrain
+    assert (want["prim"][:len(v)] != rqm.MISS).all()  # the downward rays all land on the terrain
     engine.configure(node_width=width)
     acc = engine.build(s, acc_name)
     got = engine.trace_closest(acc, rays)

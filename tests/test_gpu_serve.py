@@ -74,22 +74,62 @@ def test_served_pixels_equal_alone_and_rq_render(engine, rqm):
 
 
 def test_lru_residency_under_a_small_budget(engine, rqm):
-    lib = _library(seed=200, count=4)
-    reqs = _requests(rqm, lib, 16, seed=9)
+    """Four meshes of about 50k triangles (some 8 MB each on the device with
+    their LBVHs) under a 24 MB budget, which also holds the wavefront buffers
+    and build scratch: the requests cycle through the library, so meshes are
+    evicted and rebuilt, and every image stays the same."""
+    lib = {20 + k: scenes.wave_heightfield(160, 160 + k, seed=400 + k) for k in range(4)}
+    rng = np.random.default_rng(11)
+    reqs = []
+    for k in range(16):
+        az = rng.uniform(0, 6.28)
+        view = rqm.make_view(eye=(float(2.2 * np.cos(az)), float(2.2 * np.sin(az)), 1.0), target=(0, 0, 0),
+                             up=(0, 0, 1), fov_deg=45.0, light=(1.0, -2.0, 3.0), albedo=(0.7, 0.65, 0.6),
+                             ambient=0.1, seed=int(50 + k))
+        reqs.append((20 + k % 4, view, 48, 32, 1))
     accs = {mid: engine.build(engine.scene_triangles(v, f), "LBVH") for mid, (v, f) in lib.items()}
     want = [_render_alone(engine, rqm, lib, accs, r) for r in reqs]
-    biggest = max(len(f) for _, f in lib.values())
-    budget = int(1.2 * biggest * 140)  # the largest mesh fits, the whole library does not
-    srv = rqm.Server(batching=False, hbm_budget=budget)
-    for mid, (v, f) in lib.items():
-        srv.add_mesh(mid, v, f)
-    for req, ref in zip(reqs, want):
-        status, pix = srv.wait(srv.submit(req[0], req[1], req[2], req[3], req[4]))
-        assert status == 0 and np.array_equal(pix, ref)
-    st = srv.stats()
+    budget = 24 << 20
+    for batching in (False, True):
+        srv = rqm.Server(batching=batching, hbm_budget=budget)
+        for mid, (v, f) in lib.items():
+            srv.add_mesh(mid, v, f)
+        for req, ref in zip(reqs, want):
+            status, pix = srv.wait(srv.submit(req[0], req[1], req[2], req[3], req[4]))
+            assert status == 0 and np.array_equal(pix, ref)
+        st = srv.stats()
+        srv.close()
+        assert st.evictions > 0 and st.builds > len(lib)
+        assert st.resident_bytes <= budget and st.resident_meshes < len(lib)
+
+
+def test_arrivals_are_served_while_a_long_step_runs(engine, rqm):
+    """Continuous batching: a small request that arrives while a large one is
+    on the GPU goes into the other wavefront slot and lands first; its pixels
+    are still exactly rq_render's."""
+    import time
+    v, f = scenes.heightfield(501, 500, seed=21)  # 499,000 triangles
+    small_v, small_f = scenes.wave_heightfield(60, 60, seed=22)
+    view = rqm.make_view(eye=(0.0, -2.2, 1.2), target=(0, 0, 0), up=(0, 0, 1), fov_deg=45.0,
+                         light=(1.0, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=5)
+    acc = engine.build(engine.scene_triangles(small_v, small_f), "LBVH")
+    engine.configure(width=64, height=48, aa_samples=1, backgroundColor=(1.0, 1.0, 1.0))
+    want_small, _, _ = engine.render(acc, view)
+    srv = rqm.Server(batching=True)
+    srv.add_mesh(1, v, f)
+    srv.add_mesh(2, small_v, small_f)
+    for mid in (1, 2):  # both resident before timing
+        srv.wait(srv.submit(mid, view, 32, 32, 1, keep_pixels=False), want_pixels=False)
+    big = srv.submit(1, view, 1920, 1080, 16, keep_pixels=False)  # 33M camera rays
+    time.sleep(0.001)
+    small = srv.submit(2, view, 64, 48, 1)
+    status, pix = srv.wait(small)
+    t_small = time.perf_counter()
+    assert srv.wait(big, want_pixels=False)[0] == 0
+    t_big = time.perf_counter()
     srv.close()
-    assert st.evictions > 0 and st.builds > len(lib)
-    assert st.resident_bytes <= budget and st.resident_meshes < len(lib)
+    assert status == 0 and np.array_equal(pix, want_small)
+    assert t_big - t_small > 0.001  # the large step was still running when the small one landed
 
 
 def test_admission_errors(rqm):
