@@ -241,7 +241,8 @@ def run_ours(args):
                   rq.RAY_SORT_OCTANT_MORTON12: "octant_morton12", rq.RAY_SORT_OCTANT: "octant",
                   rq.RAY_SORT_OCTANT_MORTON3: "octant_morton3"}
     sched_names = {rq.SCHEDULING_THREAD_PER_RAY: "thread_per_ray", rq.SCHEDULING_LANE_REFILL: "lane_refill",
-                   rq.SCHEDULING_SPECULATIVE: "speculative", rq.SCHEDULING_WARP_PACKET: "warp_packet"}
+                   rq.SCHEDULING_SPECULATIVE: "speculative", rq.SCHEDULING_WARP_PACKET: "warp_packet",
+                   rq.SCHEDULING_SHARED_TOP: "shared_top"}
     morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
     tuning = {}
     best = None

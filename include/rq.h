@@ -89,7 +89,8 @@ typedef enum rq_scheduling_t {
   RQ_SCHEDULING_THREAD_PER_RAY = 0, /* one thread per ray */
   RQ_SCHEDULING_LANE_REFILL = 1,    /* persistent warps refill finished lanes with new rays */
   RQ_SCHEDULING_SPECULATIVE = 2,    /* while-while walk that postpones leaves until the warp has one each */
-  RQ_SCHEDULING_WARP_PACKET = 3     /* the warp walks one shared stack (lane masks per entry): coherent rays */
+  RQ_SCHEDULING_WARP_PACKET = 3,    /* the warp walks one shared stack (lane masks per entry): coherent rays */
+  RQ_SCHEDULING_SHARED_TOP = 4      /* one thread per ray; the top 6 tree levels staged in shared memory per block */
 } rq_scheduling_t;
 
 /* Node fan-out of BVH structures (RQ_BVH, RQ_LBVH), fixed when the structure

@@ -212,7 +212,8 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   const bool refill = fast && cfg.scheduling == RQ_SCHEDULING_LANE_REFILL && !wide;
   const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && !wide;
   const bool packet = fast && cfg.scheduling == RQ_SCHEDULING_WARP_PACKET && !wide;
-  if (!sorted && !refill && !spec && !packet) {
+  const bool top = fast && cfg.scheduling == RQ_SCHEDULING_SHARED_TOP && !wide && !q.small_stack;
+  if (!sorted && !refill && !spec && !packet && !top) {
     launch_query(type, s, a, cfg.traversal, any, q, err, st);
     RQ_B(cudaGetLastError(), "trace launch");
     return {};
@@ -235,6 +236,12 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   }
   Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
              a.root.as<const float>(), a.n_nodes, a.n_slots};
+  if (top) {
+    RQ_B(sc.top.ensure(64 * 64), "top-level copy");
+    launch_trace_bvh2_top(s.kind, any, v, sc.top.as<float4>(), q.rays, q.n, q.hits, q.occ, err, perm, st);
+    RQ_B(cudaGetLastError(), "trace launch");
+    return {};
+  }
   if (packet) {
     launch_trace_bvh2_packet(s.kind, any, v, q.rays, q.n, q.hits, q.occ, err, perm, st);
     RQ_B(cudaGetLastError(), "trace launch");

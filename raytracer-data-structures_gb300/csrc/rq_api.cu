@@ -192,8 +192,8 @@ rq_status_t rq_set_settings(rq_ctx_t ctx, const rq_settings_t* s) {
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.node_width must be 2, 4 or 8");
   if (s->ray_sort < RQ_RAY_SORT_NONE || s->ray_sort > RQ_RAY_SORT_OCTANT_MORTON3)
     return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.ray_sort out of range");
-  if (s->scheduling < RQ_SCHEDULING_THREAD_PER_RAY || s->scheduling > RQ_SCHEDULING_WARP_PACKET)
-    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.scheduling must be THREAD_PER_RAY, LANE_REFILL or SPECULATIVE");
+  if (s->scheduling < RQ_SCHEDULING_THREAD_PER_RAY || s->scheduling > RQ_SCHEDULING_SHARED_TOP)
+    return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "settings.scheduling out of range (rq_scheduling_t)");
   ctx->settings = *s;
   return RQ_SUCCESS;
 }
@@ -929,7 +929,7 @@ rq_status_t rq_trace_queries(rq_ctx_t ctx, rq_accel_t a, const rq_query_t* queri
   for (uint32_t k = 0; k < n_queries; ++k) {
     const rq_query_t& q = queries[k];
     if (q.n && (!q.rays || !q.out)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "null ray or result buffer");
-    if (q.ray_sort > RQ_RAY_SORT_OCTANT_MORTON3 || q.scheduling > RQ_SCHEDULING_WARP_PACKET)
+    if (q.ray_sort > RQ_RAY_SORT_OCTANT_MORTON3 || q.scheduling > RQ_SCHEDULING_SHARED_TOP)
       return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "query ray_sort or scheduling out of range");
   }
   rq_status_t st = trace_queries_enqueue(ctx, a, queries, n_queries);

@@ -55,9 +55,11 @@ struct BuildScratch {
   DevBuf m0, m1, m2, m3, m4, m5, m6, m7;  // median / KD working arrays
   DevBuf kd_refs;             // KD: next level's primitive references
   DevBuf work;                // work counter of lane-refill traversal
+  DevBuf top;                 // top-level node copy of RQ_SCHEDULING_SHARED_TOP queries
   const uint32_t* stall = nullptr;  // sort test hook (SortScratch::stall); null in normal use
   void release() {
     work.release();
+    top.release();
     keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); mark.release(); lohi.release();
     keys.release(); vals.release();
     m0.release(); m1.release(); m2.release(); m3.release(); m4.release(); m5.release(); m6.release(); m7.release();

@@ -166,6 +166,10 @@ cudaError_t launch_trace_bvh2_refill(int kind, bool any, const Bvh2View& v, cons
 // Warp-packet FAST traversal (RQ_SCHEDULING_WARP_PACKET): one stack per warp.
 void launch_trace_bvh2_packet(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
                               uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s);
+// FAST traversal with the top levels of the tree staged in shared memory per
+// block (RQ_SCHEDULING_SHARED_TOP); top: 4 KB of scratch for their copy.
+void launch_trace_bvh2_top(int kind, bool any, const Bvh2View& v, float4* top, const float4* rays, uint32_t n,
+                           float4* hits, uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s);
 void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
                             uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s);
 // Coherence sort keys (mode: rq_ray_sort_t other than NONE, 30 bits); vals = identity.

@@ -22,9 +22,32 @@ namespace {
 
 constexpr int kThreads = 128;
 
+// One ray with the exact box test (rq_device.cuh: rays whose direction has a
+// zero component), result written like k_trace_fast's.  Out of line and
+// called only after a block's other rays are done, so the fused walk's
+// register budget does not carry it.
+template <int KIND, bool ANY, bool COUNT, int STACK>
+__device__ __noinline__ void trace_exact_ray(const Bvh2View& bvh, const float4* __restrict__ rays, uint32_t r,
+                                             float4* __restrict__ hits, uint32_t* __restrict__ occ, uint32_t* err,
+                                             unsigned long long* counters) {
+  const Ray ray = load_ray(rays, r);
+  Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+  uint32_t visits = 0, tests = 0;
+  const bool occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, c, visits, tests, err);
+  if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+  if (ANY && occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+  if (COUNT) {
+    atomicAdd(counters, (unsigned long long)visits);
+    atomicAdd(counters + 1, (unsigned long long)tests);
+  }
+}
+
 // perm (may be null): thread i traces ray perm[i] and writes that ray's result
 // (a reordering for coherence that leaves every result where the caller
 // expects it).  With perm, any-hit bits are set with atomicOr on a zeroed array.
+// Rays that need the exact box test are set aside in shared memory and traced
+// by the block's threads after the others (their any-hit bits are then set
+// with atomicOr over the ballot's word, which the block has already stored).
 // At most 48 registers (10 blocks of 128 per SM): measured 3-4% faster on
 // the closest-hit triangle walk than the unconstrained 52.
 template <int KIND, bool ANY, bool COUNT = false, int STACK = kStackSize>
@@ -33,15 +56,23 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const
                                                          uint32_t* __restrict__ occ, uint32_t* err,
                                                          unsigned long long* counters = nullptr,
                                                          const uint32_t* __restrict__ perm = nullptr) {
+  __shared__ uint32_t s_exact[kThreads];
+  __shared__ uint32_t s_n;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t r = (perm && i < n) ? __ldg(perm + i) : i;
   bool occluded = false;
   uint32_t visits = 0, tests = 0;
   if (i < n) {
     Ray ray = load_ray(rays, r);
-    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
-    occluded = walk_bvh2<KIND, ANY, COUNT, STACK>(bvh, ray, c, visits, tests, err);
-    if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+    if (zero_dir(slab_ray(ray.o, ray.d))) {
+      s_exact[atomicAdd(&s_n, 1u)] = r;
+    } else {
+      Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+      occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
+      if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+    }
   }
   if (ANY) {
     if (perm) {
@@ -53,6 +84,157 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const
     }
   }
   if (COUNT) add_counts(counters, visits, tests);
+  __syncthreads();
+  const uint32_t ne = s_n;
+  for (uint32_t k = threadIdx.x; k < ne; k += blockDim.x)
+    trace_exact_ray<KIND, ANY, COUNT, STACK>(bvh, rays, s_exact[k], hits, occ, err, counters);
+}
+
+// ------------------------------------------------ top levels in shared memory
+// RQ_SCHEDULING_SHARED_TOP: the top kTopLevels levels of the binary tree
+// (at most 63 nodes, 4 KB), copied breadth first into one small array whose
+// internal links inside the copy are renumbered kTopBit | position; every
+// block stages that array in shared memory and walks it from there, then
+// continues in global memory below it.  Same walk, same results.
+constexpr int kTopLevels = 6;
+constexpr int kTopNodes = (1 << kTopLevels) - 1;
+constexpr int kTopBit = 0x40000000;  // node links are below 2^30
+
+// One warp: breadth-first list of the top levels, then the renumbered copies.
+__global__ void __launch_bounds__(32) k_top_copy(const float4* __restrict__ nodes, uint32_t n_internal,
+                                                 float4* __restrict__ top) {
+  __shared__ int32_t q[kTopNodes];
+  const uint32_t lane = threadIdx.x;
+  int lo = 0, hi = n_internal ? 1 : 0;
+  if (lane == 0) q[0] = 0;
+  __syncwarp();
+  for (int level = 0; level + 1 < kTopLevels && lo < hi; ++level) {
+    const int j = lo + (int)lane;  // a level holds at most 32 nodes
+    int4 l = make_int4(-1, -1, 0, 0);
+    if (j < hi) l = __ldg(reinterpret_cast<const int4*>(nodes + 4 * (size_t)q[j] + 3));
+    const uint32_t c = (l.x >= 0 ? 1u : 0u) + (l.y >= 0 ? 1u : 0u);
+    uint32_t incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const int at = hi + (int)(incl - c);
+    if (l.x >= 0) q[at] = l.x;
+    if (l.y >= 0) q[at + (l.x >= 0 ? 1 : 0)] = l.y;
+    __syncwarp();
+    lo = hi;
+    hi += (int)total;
+  }
+  for (int k = (int)lane; k < hi; k += 32) {
+    const float4* nd = nodes + 4 * (size_t)q[k];
+    int4 l = __ldg(reinterpret_cast<const int4*>(nd + 3));
+    for (int m = 0; m < hi; ++m) {  // children that are in the copy
+      if (l.x >= 0 && q[m] == l.x) l.x = kTopBit | m;
+      if (l.y >= 0 && q[m] == l.y) l.y = kTopBit | m;
+    }
+    top[4 * k] = __ldg(nd);
+    top[4 * k + 1] = __ldg(nd + 1);
+    top[4 * k + 2] = __ldg(nd + 2);
+    reinterpret_cast<int4*>(top)[4 * k + 3] = l;
+  }
+}
+
+template <int KIND, bool ANY>
+__device__ __forceinline__ bool walk_bvh2_top(const Bvh2View& bvh, const float4* s_top, const Ray& ray, Closest& c,
+                                              uint32_t* err) {
+  const SlabRay sr = slab_ray(ray.o, ray.d);
+  float tn;
+  const float* rb = bvh.root;
+  if (!slab_box<false>(sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
+  int2 stack[kStackSize];
+  int sp = 0;
+  int cur = bvh.n_internal ? kTopBit : -1;
+  int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
+  const uint32_t max_steps = 2u * (bvh.n_internal + bvh.n_slots) + 8u;
+  uint32_t steps = 0;
+  for (;;) {
+    if (++steps > max_steps) { atomicOr(err, kErrCorrupt); return false; }
+    if (cur >= 0) {
+      float4 a, b, z;
+      int4 l;
+      if (cur & kTopBit) {
+        const float4* nd = s_top + 4 * (cur & (kTopBit - 1));
+        a = nd[0]; b = nd[1]; z = nd[2];
+        l = reinterpret_cast<const int4*>(nd)[3];
+      } else {
+        load_node(bvh.nodes + 4 * (size_t)cur, a, b, z, l);
+      }
+      const float tfar = ANY ? ray.tmax : c.t;
+      float tl, tr;
+      const bool hl = slab_box<false>(sr, ray.o, a.x, a.y, a.z, a.w, z.x, z.y, ray.tmin, tfar, tl);
+      const bool hr = slab_box<false>(sr, ray.o, b.x, b.y, b.z, b.w, z.z, z.w, ray.tmin, tfar, tr);
+      if (hl && hr) {
+        int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
+        if (tr < tl) { int2 t = nearE; nearE = farE; farE = t; }
+        if (sp >= kStackSize) { atomicOr(err, kErrStackOverflow); return false; }
+        stack[sp++] = farE;
+        cur = nearE.x;
+        cnt = nearE.y;
+        continue;
+      }
+      if (hl) { cur = l.x; cnt = l.z; continue; }
+      if (hr) { cur = l.y; cnt = l.w; continue; }
+    } else {
+      if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) return true;
+    }
+    if (sp == 0) return false;
+    const int2 e = stack[--sp];
+    cur = e.x;
+    cnt = e.y;
+  }
+}
+
+template <int KIND, bool ANY>
+__global__ void __launch_bounds__(kThreads, 10) k_trace_top(Bvh2View bvh, const float4* __restrict__ top,
+                                                        const float4* __restrict__ rays, uint32_t n,
+                                                        float4* __restrict__ hits, uint32_t* __restrict__ occ,
+                                                        uint32_t* err, const uint32_t* __restrict__ perm) {
+  __shared__ float4 s_top[4 * kTopNodes];
+  __shared__ uint32_t s_exact[kThreads];
+  __shared__ uint32_t s_n;
+  for (int k = threadIdx.x; k < 4 * kTopNodes; k += kThreads) s_top[k] = __ldg(top + k);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t r = (perm && i < n) ? __ldg(perm + i) : i;
+  bool occluded = false;
+  if (i < n) {
+    const Ray ray = load_ray(rays, r);
+    if (zero_dir(slab_ray(ray.o, ray.d))) {
+      s_exact[atomicAdd(&s_n, 1u)] = r;
+    } else {
+      Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+      occluded = walk_bvh2_top<KIND, ANY>(bvh, s_top, ray, c, err);
+      if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+    }
+  }
+  if (ANY) {
+    if (perm) {
+      if (occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+    } else {
+      const uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+      const uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+      if ((threadIdx.x & 31) == 0 && w0 < n) occ[w0 >> 5] = bits;
+    }
+  }
+  __syncthreads();
+  const uint32_t ne = s_n;
+  for (uint32_t k = threadIdx.x; k < ne; k += blockDim.x) {
+    // inline: an out-of-line call here has crashed ptxas 13.0
+    const uint32_t re = s_exact[k];
+    const Ray ray = load_ray(rays, re);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    uint32_t visits = 0, tests = 0;
+    const bool occ_e = walk_bvh2_form<KIND, ANY, false, kStackSize, true>(bvh, ray, c, visits, tests, err);
+    if (!ANY) hits[re] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+    if (ANY && occ_e) atomicOr(occ + (re >> 5), 1u << (re & 31));
+  }
 }
 
 template <int KIND, bool ANY, bool COUNT = false>
@@ -708,6 +890,22 @@ void launch_trace_bvh4(int kind, bool any, const Bvh4View& v, const float4* rays
   } else {
     if (any) dispatch_bvh4<kSpheres, true>(v, rays, n, hits, occ, err, perm, counters, s);
     else dispatch_bvh4<kSpheres, false>(v, rays, n, hits, occ, err, perm, counters, s);
+  }
+}
+
+void launch_trace_bvh2_top(int kind, bool any, const Bvh2View& v, float4* top, const float4* rays, uint32_t n,
+                           float4* hits, uint32_t* occ, uint32_t* err, const uint32_t* perm, cudaStream_t s) {
+  if (n == 0) return;
+  count_launch(2);
+  k_top_copy<<<1, 32, 0, s>>>(v.nodes, v.n_internal, top);
+  if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
+  const uint32_t g = (n + kThreads - 1) / kThreads;
+  if (kind == kTriangles) {
+    if (any) k_trace_top<kTriangles, true><<<g, kThreads, 0, s>>>(v, top, rays, n, hits, occ, err, perm);
+    else k_trace_top<kTriangles, false><<<g, kThreads, 0, s>>>(v, top, rays, n, hits, occ, err, perm);
+  } else {
+    if (any) k_trace_top<kSpheres, true><<<g, kThreads, 0, s>>>(v, top, rays, n, hits, occ, err, perm);
+    else k_trace_top<kSpheres, false><<<g, kThreads, 0, s>>>(v, top, rays, n, hits, occ, err, perm);
   }
 }
 

@@ -22,6 +22,7 @@ RAY_SORT_NONE, RAY_SORT_OCTANT_MORTON, RAY_SORT_ORIGIN_DIRECTION, RAY_SORT_DIREC
 RAY_SORT_OCTANT, RAY_SORT_OCTANT_MORTON3 = 5, 6
 NODE_WIDTH_2, NODE_WIDTH_4, NODE_WIDTH_8 = 0, 4, 8
 SCHEDULING_THREAD_PER_RAY, SCHEDULING_LANE_REFILL, SCHEDULING_SPECULATIVE, SCHEDULING_WARP_PACKET = 0, 1, 2, 3
+SCHEDULING_SHARED_TOP = 4
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE, MORTON_SCENE_CUBE = 0, 1, 2
 # SceneModel (settings.h:4)
 IGEA, ARMADILLO, BUNNY_MODEL, BUNNIES, TEST, GRASS, BUDDHA, CITY = range(8)

@@ -71,10 +71,11 @@ def test_streamed_host_queries_equal_device_queries(engine, rqm):
 
 @pytest.mark.parametrize("acc_name", ["LBVH", "BVH"])
 @pytest.mark.parametrize("ray_sort", [0, 1])
-@pytest.mark.parametrize("sched", ["LANE_REFILL", "SPECULATIVE", "WARP_PACKET"])
+@pytest.mark.parametrize("sched", ["LANE_REFILL", "SPECULATIVE", "WARP_PACKET", "SHARED_TOP"])
 def test_scheduling_is_result_neutral(engine, oracle, rqm, acc_name, ray_sort, sched):
     """Persistent warps that refill finished lanes, the speculative
-    while-while walk and the warp-packet walk (settings.scheduling) give
+    while-while walk, the warp-packet walk and the walk that stages the top
+    tree levels in shared memory (settings.scheduling) give
     bit-identical hits and occlusion bits, with and without ray reordering,
     for camera and secondary rays, triangles and spheres, equal to the
     oracle's plain walk."""
