@@ -701,7 +701,10 @@ def run_batch_leg(eng, stream, dev, args):
                        "build_mtri_s": round(n_tri / (batched_build_ms * 1e-3) / 1e6, 1),
                        "graph_kernels": int(info.graph_kernels),
                        "shape": {"block": int(info.block_threads), "stack": int(info.stack_entries),
-                                 "ray_order": bool(info.ray_order),
+                                 "ray_order": bool(info.ray_order), "node_width": int(info.node_width),
+                                 "width_ms": {"2": round(float(info.width_ms[0]), 3),
+                                              "4": round(float(info.width_ms[1]), 3),
+                                              "8": round(float(info.width_ms[2]), 3)},
                                  "tuned_ms": [round(float(x), 3) for x in info.shape_ms],
                                  "tuned_ordered_ms": [round(float(x), 3) for x in info.ordered_ms]}},
            "speedup": round(plain_ms / batched_ms, 3), "hits_identical": same,

@@ -389,9 +389,12 @@ rq_status_t rq_trace_batched(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_
 /* A captured step over fixed device buffers, replayed as one CUDA graph:
  * [rq_accel_rebuild_batched of the batch] + the many-structure query of
  * rq_trace_batched.  rq_plan_create autotunes the query's launch shape
- * (block of 128 or 256 threads x shallow or deep traversal stack) by timing
- * each on `rays`, drops shapes whose stack overflows on these trees, then
- * captures the step.  rays and out are device buffers whose contents may
+ * (block of 128 or 256 threads x shallow or deep traversal stack, each
+ * without and with a per-scene ray order) by timing each on `rays`, drops
+ * shapes whose stack overflows on these trees, then captures the step.  A
+ * rebuilding plan (rebuild = 1) also tries every node width (binary,
+ * collapsed 4-wide, compressed 8-wide) and leaves the batch's structures at
+ * the width it picked.  rays and out are device buffers whose contents may
  * change between launches; the structures and scenes must outlive the plan.
  * rebuild = 1 needs accels to be the whole batch of one rq_build_batched
  * call.  No reference counterpart. */
@@ -405,6 +408,8 @@ typedef struct rq_plan_info_t {
   float shape_ms[4];        /* query time of 128/shallow, 128/deep, 256/shallow, 256/deep; < 0: dropped */
   uint32_t ray_order;       /* 1 when the plan traces through a per-scene ray order (chosen by time) */
   float ordered_ms[4];      /* the same shapes with the ray order (keys + sort + query); < 0: not offered */
+  uint32_t node_width;      /* node width the plan runs with (2, 4 or 8) */
+  float width_ms[3];        /* best query time with node width 2 / 4 / 8; < 0: not tried */
 } rq_plan_info_t;
 rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_accels, int32_t rebuild,
                            const rq_ray_t* rays, const uint32_t* ray_offsets, int32_t any, void* out,

@@ -1073,58 +1073,108 @@ rq_status_t rq_plan_create(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t n_ac
   }
   // Autotuning: time every launch shape on these rays, without and with the
   // ray order (whose time includes its keys and sort); a shape whose stack
-  // overflows on these trees is dropped.
+  // overflows on these trees is dropped.  A rebuilding plan owns its batch
+  // and also tries every node width (binary, collapsed 4-wide, compressed
+  // 8-wide): the structures keep the width the plan picks.
   const int shapes[4][2] = {{128, 0}, {128, 1}, {256, 0}, {256, 1}};
+  const uint32_t width0 = accels[0]->buf.node_width;
+  std::vector<uint32_t> widths;
+  if (rebuild) widths = {2, 4, 8};
+  else widths = {width0};
+  auto set_width = [&](uint32_t w) -> rq_status_t {
+    for (uint32_t k = 0; k < n_accels; ++k) {
+      AccelBuffers& b = accels[k]->buf;
+      if (b.node_width == w) continue;
+      b.node_width = 2;
+      BuildResult r;
+      if (w == 4) r = collapse_bvh4(b, ctx->scratch, ctx->d_err, ctx->stream);
+      else if (w == 8) r = collapse_bvh8(b, ctx->scratch, ctx->d_err, ctx->stream);
+      if (!r.ok()) return r.cuda != cudaSuccess ? cuda_fail(ctx, r.cuda, r.what) : fail(ctx, r.status, r.what);
+    }
+    RQ_TRY(collect_device_errors(ctx));
+    BatchedTrace keep = p->trace;
+    RQ_TRY(batch_tables(ctx, accels, n_accels, ray_offsets, any != 0, p->table, p->trace));
+    p->trace.rays = keep.rays;
+    p->trace.hits = keep.hits;
+    p->trace.occ = keep.occ;
+    return RQ_SUCCESS;
+  };
   float best = -1.f;
+  uint32_t best_width = width0;
+  auto wi = [](uint32_t w) { return w == 4 ? 1 : w == 8 ? 2 : 0; };
+  float tab[3][2][4];
+  for (auto& a : tab)
+    for (auto& b : a)
+      for (float& x : b) x = -1.f;
   if (p->trace.n > 0) {
     cudaEvent_t e0, e1;
     RQ_TRY_CUDA(ctx, cudaEventCreate(&e0));
     RQ_TRY_CUDA(ctx, cudaEventCreate(&e1));
-    for (int v = 0; v < (can_order ? 2 : 1); ++v) {
-      for (int k = 0; k < 4; ++k) {
-        float ms = 1e30f;
-        cudaError_t ce = cudaSuccess;
-        for (int rep = 0; rep < 3 && ce == cudaSuccess; ++rep) {
-          BatchedTrace t = p->trace;
-          ce = cudaEventRecord(e0, ctx->stream);
-          if (ce == cudaSuccess && v == 1) {
-            BuildResult br = enqueue_batch_order(t, p->order_keys, p->order_vals, p->order_scratch, ctx->d_err,
-                                                 ctx->stream);
-            if (!br.ok()) ce = br.cuda != cudaSuccess ? br.cuda : cudaErrorInvalidValue;
-          }
-          if (ce == cudaSuccess) ce = launch_trace_batched(t, shapes[k][0], shapes[k][1], ctx->stream);
-          if (ce == cudaSuccess) ce = cudaEventRecord(e1, ctx->stream);
-          if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
-          float tm = 0.f;
-          if (ce == cudaSuccess) ce = cudaEventElapsedTime(&tm, e0, e1);
-          if (ce == cudaSuccess && rep > 0) ms = std::min(ms, tm);
-        }
-        uint32_t derr = 0;
-        if (ce == cudaSuccess) ce = take_device_errors(ctx, &derr);
-        if (ce != cudaSuccess) {
+    for (uint32_t w : widths) {
+      if (widths.size() > 1) {
+        rq_status_t sw = set_width(w);
+        if (sw != RQ_SUCCESS) {
           cudaEventDestroy(e0);
           cudaEventDestroy(e1);
-          return cuda_fail(ctx, ce, "plan autotuning");
-        }
-        if (derr & ~kErrStackOverflow) {
-          cudaEventDestroy(e0);
-          cudaEventDestroy(e1);
-          return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed structure or input seen while autotuning");
-        }
-        if (derr & kErrStackOverflow) continue;
-        (v ? p->ordered_ms : p->shape_ms)[k] = ms;
-        if (best < 0.f || ms < best) {
-          best = ms;
-          p->block = shapes[k][0];
-          p->deep = shapes[k][1];
-          p->ordered = v == 1;
+          return sw;
         }
       }
+      float best_w = -1.f;
+      for (int v = 0; v < (can_order ? 2 : 1); ++v) {
+        for (int k = 0; k < 4; ++k) {
+          float ms = 1e30f;
+          cudaError_t ce = cudaSuccess;
+          for (int rep = 0; rep < 3 && ce == cudaSuccess; ++rep) {
+            BatchedTrace t = p->trace;
+            ce = cudaEventRecord(e0, ctx->stream);
+            if (ce == cudaSuccess && v == 1) {
+              BuildResult br = enqueue_batch_order(t, p->order_keys, p->order_vals, p->order_scratch, ctx->d_err,
+                                                   ctx->stream);
+              if (!br.ok()) ce = br.cuda != cudaSuccess ? br.cuda : cudaErrorInvalidValue;
+            }
+            if (ce == cudaSuccess) ce = launch_trace_batched(t, shapes[k][0], shapes[k][1], ctx->stream);
+            if (ce == cudaSuccess) ce = cudaEventRecord(e1, ctx->stream);
+            if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+            float tm = 0.f;
+            if (ce == cudaSuccess) ce = cudaEventElapsedTime(&tm, e0, e1);
+            if (ce == cudaSuccess && rep > 0) ms = std::min(ms, tm);
+          }
+          uint32_t derr = 0;
+          if (ce == cudaSuccess) ce = take_device_errors(ctx, &derr);
+          if (ce != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(ctx, ce, "plan autotuning");
+          }
+          if (derr & ~kErrStackOverflow) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "malformed structure or input seen while autotuning");
+          }
+          if (derr & kErrStackOverflow) continue;
+          tab[wi(w)][v][k] = ms;
+          if (best_w < 0.f || ms < best_w) best_w = ms;
+          if (best < 0.f || ms < best) {
+            best = ms;
+            best_width = w;
+            p->block = shapes[k][0];
+            p->deep = shapes[k][1];
+            p->ordered = v == 1;
+          }
+        }
+      }
+      p->width_ms[wi(w)] = best_w;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best < 0.f) return fail(ctx, RQ_ERROR_STACK_OVERFLOW, "every launch shape overflowed its traversal stack");
+    if (widths.size() > 1) RQ_TRY(set_width(best_width));
+    for (int k = 0; k < 4; ++k) {
+      p->shape_ms[k] = tab[wi(best_width)][0][k];
+      p->ordered_ms[k] = tab[wi(best_width)][1][k];
+    }
   }
+  p->node_width = best_width;
   // Capture [rebuild] + query into one graph on a private stream.
   cudaStream_t cap = nullptr;
   RQ_TRY_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -1176,6 +1226,8 @@ rq_status_t rq_plan_get_info(rq_plan_t p, rq_plan_info_t* info) {
   for (int k = 0; k < 4; ++k) info->shape_ms[k] = p->shape_ms[k];
   info->ray_order = p->ordered ? 1u : 0u;
   for (int k = 0; k < 4; ++k) info->ordered_ms[k] = p->ordered_ms[k];
+  info->node_width = p->node_width;
+  for (int k = 0; k < 3; ++k) info->width_ms[k] = p->width_ms[k];
   return RQ_SUCCESS;
 }
 

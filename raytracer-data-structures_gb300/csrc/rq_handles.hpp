@@ -95,6 +95,8 @@ struct rq_plan {
   bool ordered = false;                   // the query runs through a per-scene ray order
   float shape_ms[4] = {-1.f, -1.f, -1.f, -1.f};
   float ordered_ms[4] = {-1.f, -1.f, -1.f, -1.f};
+  uint32_t node_width = 2;                // the structures' node width the plan runs with
+  float width_ms[3] = {-1.f, -1.f, -1.f}; // best query time per node width 2 / 4 / 8 (< 0: not tried)
   DevBuf order_keys, order_vals;          // ray order keys and the permutation
   BuildScratch order_scratch;             // its sort's scratch (sized before the capture)
   cudaGraph_t graph = nullptr;

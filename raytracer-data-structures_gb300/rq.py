@@ -79,7 +79,8 @@ class Query(C.Structure):
 class PlanInfo(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("stack_entries", C.c_uint32), ("graph_kernels", C.c_uint32),
                 ("n_rays", C.c_uint32), ("rebuilds", C.c_uint32), ("shape_ms", C.c_float * 4),
-                ("ray_order", C.c_uint32), ("ordered_ms", C.c_float * 4)]
+                ("ray_order", C.c_uint32), ("ordered_ms", C.c_float * 4), ("node_width", C.c_uint32),
+                ("width_ms", C.c_float * 3)]
 
 
 class Plan:

@@ -133,9 +133,12 @@ def test_plan_replays_rebuild_and_query(engine, rqm):
     assert info.block_threads in (128, 256) and info.n_rays == n and info.rebuilds == 1
     assert info.graph_kernels >= 8  # the batched build's stages + the query
     assert max(info.shape_ms) > 0 and max(info.ordered_ms) > 0  # both variants timed
-    k = [128, 128, 256, 256].index(info.block_threads) + (1 if info.stack_entries == 64 else 0)
+    deep_entries = {2: 64, 4: 96, 8: 32}[info.node_width]  # the tuner also picked the node width
+    k = [128, 128, 256, 256].index(info.block_threads) + (1 if info.stack_entries == deep_entries else 0)
     chosen = (info.ordered_ms if info.ray_order else info.shape_ms)[k]
     assert chosen == min(t for t in list(info.shape_ms) + list(info.ordered_ms) if t >= 0)
+    assert min(info.width_ms) > 0 and chosen == min(info.width_ms)  # binary, 4-wide and 8-wide all timed
+    assert accs[0].info().node_width == info.node_width
     # move every mesh, then one replay rebuilds and traces
     for k2, (v, f) in enumerate(meshes):
         sc[k2].update((v + np.float32(0.25 * k2)).astype(np.float32))
