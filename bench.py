@@ -1007,10 +1007,19 @@ def run_case(args):
     --ray-sort 0/1), build (the LBVH rebuild), build-bvh / build-kd (the median
     BVH and SAH KD rebuilds of the same mesh), batched (the many-structure
     persistent query on the many-scene workload, 32 scenes with --small),
-    build-batched (the batched LBVH rebuild of the same scenes)."""
+    build-batched (the batched LBVH rebuild of the same scenes), render-c1
+    (rq_render of the small plain workload: camera rays, shading, shadow
+    rays, pixels), reference-render (rq_render_reference: the reference's
+    sphere render with the REFERENCE walk), brute (RQ_NONE on C1's 64x48
+    crop), serve (the serving loop's kernels: a few batched requests).
+    --node-width 4/8 walks the wide copies for primary/secondary/shadow."""
     import torch
     import rq
     import scenes
+
+    if args.case in ("render-c1", "reference-render", "brute", "serve"):
+        run_case_render(args)
+        return
 
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(dev)
@@ -1032,6 +1041,9 @@ def run_case(args):
         scene = eng.scene_triangles(verts, idx)
         acc = eng.build(scene, rq.LBVH)
         hits_p = eng.trace_closest(acc, primary)
+        if args.node_width != 2 and args.case in ("primary", "secondary", "shadow"):
+            eng.configure(node_width=args.node_width)
+            acc = eng.build(scene, rq.LBVH)
         if args.structure != "LBVH" and args.case in ("primary", "secondary", "shadow"):
             acc = eng.build(scene, args.structure)  # the same rays through another structure
         rays = {"primary": primary, "build": primary, "build-bvh": primary, "build-kd": primary,
@@ -1056,6 +1068,51 @@ def run_case(args):
     eng.close()
 
 
+def run_case_render(args):
+    """The render-step and serving kernels for profiling (see run_case)."""
+    import rq
+    import scenes
+
+    eng = rq.Engine(0)
+    if args.case == "reference-render":
+        sph = np.load(os.path.join(ROOT, "tests", "golden", "bunny.npz"))["spheres"]
+        colors = np.tile(np.array([0.8, 0.7, 0.0], np.float32), (len(sph), 1))
+        colors[-1] = 0.0
+        acc = eng.build(eng.scene_spheres(sph), rq.BVH)
+        eng.configure(traversal=rq.TRAVERSAL_REFERENCE)
+        call = lambda: eng.render_reference(acc, surface_rgb=colors)  # noqa: E731
+    elif args.case == "serve":
+        srv = rq.Server(batching=True)
+        meshes = scenes.mixed_meshes(8, 1e4, 2e5, SEED + 60, kinds=("icosphere",))
+        for k, (v, f, _) in enumerate(meshes):
+            srv.add_mesh(k, v, f)
+        view = rq.make_view(eye=(2.7, 0.5, 0.9), target=(0.5, 0.5, 0.5), up=(0.0, 0.0, 1.0), fov_deg=45.0,
+                            light=(1.5, -2.0, 3.0), albedo=(0.7, 0.65, 0.6), ambient=0.1, seed=7)
+
+        def call():
+            tickets = [srv.submit(k % 8, view, 640, 480, 2, keep_pixels=False) for k in range(16)]
+            for t in tickets:
+                srv.wait(t, want_pixels=False)
+    else:
+        v, f = scenes.c1_mesh()
+        s = eng.scene_triangles(v, f)
+        eng.configure(width=640, height=480, aa_samples=1)
+        if args.case == "brute":
+            acc = eng.build(s, rq.NONE)
+            view = rq.make_view(window=(288, 216, 64, 48), **scenes.C1_VIEW)
+        else:
+            acc = eng.build(s, rq.LBVH)
+            view = rq.make_view(**scenes.C1_VIEW)
+        call = lambda: eng.render(acc, view)  # noqa: E731
+    for _ in range(args.warmup + args.steps):
+        call()
+    eng.synchronize()
+    log(f"[bench] case {args.case}: {args.warmup + args.steps} calls done")
+    if args.case == "serve":
+        srv.close()
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1070,11 +1127,13 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="skip the many-scene leg")
     ap.add_argument("--skip-serve", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--case", choices=["primary", "secondary", "shadow", "build", "build-bvh", "build-kd",
-                                       "batched", "build-batched"],
+                                       "batched", "build-batched", "render-c1", "reference-render", "brute",
+                                       "serve"],
                     help="profiling driver: run one query class, print no bench line")
     ap.add_argument("--structure", choices=["LBVH", "BVH", "KDTREE"], default="LBVH",
                     help="structure traced by --case primary/secondary/shadow")
     ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
+    ap.add_argument("--node-width", type=int, default=2, choices=[2, 4, 8], help="--case: settings.node_width")
     ap.add_argument("--scheduling", type=int, default=0, help="--case: settings.scheduling (0-3)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner and use its GB300 choice (binary nodes, cube Morton codes, "

@@ -199,7 +199,8 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
   } else {
     Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
                a.root.as<const float>(), a.n_nodes, a.n_slots};
-    launch_trace_bvh2(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, nullptr, q.small_stack);
+    launch_trace_bvh2(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, nullptr, q.small_stack,
+                      q.exact);
   }
 }
 
@@ -213,8 +214,13 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   const bool spec = fast && cfg.scheduling == RQ_SCHEDULING_SPECULATIVE && !wide;
   const bool packet = fast && cfg.scheduling == RQ_SCHEDULING_WARP_PACKET && !wide;
   const bool top = fast && cfg.scheduling == RQ_SCHEDULING_SHARED_TOP && !wide && !q.small_stack;
+  QueryTarget qx = q;
+  if (bvh2 && cfg.traversal == RQ_TRAVERSAL_FAST && a.node_width == 2 && !q.small_stack) {
+    RQ_B(sc.exact.ensure(((size_t)q.n + 1) * 4), "exact-ray list");
+    qx.exact = sc.exact.as<uint32_t>();
+  }
   if (!sorted && !refill && !spec && !packet && !top) {
-    launch_query(type, s, a, cfg.traversal, any, q, err, st);
+    launch_query(type, s, a, cfg.traversal, any, qx, err, st);
     RQ_B(cudaGetLastError(), "trace launch");
     return {};
   }
@@ -260,7 +266,8 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   }
   if (a.node_width == 4) launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
   else if (a.node_width == 8) launch_trace_bvh8(s.kind, any, bvh8_view(a), q.rays, q.n, q.hits, q.occ, err, st, perm);
-  else launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm, q.small_stack);
+  else launch_trace_bvh2(s.kind, cfg.traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, perm, q.small_stack,
+                         qx.exact);
   RQ_B(cudaGetLastError(), "trace launch");
   return {};
 }

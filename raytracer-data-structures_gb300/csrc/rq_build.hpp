@@ -56,10 +56,12 @@ struct BuildScratch {
   DevBuf kd_refs;             // KD: next level's primitive references
   DevBuf work;                // work counter of lane-refill traversal
   DevBuf top;                 // top-level node copy of RQ_SCHEDULING_SHARED_TOP queries
+  DevBuf exact;               // rays that need the exact box test, set aside by FAST queries
   const uint32_t* stall = nullptr;  // sort test hook (SortScratch::stall); null in normal use
   void release() {
     work.release();
     top.release();
+    exact.release();
     keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); mark.release(); lohi.release();
     keys.release(); vals.release();
     m0.release(); m1.release(); m2.release(); m3.release(); m4.release(); m5.release(); m6.release(); m7.release();
@@ -145,6 +147,7 @@ struct QueryTarget {
   float4* hits = nullptr;
   uint32_t* occ = nullptr;
   bool small_stack = false;  // test hook: FAST BVH2 walk with a traversal stack of kDebugStack entries
+  uint32_t* exact = nullptr;  // n + 1 words: rays set aside for the exact box test (launch_trace_bvh2)
 };
 // Batches of at least this many rays are reordered when settings.ray_sort asks.
 constexpr uint32_t kRaySortMin = 65536;

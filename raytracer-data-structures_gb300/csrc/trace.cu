@@ -22,56 +22,41 @@ namespace {
 
 constexpr int kThreads = 128;
 
-// One ray with the exact box test (rq_device.cuh: rays whose direction has a
-// zero component), result written like k_trace_fast's.  Out of line and
-// called only after a block's other rays are done, so the fused walk's
-// register budget does not carry it.
-template <int KIND, bool ANY, bool COUNT, int STACK>
-__device__ __noinline__ void trace_exact_ray(const Bvh2View& bvh, const float4* __restrict__ rays, uint32_t r,
-                                             float4* __restrict__ hits, uint32_t* __restrict__ occ, uint32_t* err,
-                                             unsigned long long* counters) {
-  const Ray ray = load_ray(rays, r);
-  Closest c = {ray.tmax, kMiss, 0.f, 0.f};
-  uint32_t visits = 0, tests = 0;
-  const bool occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, c, visits, tests, err);
-  if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
-  if (ANY && occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
-  if (COUNT) {
-    atomicAdd(counters, (unsigned long long)visits);
-    atomicAdd(counters + 1, (unsigned long long)tests);
-  }
-}
-
 // perm (may be null): thread i traces ray perm[i] and writes that ray's result
 // (a reordering for coherence that leaves every result where the caller
 // expects it).  With perm, any-hit bits are set with atomicOr on a zeroed array.
-// Rays that need the exact box test are set aside in shared memory and traced
-// by the block's threads after the others (their any-hit bits are then set
-// with atomicOr over the ballot's word, which the block has already stored).
+// SPLIT: rays that need the exact box test (rq_device.cuh: a direction
+// component zero or too small for the fused form) are not walked here but
+// appended to `exact` (count in word 0, ray indices after it) for
+// k_trace_exact, so this kernel carries only the fused walk; otherwise both
+// walks are inlined and each ray takes the one it needs.
 // At most 48 registers (10 blocks of 128 per SM): measured 3-4% faster on
 // the closest-hit triangle walk than the unconstrained 52.
-template <int KIND, bool ANY, bool COUNT = false, int STACK = kStackSize>
+template <int KIND, bool ANY, bool COUNT = false, int STACK = kStackSize, bool SPLIT = false>
 __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const float4* __restrict__ rays,
                                                          uint32_t n, float4* __restrict__ hits,
                                                          uint32_t* __restrict__ occ, uint32_t* err,
                                                          unsigned long long* counters = nullptr,
-                                                         const uint32_t* __restrict__ perm = nullptr) {
-  __shared__ uint32_t s_exact[kThreads];
-  __shared__ uint32_t s_n;
-  if (threadIdx.x == 0) s_n = 0;
-  __syncthreads();
+                                                         const uint32_t* __restrict__ perm = nullptr,
+                                                         uint32_t* __restrict__ exact = nullptr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t r = (perm && i < n) ? __ldg(perm + i) : i;
   bool occluded = false;
   uint32_t visits = 0, tests = 0;
   if (i < n) {
     Ray ray = load_ray(rays, r);
-    if (zero_dir(slab_ray(ray.o, ray.d))) {
-      s_exact[atomicAdd(&s_n, 1u)] = r;
-    } else {
-      Closest c = {ray.tmax, kMiss, 0.f, 0.f};
-      occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    if (!SPLIT) {
+      occluded = walk_bvh2<KIND, ANY, COUNT, STACK>(bvh, ray, c, visits, tests, err);
       if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+    } else {
+      const SlabRay sr = slab_ray(ray.o, ray.d);
+      if (zero_dir(sr)) {
+        exact[1 + atomicAdd(exact, 1u)] = r;
+      } else {
+        occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, sr, c, visits, tests, err);
+        if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+      }
     }
   }
   if (ANY) {
@@ -84,10 +69,28 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const
     }
   }
   if (COUNT) add_counts(counters, visits, tests);
-  __syncthreads();
-  const uint32_t ne = s_n;
-  for (uint32_t k = threadIdx.x; k < ne; k += blockDim.x)
-    trace_exact_ray<KIND, ANY, COUNT, STACK>(bvh, rays, s_exact[k], hits, occ, err, counters);
+}
+
+// The rays k_trace_fast<SPLIT> set aside, walked with the exact box test; a
+// fixed grid strides over the list (empty in most queries).  Any-hit bits
+// are set with atomicOr over the words k_trace_fast stored before.
+constexpr uint32_t kExactBlocks = 304;
+template <int KIND, bool ANY>
+__global__ void __launch_bounds__(kThreads) k_trace_exact(Bvh2View bvh, const float4* __restrict__ rays,
+                                                          const uint32_t* __restrict__ exact,
+                                                          float4* __restrict__ hits, uint32_t* __restrict__ occ,
+                                                          uint32_t* err) {
+  const uint32_t count = exact[0];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    const uint32_t r = exact[1 + k];
+    const Ray ray = load_ray(rays, r);
+    Closest c = {ray.tmax, kMiss, 0.f, 0.f};
+    uint32_t visits = 0, tests = 0;
+    const bool occluded =
+        walk_bvh2_form<KIND, ANY, false, kStackSize, true>(bvh, ray, slab_ray(ray.o, ray.d), c, visits, tests, err);
+    if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+    if (ANY && occluded) atomicOr(occ + (r >> 5), 1u << (r & 31));
+  }
 }
 
 // ------------------------------------------------ top levels in shared memory
@@ -231,7 +234,8 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_top(Bvh2View bvh, const 
     const Ray ray = load_ray(rays, re);
     Closest c = {ray.tmax, kMiss, 0.f, 0.f};
     uint32_t visits = 0, tests = 0;
-    const bool occ_e = walk_bvh2_form<KIND, ANY, false, kStackSize, true>(bvh, ray, c, visits, tests, err);
+    const bool occ_e =
+        walk_bvh2_form<KIND, ANY, false, kStackSize, true>(bvh, ray, slab_ray(ray.o, ray.d), c, visits, tests, err);
     if (!ANY) hits[re] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
     if (ANY && occ_e) atomicOr(occ + (re >> 5), 1u << (re & 31));
   }
@@ -819,14 +823,22 @@ __global__ void __launch_bounds__(kThreads) k_brute(const float4* __restrict__ p
 
 template <int KIND, bool ANY>
 void dispatch_bvh2(int traversal, const Bvh2View& v, const float4* rays, uint32_t n, float4* hits,
-                   uint32_t* occ, uint32_t* err, const uint32_t* perm, bool small_stack, cudaStream_t s) {
+                   uint32_t* occ, uint32_t* err, const uint32_t* perm, bool small_stack, uint32_t* exact,
+                   cudaStream_t s) {
   uint32_t g = (n + kThreads - 1) / kThreads;
-  if (traversal == RQ_TRAVERSAL_REFERENCE)
+  if (traversal == RQ_TRAVERSAL_REFERENCE) {
     k_trace_ref<KIND, ANY><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err);
-  else if (small_stack)
+  } else if (small_stack) {
     k_trace_fast<KIND, ANY, false, kDebugStack><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr, perm);
-  else
+  } else if (exact) {
+    cudaMemsetAsync(exact, 0, 4, s);
+    k_trace_fast<KIND, ANY, false, kStackSize, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr,
+                                                                            perm, exact);
+    count_launch();
+    k_trace_exact<KIND, ANY><<<kExactBlocks, kThreads, 0, s>>>(v, rays, exact, hits, occ, err);
+  } else {
     k_trace_fast<KIND, ANY, false><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr, perm);
+  }
 }
 
 template <int KIND, bool ANY>
@@ -864,17 +876,17 @@ void launch_trace_bvh2_counted(int kind, bool any, const Bvh2View& v, const floa
 
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
                        uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
-                       const uint32_t* perm, bool small_stack) {
+                       const uint32_t* perm, bool small_stack, uint32_t* exact) {
   if (n == 0) return;
   count_launch();
   if (traversal == RQ_TRAVERSAL_REFERENCE) perm = nullptr;
   if (any && perm) cudaMemsetAsync(occ, 0, (size_t)((n + 31) / 32) * 4, s);
   if (kind == kTriangles) {
-    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
-    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
+    if (any) dispatch_bvh2<kTriangles, true>(traversal, v, rays, n, hits, occ, err, perm, small_stack, exact, s);
+    else dispatch_bvh2<kTriangles, false>(traversal, v, rays, n, hits, occ, err, perm, small_stack, exact, s);
   } else {
-    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
-    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, perm, small_stack, s);
+    if (any) dispatch_bvh2<kSpheres, true>(traversal, v, rays, n, hits, occ, err, perm, small_stack, exact, s);
+    else dispatch_bvh2<kSpheres, false>(traversal, v, rays, n, hits, occ, err, perm, small_stack, exact, s);
   }
 }
 

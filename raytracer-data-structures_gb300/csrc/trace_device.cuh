@@ -95,9 +95,8 @@ __device__ __forceinline__ void load_node(const float4* nd, float4& a, float4& b
 // EXACT: the exact-sign box test (rays with a zero direction component).
 // Returns true when an any-hit query found a hit.
 template <int KIND, bool ANY, bool COUNT, int STACK, bool EXACT>
-__device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
-                                               uint32_t& tests, uint32_t* err) {
-  const SlabRay sr = slab_ray(ray.o, ray.d);
+__device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& ray, const SlabRay& sr, Closest& c,
+                                               uint32_t& visits, uint32_t& tests, uint32_t* err) {
   float tn;
   const float* rb = bvh.root;
   if (!slab_box<EXACT>(sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
@@ -151,8 +150,9 @@ __device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& r
 template <int KIND, bool ANY, bool COUNT, int STACK>
 __device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
                                           uint32_t& tests, uint32_t* err) {
-  return zero_dir(slab_ray(ray.o, ray.d)) ? walk_bvh2_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, c, visits, tests, err)
-                         : walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, c, visits, tests, err);
+  const SlabRay sr = slab_ray(ray.o, ray.d);
+  return zero_dir(sr) ? walk_bvh2_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, sr, c, visits, tests, err)
+                      : walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, sr, c, visits, tests, err);
 }
 
 // Sum the per-thread visit / test counts of a warp into counters[0..1].

@@ -156,6 +156,8 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
     if ((e = rs.list_b.ensure(nray * 4)) != cudaSuccess) return e;
     if ((e = rs.list_s.ensure(nray * 4)) != cudaSuccess) return e;
     if ((e = rs.list_n.ensure(64)) != cudaSuccess) return e;
+    if ((e = sc.exact.ensure((nray + 1) * 4)) != cudaSuccess) return e;
+    uint32_t* exact = sc.exact.as<uint32_t>();
     uint32_t* live = nullptr;  // null: every sample (depth 0)
     uint32_t* next = rs.list_a.as<uint32_t>();
     uint32_t* spare = rs.list_b.as<uint32_t>();
@@ -185,7 +187,8 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
       } else if (a.node_width == 8) {
         launch_trace_bvh8(s.kind, false, b8, rays, n_live, hits, nullptr, err, st, live);
       } else {
-        launch_trace_bvh2(s.kind, RQ_TRAVERSAL_FAST, false, bv, rays, n_live, hits, nullptr, err, st, live);
+        launch_trace_bvh2(s.kind, RQ_TRAVERSAL_FAST, false, bv, rays, n_live, hits, nullptr, err, st, live, false,
+                          exact);
       }
       if ((e = cudaMemsetAsync(counts, 0, 8, st)) != cudaSuccess) return e;
       count_launch();
@@ -209,7 +212,8 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
         else if (a.node_width == 8)
           launch_trace_bvh8(s.kind, true, b8, shadow, n_shadow, nullptr, bits, err, st, slist);
         else
-          launch_trace_bvh2(s.kind, RQ_TRAVERSAL_FAST, true, bv, shadow, n_shadow, nullptr, bits, err, st, slist);
+          launch_trace_bvh2(s.kind, RQ_TRAVERSAL_FAST, true, bv, shadow, n_shadow, nullptr, bits, err, st, slist,
+                            false, exact);
         count_launch();
         k_accum_list<<<(n_shadow + kThreads - 1) / kThreads, kThreads, 0, st>>>(slist, n_shadow, bits, pend, cw);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
