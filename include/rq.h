@@ -547,15 +547,21 @@ rq_status_t rq_reference_spheres(const char* path, int32_t clones, float** spher
  *    (width * height * spp) must fit max_batch_rays; requests whose mesh
  *    cannot fit the HBM budget complete with RQ_ERROR_OUT_OF_MEMORY.
  *  - Residency: meshes are kept on the host; a request's mesh is uploaded and
- *    its LBVH built on first use.  Resident scenes and structures stay within
- *    hbm_budget bytes by evicting the least recently used meshes the batch
- *    being formed does not need (rebuilt when requested again).
- *  - Continuous batching (batching = 1): every step takes the waiting
- *    requests in arrival order up to max_batch_rays camera rays and
- *    max_batch_requests requests and renders them as one wavefront (camera
+ *    its LBVH built on first use, on a stream of its own beside the rendering.
+ *    Resident scenes and structures and the wavefront buffers (112 bytes per
+ *    camera sample in flight) stay within hbm_budget bytes by evicting the
+ *    least recently used meshes that no step being formed or in flight needs
+ *    (rebuilt when requested again).
+ *  - Continuous batching (batching = 1): each step takes rows of the waiting
+ *    requests in arrival order, up to step_rays camera rays and
+ *    max_batch_requests requests (a larger request is split by rows and
+ *    finished in later steps), and renders them as one wavefront (camera
  *    rays, one many-structure closest-hit query, shading, one many-structure
- *    shadow query, pixels, one download).  batching = 0 renders one request
- *    per step.
+ *    shadow query, pixels, one download).  Two steps are in flight at once on
+ *    two streams: requests that arrive while one step runs go into the next,
+ *    which starts on the GPU beside it.  A request completes when its last
+ *    rows land.  batching = 0 renders one whole request per step and waits
+ *    for each step before the next.
  *  - A request renders exactly what rq_render renders for the same view with
  *    bounces = 0, settings.bias = 1e-4 and its width, height, spp and
  *    background, alone or among others.
@@ -565,9 +571,10 @@ typedef struct rq_server* rq_server_t;
 typedef struct rq_server_config_t {
   int32_t device;              /* CUDA ordinal */
   int32_t batching;            /* 1: continuous batching; 0: one request per step */
-  uint64_t hbm_budget;         /* bytes of resident scenes + structures; 0: 80 GB */
-  uint32_t max_batch_rays;     /* camera rays per step; 0: 2^25 (below 2^31) */
-  uint32_t max_batch_requests; /* requests per step; 0: 256 */
+  uint64_t hbm_budget;         /* bytes of resident scenes + structures + wavefront buffers; 0: 80 GB */
+  uint32_t max_batch_rays;     /* camera rays of one request at most; 0: 2^25 (below 2^31) */
+  uint32_t max_batch_requests; /* requests (or parts of requests) per step; 0: 256 */
+  uint32_t step_rays;          /* batching: camera rays per step; larger requests are split by rows; 0: 2^22 */
 } rq_server_config_t;
 typedef struct rq_request_t {
   uint32_t mesh_id;

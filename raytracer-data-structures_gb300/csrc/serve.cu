@@ -11,17 +11,19 @@
 //    within the HBM budget: the least recently used meshes that neither the
 //    batch being formed nor a batch in flight needs are evicted.
 //  * Continuous batching (batching = 1): two wavefront slots, each with its
-//    own stream and buffers.  While one slot's step runs on the GPU, the
-//    requests that arrive are formed into the next step (everything waiting,
-//    in arrival order, up to the batch limits and the memory budget) and
-//    launched on the other slot, so consecutive steps overlap on the device.
-//    A step renders all its requests as one wavefront: camera rays of every
-//    request, one persistent many-structure closest-hit query, shading, one
-//    many-structure shadow query, the light terms and every request's pixels,
-//    then one download; a host callback on the slot's stream tells the worker
-//    when it has landed.  batching = 0 serves one request per step on one
-//    slot, each step waited for before the next (the one-request-per-launch
-//    comparison).
+//    own stream and buffers.  A step takes rows of the waiting requests, in
+//    arrival order, up to a bounded number of camera rays (step_rays); a
+//    larger request is split by rows (a window of its image: the same
+//    samples as the whole image's) and finished in later steps, so no
+//    request holds the GPU for long.  While one slot's step runs, the rows
+//    waiting are formed into the next step on the other slot, which starts
+//    on the GPU beside it.  A step renders all its rows as one wavefront:
+//    camera rays, one persistent many-structure closest-hit query, shading,
+//    one many-structure shadow query, the light terms and the pixels, then
+//    one download; a host callback on the slot's stream tells the worker
+//    when it has landed, and a request completes with its last rows.
+//    batching = 0 serves one whole request per step on one slot, each step
+//    waited for before the next (the one-request-per-launch comparison).
 //  * Latency: from rq_server_submit to the moment the request's pixels are
 //    in host memory; the worker keeps every completed request's latency for
 //    the percentile statistics.  Busy time is the time at least one step is
@@ -123,6 +125,14 @@ struct Pending {
   bool done = false;
   rq_status_t status = RQ_SUCCESS;
   std::vector<uint8_t> pixels;
+  uint32_t next_row = 0;     // rows handed to steps (worker)
+  uint32_t rows_landed = 0;  // rows whose step has landed or failed (worker)
+};
+
+// A step's share of one request: image rows [y0, y0 + rows).
+struct Item {
+  Pending* p = nullptr;
+  uint32_t y0 = 0, rows = 0;
 };
 
 // One wavefront slot: a stream, its buffers and the step in flight on it.
@@ -134,11 +144,11 @@ struct Slot {
   bool busy = false;
   uint64_t seq = 0;
   std::atomic<bool> landed{false};
-  std::vector<Pending*> batch;
-  std::vector<rq_status_t> status;
-  std::vector<Mesh*> mesh;
+  std::vector<Item> items;
+  std::vector<rq_status_t> status;  // per item
+  std::vector<Mesh*> mesh;          // per item
   std::vector<uint32_t> poff;
-  std::vector<size_t> which;
+  std::vector<size_t> which;        // items that went ahead
   uint32_t npix = 0;
   uint64_t nray = 0;
   uint64_t device_bytes() const {
@@ -200,12 +210,12 @@ struct rq_server {
   void run();
   Slot* free_slot();
   Slot* oldest_busy();
-  bool launch(Slot& sl, std::vector<Pending*>& batch);
+  bool launch(Slot& sl, std::vector<Item>& items);
   void retire(Slot& sl);
   uint64_t engine_bytes() const;
   rq_status_t make_resident(Mesh& mesh, const std::vector<Mesh*>& keep, uint64_t wavefront);
   bool evict_one(const std::vector<Mesh*>& keep);
-  void finish(std::vector<Pending*>& batch, const std::vector<rq_status_t>& status);
+  void land(const Item& it, rq_status_t status, const uint8_t* pixels);
 };
 
 namespace {
@@ -280,20 +290,28 @@ rq_status_t rq_server::make_resident(Mesh& mesh, const std::vector<Mesh*>& keep,
   return RQ_SUCCESS;
 }
 
-void rq_server::finish(std::vector<Pending*>& batch, const std::vector<rq_status_t>& status) {
+// Rows of a request have landed (or failed): copy its pixels in; the
+// request completes with its last rows.
+void rq_server::land(const Item& it, rq_status_t status, const uint8_t* pixels) {
+  Pending* p = it.p;
+  const rq_request_t& r = p->req;
+  if (status != RQ_SUCCESS && p->status == RQ_SUCCESS) p->status = status;
+  if (status == RQ_SUCCESS && r.keep_pixels && pixels) {
+    if (p->pixels.empty()) p->pixels.resize((size_t)r.width * r.height * 3);
+    std::memcpy(p->pixels.data() + (size_t)it.y0 * r.width * 3, pixels, (size_t)it.rows * r.width * 3);
+  }
+  p->rows_landed += it.rows;
+  if (p->rows_landed < r.height) return;
   const Clock::time_point now = Clock::now();
   {
     std::lock_guard<std::mutex> g(m);
-    for (size_t k = 0; k < batch.size(); ++k) {
-      Pending* p = batch[k];
-      p->status = status[k];
-      p->done = true;
-      if (status[k] == RQ_SUCCESS) {
-        ++st.completed;
-        lat_ms.push_back(std::chrono::duration<double, std::milli>(now - p->t_submit).count());
-      } else {
-        ++st.rejected;
-      }
+    p->done = true;
+    if (p->status == RQ_SUCCESS) {
+      ++st.completed;
+      lat_ms.push_back(std::chrono::duration<double, std::milli>(now - p->t_submit).count());
+    } else {
+      p->pixels.clear();
+      ++st.rejected;
     }
   }
   cv_done.notify_all();
@@ -314,17 +332,17 @@ Slot* rq_server::oldest_busy() {
 
 // Resolve meshes, make them resident, build the step's tables and enqueue the
 // whole wavefront on the slot's stream.  Returns true when a step went in
-// flight; requests that cannot go ahead are finished at once.
-bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
-  const size_t n = batch.size();
-  sl.batch = batch;
+// flight; items that cannot go ahead land at once with their error.
+bool rq_server::launch(Slot& sl, std::vector<Item>& items) {
+  const size_t n = items.size();
+  sl.items = items;
   sl.status.assign(n, RQ_SUCCESS);
   sl.mesh.assign(n, nullptr);
   ++batch_no;
   {
     std::lock_guard<std::mutex> g(m);
     for (size_t k = 0; k < n; ++k) {
-      auto it = meshes.find(batch[k]->req.mesh_id);
+      auto it = meshes.find(items[k].p->req.mesh_id);
       if (it == meshes.end()) sl.status[k] = RQ_ERROR_INVALID_ARGUMENT;
       else sl.mesh[k] = it->second.get();
     }
@@ -332,9 +350,9 @@ bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
   // Wavefront growth this step would add to the slot's buffers.
   uint64_t rays_all = 0, pix_all = 0;
   for (size_t k = 0; k < n; ++k) {
-    const rq_request_t& r = batch[k]->req;
-    rays_all += (uint64_t)r.width * r.height * r.spp;
-    pix_all += (uint64_t)r.width * r.height;
+    const rq_request_t& r = items[k].p->req;
+    rays_all += (uint64_t)r.width * items[k].rows * r.spp;
+    pix_all += (uint64_t)r.width * items[k].rows;
   }
   const uint64_t want = rays_all * kSampleBytes + pix_all * 3 + 4096;
   const uint64_t have = sl.device_bytes();
@@ -346,7 +364,8 @@ bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
   }
   while (resident + engine_bytes() + grow > cfg.hbm_budget && evict_one(sl.mesh)) {
   }
-  // Tables of the requests that go ahead.
+  // Tables of the items that go ahead: each renders its rows as a window of
+  // the request's full image.
   std::vector<ServeReq> sreq;
   std::vector<Bvh2View> views;
   std::vector<uint32_t> roff(1, 0);
@@ -354,11 +373,14 @@ bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
   sl.which.clear();
   for (size_t k = 0; k < n; ++k) {
     if (sl.status[k] != RQ_SUCCESS) continue;
-    const rq_request_t& r = batch[k]->req;
+    const rq_request_t& r = items[k].p->req;
     const float tan_half = (float)std::tan((double)r.view.fov_deg * 3.141592653589793 / 360.0);
     rq_view_t view = r.view;
     view.bounces = 0;
-    view.window[0] = view.window[1] = view.window[2] = view.window[3] = 0;
+    view.window[0] = 0;
+    view.window[1] = items[k].y0;
+    view.window[2] = r.width;
+    view.window[3] = items[k].rows;
     ServeReq q;
     q.v = make_view_dev(view, r.width, r.height, r.spp, r.background, ctx->settings.bias, tan_half);
     rq_scene_t sc = sl.mesh[k]->scene;
@@ -374,13 +396,13 @@ bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
     const AccelBuffers& b = sl.mesh[k]->accel->buf;
     views.push_back({b.nodes.as<const float4>(), b.prims.as<const float4>(), b.order.as<const uint32_t>(),
                      b.root.as<const float>(), b.n_nodes, b.n_slots});
-    roff.push_back(roff.back() + r.width * r.height * r.spp);
-    sl.poff.push_back(sl.poff.back() + r.width * r.height);
+    roff.push_back(roff.back() + r.width * items[k].rows * r.spp);
+    sl.poff.push_back(sl.poff.back() + r.width * items[k].rows);
     sl.which.push_back(k);
   }
   const uint32_t nq = (uint32_t)sl.which.size();
   if (nq == 0) {
-    finish(sl.batch, sl.status);
+    for (size_t k = 0; k < n; ++k) land(items[k], sl.status[k], nullptr);
     return false;
   }
   const uint32_t nray = roff.back(), npix = sl.poff.back();
@@ -482,10 +504,12 @@ bool rq_server::launch(Slot& sl, std::vector<Pending*>& batch) {
     }
     cudaGetLastError();
     for (size_t j = 0; j < sl.which.size(); ++j) sl.status[sl.which[j]] = RQ_ERROR_CUDA;
-    finish(sl.batch, sl.status);
+    for (size_t k = 0; k < n; ++k) land(items[k], sl.status[k], nullptr);
     return false;
   }
   for (size_t j = 0; j < sl.which.size(); ++j) ++sl.mesh[sl.which[j]]->in_flight;
+  for (size_t k = 0; k < n; ++k)  // items that could not go ahead land now
+    if (sl.status[k] != RQ_SUCCESS) land(items[k], sl.status[k], nullptr);
   sl.npix = npix;
   sl.nray = nray;
   sl.busy = true;
@@ -504,16 +528,6 @@ void rq_server::retire(Slot& sl) {
     std::lock_guard<std::mutex> g(m);
     worker_error = "device error flag set during a batch";
   }
-  for (size_t j = 0; j < sl.which.size(); ++j) {
-    const size_t k = sl.which[j];
-    --sl.mesh[k]->in_flight;
-    if (derr) {
-      sl.status[k] = (derr & kErrStackOverflow) ? RQ_ERROR_STACK_OVERFLOW : RQ_ERROR_INVALID_ARGUMENT;
-      continue;
-    }
-    if (sl.batch[k]->req.keep_pixels)
-      sl.batch[k]->pixels.assign(sl.host + 3 * (size_t)sl.poff[j], sl.host + 3 * (size_t)sl.poff[j + 1]);
-  }
   sl.busy = false;
   {
     std::lock_guard<std::mutex> g(m);
@@ -522,7 +536,13 @@ void rq_server::retire(Slot& sl) {
     st.shadow_rays += shadow_rays;
     st.resident_bytes = resident;
   }
-  finish(sl.batch, sl.status);
+  for (size_t j = 0; j < sl.which.size(); ++j) {
+    const size_t k = sl.which[j];
+    --sl.mesh[k]->in_flight;
+    const rq_status_t stt =
+        derr ? ((derr & kErrStackOverflow) ? RQ_ERROR_STACK_OVERFLOW : RQ_ERROR_INVALID_ARGUMENT) : RQ_SUCCESS;
+    land(sl.items[k], stt, sl.host + 3 * (size_t)sl.poff[j]);
+  }
 }
 
 void rq_server::run() {
@@ -538,26 +558,57 @@ void rq_server::run() {
         st.busy_s += std::chrono::duration<double>(Clock::now() - busy_since).count();
       }
     }
-    std::vector<Pending*> batch;
+    std::vector<Item> items;
     Slot* sl = free_slot();
     {
       std::unique_lock<std::mutex> lk(m);
       if (stop && !oldest_busy()) return;
       if (sl && !queue.empty() && !stop) {
-        // everything waiting, in arrival order, up to the limits
-        uint64_t rays_in = 0;
-        while (!queue.empty()) {
+        if (!cfg.batching) {  // one whole request per step
           Pending* p = queue.front();
-          const uint64_t r = (uint64_t)p->req.width * p->req.height * p->req.spp;
-          if (!batch.empty() && (!cfg.batching || batch.size() >= cfg.max_batch_requests ||
-                                 rays_in + r > cfg.max_batch_rays))
-            break;
-          batch.push_back(p);
-          rays_in += r;
           queue.pop_front();
+          items.push_back({p, 0, p->req.height});
+          p->next_row = p->req.height;
+        } else {
+          // Rows of the waiting requests up to the step's ray budget: first
+          // an equal share of the budget each (at least one row), then what
+          // is left, in arrival order.  A request larger than its share is
+          // split by rows and finished in later steps, so requests that
+          // arrive behind a large one are not held up by all of it.
+          std::vector<Pending*> cand;
+          for (Pending* p : queue) {
+            cand.push_back(p);
+            if (cand.size() >= cfg.max_batch_requests) break;
+          }
+          const uint64_t budget = cfg.step_rays;
+          const uint64_t share = std::max<uint64_t>(1, budget / cand.size());
+          std::vector<uint32_t> take(cand.size(), 0);
+          uint64_t used = 0;
+          for (int pass = 0; pass < 2; ++pass) {
+            for (size_t k = 0; k < cand.size(); ++k) {
+              const Pending* p = cand[k];
+              const uint64_t row_rays = (uint64_t)p->req.width * p->req.spp;
+              const uint64_t rows_left = p->req.height - p->next_row - take[k];
+              const uint64_t room = budget > used ? (budget - used) / row_rays : 0;
+              uint64_t t = pass == 0 ? std::min<uint64_t>(std::max<uint64_t>(1, share / row_rays), room) : room;
+              if (pass == 0 && used == 0 && t == 0) t = 1;  // a row wider than the budget still goes, alone
+              t = std::min<uint64_t>(t, rows_left);
+              take[k] += (uint32_t)t;
+              used += t * row_rays;
+            }
+          }
+          for (size_t k = 0; k < cand.size(); ++k) {
+            if (!take[k]) continue;
+            items.push_back({cand[k], cand[k]->next_row, take[k]});
+            cand[k]->next_row += take[k];
+          }
+          for (auto it = queue.begin(); it != queue.end();) {  // fully handed out: leave the queue
+            if ((*it)->next_row == (*it)->req.height) it = queue.erase(it);
+            else ++it;
+          }
         }
       }
-      if (batch.empty()) {
+      if (items.empty()) {
         // wait for an arrival (when a slot is free) or for a step to land
         // (slot states change only on this thread; `landed` is set under m)
         cv_work.wait(lk, [&] {
@@ -571,7 +622,7 @@ void rq_server::run() {
     }
     const bool was_idle = oldest_busy() == nullptr;
     const Clock::time_point t0 = Clock::now();
-    if (launch(*sl, batch) && was_idle) busy_since = t0;
+    if (launch(*sl, items) && was_idle) busy_since = t0;
     if (!cfg.batching) {  // the plain path: each step waited for before the next
       cudaStreamSynchronize(sl->stream);
     }
@@ -590,6 +641,7 @@ rq_status_t rq_server_create(const rq_server_config_t* cfg, rq_server_t* out) {
   if (s->cfg.hbm_budget == 0) s->cfg.hbm_budget = 80ull << 30;
   if (s->cfg.max_batch_rays == 0) s->cfg.max_batch_rays = 1u << 25;
   if (s->cfg.max_batch_requests == 0) s->cfg.max_batch_requests = 256;
+  if (s->cfg.step_rays == 0) s->cfg.step_rays = 1u << 22;
   if (s->cfg.max_batch_rays >= (1u << 31)) return RQ_ERROR_INVALID_ARGUMENT;
   // the server's own context: cube Morton normalisation (tighter LBVHs on
   // flat scenes; results do not depend on the tree)

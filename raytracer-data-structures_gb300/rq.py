@@ -105,7 +105,7 @@ class Plan:
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("batching", C.c_int32), ("hbm_budget", C.c_uint64),
-                ("max_batch_rays", C.c_uint32), ("max_batch_requests", C.c_uint32)]
+                ("max_batch_rays", C.c_uint32), ("max_batch_requests", C.c_uint32), ("step_rays", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -125,9 +125,9 @@ class Server:
     """rq_server_t: the serving loop (admission, HBM budget with LRU residency,
     continuous batching, latency statistics) on its own worker thread."""
 
-    def __init__(self, device=0, batching=True, hbm_budget=0, max_batch_rays=0, max_batch_requests=0):
+    def __init__(self, device=0, batching=True, hbm_budget=0, max_batch_rays=0, max_batch_requests=0, step_rays=0):
         lib = load()
-        cfg = ServerConfig(device, int(batching), hbm_budget, max_batch_rays, max_batch_requests)
+        cfg = ServerConfig(device, int(batching), hbm_budget, max_batch_rays, max_batch_requests, step_rays)
         self.handle = C.c_void_p()
         self._check(lib.rq_server_create(C.byref(cfg), C.byref(self.handle)))
         self._sizes = {}
