@@ -306,6 +306,7 @@ void BatchStore::view(uint32_t s, AccelBuffers& a) const {
   a.n_slots = n;
   a.max_depth = 0;
   a.node_width = 2;
+  a.unit_leaves = true;
 }
 
 }  // namespace rq

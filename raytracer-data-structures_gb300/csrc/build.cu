@@ -140,6 +140,7 @@ static BuildResult build_lbvh(const SceneView& s, const rq_settings_t& cfg, Acce
   a.n_nodes = n > 1 ? n - 1 : 0;
   a.n_slots = n;
   a.max_depth = 0;
+  a.unit_leaves = true;  // Karras leaves are single primitives
   return {};
 }
 
@@ -157,6 +158,7 @@ BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, 
                         BuildScratch& sc, uint32_t* err, cudaStream_t st) {
   if (s.n == 0) return BuildResult::error(RQ_ERROR_EMPTY_SCENE, "empty scene");
   a.node_width = 2;
+  a.unit_leaves = false;
   if (type == RQ_LBVH || type == RQ_BVH) {
     if (cfg.node_width != RQ_NODE_WIDTH_2 && cfg.node_width != 2 && cfg.node_width != RQ_NODE_WIDTH_4 &&
         cfg.node_width != RQ_NODE_WIDTH_8)
@@ -198,7 +200,7 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
     launch_trace_bvh8(s.kind, any, bvh8_view(a), q.rays, q.n, q.hits, q.occ, err, st);
   } else {
     Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
-               a.root.as<const float>(), a.n_nodes, a.n_slots};
+               a.root.as<const float>(), a.n_nodes, a.n_slots, a.unit_leaves ? 1u : 0u};
     launch_trace_bvh2(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, nullptr, q.small_stack,
                       q.exact);
   }
@@ -241,7 +243,7 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
     if (!r.ok()) return r;
   }
   Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
-             a.root.as<const float>(), a.n_nodes, a.n_slots};
+             a.root.as<const float>(), a.n_nodes, a.n_slots, a.unit_leaves ? 1u : 0u};
   if (top) {
     RQ_B(sc.top.ensure(64 * 64), "top-level copy");
     launch_trace_bvh2_top(s.kind, any, v, sc.top.as<float4>(), q.rays, q.n, q.hits, q.occ, err, perm, st);

@@ -33,11 +33,13 @@ struct AccelBuffers {
   uint32_t max_depth = 0;
   uint32_t node_width = 2;  // BVH2 structures: 2, or 4 / 8 when nodes4 holds a wide copy
   uint32_t n4_cap = 0;      // bound of the 4-wide node count (exact count: root word 6)
+  bool unit_leaves = false; // every BVH2 leaf holds one primitive (LBVH builds)
   void release() {
     nodes.release(); prims.release(); order.release(); codes.release(); root.release();
     kd_nodes.release(); kd_idx.release(); nodes4.release();
     n_nodes = n_slots = max_depth = n4_cap = 0;
     node_width = 2;
+    unit_leaves = false;
   }
   size_t device_bytes() const {
     return nodes.cap + prims.cap + order.cap + codes.cap + root.cap + kd_nodes.cap + kd_idx.cap + nodes4.cap;

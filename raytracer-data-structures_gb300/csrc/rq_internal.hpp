@@ -143,6 +143,7 @@ struct Bvh2View {
   const float* root;      // 6 floats
   uint32_t n_internal;
   uint32_t n_slots;
+  uint32_t unit_leaves = 0;  // 1: every leaf holds one primitive (LBVH): 4-byte stack entries
 };
 // perm (optional): trace ray perm[i] in thread i (results stay in caller order).
 // small_stack (a test hook): the FAST walk's stack holds kDebugStack entries,

@@ -32,7 +32,7 @@ constexpr int kThreads = 128;
 // walks are inlined and each ray takes the one it needs.
 // At most 48 registers (10 blocks of 128 per SM): measured 3-4% faster on
 // the closest-hit triangle walk than the unconstrained 52.
-template <int KIND, bool ANY, bool COUNT = false, int STACK = kStackSize, bool SPLIT = false>
+template <int KIND, bool ANY, bool COUNT = false, int STACK = kStackSize, bool SPLIT = false, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const float4* __restrict__ rays,
                                                          uint32_t n, float4* __restrict__ hits,
                                                          uint32_t* __restrict__ occ, uint32_t* err,
@@ -54,8 +54,8 @@ __global__ void __launch_bounds__(kThreads, 10) k_trace_fast(Bvh2View bvh, const
       if (zero_dir(sr)) {
         exact[1 + atomicAdd(exact, 1u)] = r;
       } else {
-        occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, sr, c, visits, tests, err);
-        if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+        occluded = walk_bvh2_form<KIND, ANY, COUNT, STACK, false, UNIT>(bvh, ray, sr, c, visits, tests, err);
+        if (!ANY) store_hit(hits, r, c);
       }
     }
   }
@@ -832,8 +832,12 @@ void dispatch_bvh2(int traversal, const Bvh2View& v, const float4* rays, uint32_
     k_trace_fast<KIND, ANY, false, kDebugStack><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr, perm);
   } else if (exact) {
     cudaMemsetAsync(exact, 0, 4, s);
-    k_trace_fast<KIND, ANY, false, kStackSize, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr,
-                                                                            perm, exact);
+    if (v.unit_leaves)
+      k_trace_fast<KIND, ANY, false, kStackSize, true, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err,
+                                                                                    nullptr, perm, exact);
+    else
+      k_trace_fast<KIND, ANY, false, kStackSize, true><<<g, kThreads, 0, s>>>(v, rays, n, hits, occ, err, nullptr,
+                                                                              perm, exact);
     count_launch();
     k_trace_exact<KIND, ANY><<<kExactBlocks, kThreads, 0, s>>>(v, rays, exact, hits, occ, err);
   } else {

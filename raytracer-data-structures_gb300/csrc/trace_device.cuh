@@ -1,6 +1,8 @@
 // Per-ray traversal device code shared by the one-structure kernels
 // (trace.cu) and the persistent many-structure kernel (trace_batched.cu).
 #pragma once
+#include <type_traits>
+
 #include "rq_device.cuh"
 #include "rq_internal.hpp"
 
@@ -11,8 +13,10 @@ struct Ray {
   float tmin, tmax;
 };
 
+// Rays are read once: streaming loads (evict first), which leave L1 and L2
+// to the tree's nodes and primitives.
 __device__ __forceinline__ Ray load_ray(const float4* __restrict__ rays, uint32_t r) {
-  float4 a = __ldg(rays + 2 * (size_t)r), b = __ldg(rays + 2 * (size_t)r + 1);
+  float4 a = __ldcs(rays + 2 * (size_t)r), b = __ldcs(rays + 2 * (size_t)r + 1);
   return {{a.x, a.y, a.z}, {b.x, b.y, b.z}, a.w, b.w};
 }
 
@@ -21,6 +25,10 @@ struct Closest {
   uint32_t prim;
   float u, v;
 };
+// Hits are written once: a streaming store.
+__device__ __forceinline__ void store_hit(float4* __restrict__ hits, uint32_t r, const Closest& c) {
+  __stcs(hits + r, make_float4(c.t, __uint_as_float(c.prim), c.u, c.v));
+}
 
 // Test the primitives of one leaf.  Returns true when an any-hit query is done.
 // FAST closest hit (REF = false) keeps the smallest t and, among primitives
@@ -94,13 +102,16 @@ __device__ __forceinline__ void load_node(const float4* nd, float4& a, float4& b
 // per-thread stack of STACK entries, boxes clipped to [tmin, closest hit].
 // EXACT: the exact-sign box test (rays with a zero direction component).
 // Returns true when an any-hit query found a hit.
-template <int KIND, bool ANY, bool COUNT, int STACK, bool EXACT>
+// UNIT: every leaf holds one primitive (LBVH), so a stack entry is the
+// 4-byte link alone: half the local-memory footprint, which shares L1 with
+// the nodes the walk fetches.
+template <int KIND, bool ANY, bool COUNT, int STACK, bool EXACT, bool UNIT = false>
 __device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& ray, const SlabRay& sr, Closest& c,
                                                uint32_t& visits, uint32_t& tests, uint32_t* err) {
   float tn;
   const float* rb = bvh.root;
   if (!slab_box<EXACT>(sr, ray.o, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], ray.tmin, ray.tmax, tn)) return false;
-  int2 stack[STACK];
+  typename std::conditional<UNIT, int, int2>::type stack[STACK];
   int sp = 0;
   int cur = bvh.n_internal ? 0 : -1;
   int cnt = bvh.n_internal ? 0 : (int)bvh.n_slots;
@@ -128,7 +139,8 @@ __device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& r
         int2 nearE = make_int2(l.x, l.z), farE = make_int2(l.y, l.w);
         if (tr < tl) { int2 t = nearE; nearE = farE; farE = t; }
         if (sp >= STACK) { atomicOr(err, kErrStackOverflow); return false; }
-        stack[sp++] = farE;
+        if constexpr (UNIT) stack[sp++] = farE.x;
+        else stack[sp++] = farE;
         cur = nearE.x;
         cnt = nearE.y;
         continue;
@@ -136,13 +148,18 @@ __device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& r
       if (hl) { cur = l.x; cnt = l.z; continue; }
       if (hr) { cur = l.y; cnt = l.w; continue; }
     } else {
+      if (UNIT) cnt = 1;
       if (COUNT) tests += test_count<KIND, ANY>(bvh.prims, (uint32_t)(~cur), cnt, ray);
       if (test_leaf<KIND, ANY, false>(bvh.prims, bvh.order, (uint32_t)(~cur), cnt, ray, c)) return true;
     }
     if (sp == 0) return false;
-    int2 e = stack[--sp];
-    cur = e.x;
-    cnt = e.y;
+    if constexpr (UNIT) {
+      cur = stack[--sp];
+    } else {
+      const int2 e = stack[--sp];
+      cur = e.x;
+      cnt = e.y;
+    }
   }
 }
 

@@ -165,7 +165,7 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
     uint32_t* counts = rs.list_n.as<uint32_t>();
     uint32_t n_live = (uint32_t)nray;
     const Bvh2View bv{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
-                      a.root.as<const float>(), a.n_nodes, a.n_slots};
+                      a.root.as<const float>(), a.n_nodes, a.n_slots, a.unit_leaves ? 1u : 0u};
     const Bvh4View b4{a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
                       a.root.as<const float>(), a.n_nodes, a.n_slots};
     const Bvh8View b8{a.nodes4.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
