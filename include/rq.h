@@ -554,8 +554,9 @@ rq_status_t rq_reference_spheres(const char* path, int32_t clones, float** spher
  *    (rebuilt when requested again).
  *  - Continuous batching (batching = 1): each step takes rows of the waiting
  *    requests in arrival order, up to step_rays camera rays and
- *    max_batch_requests requests (a larger request is split by rows and
- *    finished in later steps), and renders them as one wavefront (camera
+ *    max_batch_requests requests; while others wait, one request takes at
+ *    most half a step (a larger request is split by rows and finished in
+ *    later steps); the step renders them as one wavefront (camera
  *    rays, one many-structure closest-hit query, shading, one many-structure
  *    shadow query, pixels, one download).  Two steps are in flight at once on
  *    two streams: requests that arrive while one step runs go into the next,
@@ -574,7 +575,7 @@ typedef struct rq_server_config_t {
   uint64_t hbm_budget;         /* bytes of resident scenes + structures + wavefront buffers; 0: 80 GB */
   uint32_t max_batch_rays;     /* camera rays of one request at most; 0: 2^25 (below 2^31) */
   uint32_t max_batch_requests; /* requests (or parts of requests) per step; 0: 256 */
-  uint32_t step_rays;          /* batching: camera rays per step; larger requests are split by rows; 0: 2^22 */
+  uint32_t step_rays;          /* batching: camera rays per step; larger requests are split by rows; 0: 2^24 */
 } rq_server_config_t;
 typedef struct rq_request_t {
   uint32_t mesh_id;

@@ -570,32 +570,30 @@ void rq_server::run() {
           items.push_back({p, 0, p->req.height});
           p->next_row = p->req.height;
         } else {
-          // Rows of the waiting requests up to the step's ray budget: first
-          // an equal share of the budget each (at least one row), then what
-          // is left, in arrival order.  A request larger than its share is
-          // split by rows and finished in later steps, so requests that
-          // arrive behind a large one are not held up by all of it.
+          // Rows of the waiting requests, in arrival order, up to the step's
+          // ray budget.  While others wait, one request takes at most half
+          // of a step and is finished in later steps, so requests that
+          // arrive behind a large one start at the next step; steps stay
+          // few requests wide (their meshes stay in L2) and large (a step's
+          // fixed cost is small beside it).
           std::vector<Pending*> cand;
           for (Pending* p : queue) {
             cand.push_back(p);
             if (cand.size() >= cfg.max_batch_requests) break;
           }
           const uint64_t budget = cfg.step_rays;
-          const uint64_t share = std::max<uint64_t>(1, budget / cand.size());
+          const uint64_t cap = queue.size() > 1 ? std::max<uint64_t>(1, budget / 2) : budget;
           std::vector<uint32_t> take(cand.size(), 0);
           uint64_t used = 0;
-          for (int pass = 0; pass < 2; ++pass) {
-            for (size_t k = 0; k < cand.size(); ++k) {
-              const Pending* p = cand[k];
-              const uint64_t row_rays = (uint64_t)p->req.width * p->req.spp;
-              const uint64_t rows_left = p->req.height - p->next_row - take[k];
-              const uint64_t room = budget > used ? (budget - used) / row_rays : 0;
-              uint64_t t = pass == 0 ? std::min<uint64_t>(std::max<uint64_t>(1, share / row_rays), room) : room;
-              if (pass == 0 && used == 0 && t == 0) t = 1;  // a row wider than the budget still goes, alone
-              t = std::min<uint64_t>(t, rows_left);
-              take[k] += (uint32_t)t;
-              used += t * row_rays;
-            }
+          for (size_t k = 0; k < cand.size() && used < budget; ++k) {
+            const Pending* p = cand[k];
+            const uint64_t row_rays = (uint64_t)p->req.width * p->req.spp;
+            const uint64_t rows_left = p->req.height - p->next_row;
+            uint64_t t = std::min(budget - used, cap) / row_rays;
+            if (t == 0 && used == 0) t = 1;  // a row wider than the budget still goes, alone
+            t = std::min<uint64_t>(t, rows_left);
+            take[k] = (uint32_t)t;
+            used += t * row_rays;
           }
           for (size_t k = 0; k < cand.size(); ++k) {
             if (!take[k]) continue;
@@ -641,7 +639,7 @@ rq_status_t rq_server_create(const rq_server_config_t* cfg, rq_server_t* out) {
   if (s->cfg.hbm_budget == 0) s->cfg.hbm_budget = 80ull << 30;
   if (s->cfg.max_batch_rays == 0) s->cfg.max_batch_rays = 1u << 25;
   if (s->cfg.max_batch_requests == 0) s->cfg.max_batch_requests = 256;
-  if (s->cfg.step_rays == 0) s->cfg.step_rays = 1u << 22;
+  if (s->cfg.step_rays == 0) s->cfg.step_rays = 1u << 24;
   if (s->cfg.max_batch_rays >= (1u << 31)) return RQ_ERROR_INVALID_ARGUMENT;
   // the server's own context: cube Morton normalisation (tighter LBVHs on
   // flat scenes; results do not depend on the tree)
