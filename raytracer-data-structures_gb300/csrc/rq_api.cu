@@ -975,6 +975,8 @@ static rq_status_t batch_tables(rq_ctx_t ctx, const rq_accel_t* accels, uint32_t
   t.kind = accels[0]->scene->kind;
   t.any = any;
   t.width = (int)accels[0]->buf.node_width;
+  t.unit = true;
+  for (uint32_t k = 0; k < n; ++k) t.unit = t.unit && accels[k]->buf.unit_leaves;
   t.views = reinterpret_cast<const Bvh2View*>(base);
   t.roff = reinterpret_cast<const uint32_t*>(base + vbytes);
   t.n_views = n;

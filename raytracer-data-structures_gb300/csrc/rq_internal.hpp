@@ -234,6 +234,7 @@ struct BatchedTrace {
   uint32_t* work = nullptr;
   uint32_t* err = nullptr;
   const uint32_t* perm = nullptr;  // optional ray order: work index -> ray index
+  bool unit = false;               // every structure's leaves hold one primitive (LBVH)
 };
 // block: 128 or 256 threads; deep: the deeper of the two stack sizes.
 cudaError_t launch_trace_batched(const BatchedTrace& t, int block, int deep, cudaStream_t s);

@@ -456,6 +456,7 @@ bool rq_server::launch(Slot& sl, std::vector<Item>& items) {
   BatchedTrace t;
   t.kind = kTriangles;
   t.width = 2;
+  t.unit = true;  // the server builds LBVHs: single-primitive leaves
   t.views = reinterpret_cast<const Bvh2View*>(tb + a1);
   t.roff = d_roff;
   t.n_views = nq;

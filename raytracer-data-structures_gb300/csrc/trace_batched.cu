@@ -18,7 +18,9 @@ namespace {
 
 constexpr uint32_t kGrab = 256;  // rays a warp takes per counter access (8 passes of 32)
 
-template <int KIND, bool ANY, int W, int STACK, int BLOCK>
+// UNIT: every structure of the launch has single-primitive leaves (batched
+// LBVH builds): 4-byte stack entries.
+template <int KIND, bool ANY, int W, int STACK, int BLOCK, bool UNIT = false>
 __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restrict__ views,
                                                          const uint32_t* __restrict__ roff, uint32_t n_views,
                                                          const float4* __restrict__ rays, uint32_t n,
@@ -48,9 +50,9 @@ __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restr
           const Bvh8View v8{v.nodes, v.prims, v.order, v.root, v.n_internal, v.n_slots};
           occluded = walk_bvh8<KIND, ANY, false, STACK>(v8, ray, c, visits, tests, err);
         } else {
-          occluded = walk_bvh2<KIND, ANY, false, STACK>(v, ray, c, visits, tests, err);
+          occluded = walk_bvh2<KIND, ANY, false, STACK, UNIT>(v, ray, c, visits, tests, err);
         }
-        if (!ANY) hits[r] = make_float4(c.t, __uint_as_float(c.prim), c.u, c.v);
+        if (!ANY) store_hit(hits, r, c);
       }
       if (ANY) {
         if (perm) {  // bits of scattered rays: set one by one in the zeroed words
@@ -66,7 +68,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_batched(const Bvh2View* __restr
 
 template <int KIND, bool ANY, int W, int STACK, int BLOCK>
 cudaError_t launch_shape(const BatchedTrace& t, cudaStream_t s) {
-  auto k = k_trace_batched<KIND, ANY, W, STACK, BLOCK>;
+  auto k = (W == 2 && t.unit) ? k_trace_batched<KIND, ANY, W, STACK, BLOCK, true>
+                              : k_trace_batched<KIND, ANY, W, STACK, BLOCK, false>;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, BLOCK, 0);
   if (e != cudaSuccess) return e;

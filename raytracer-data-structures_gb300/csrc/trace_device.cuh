@@ -164,12 +164,12 @@ __device__ __forceinline__ bool walk_bvh2_form(const Bvh2View& bvh, const Ray& r
 }
 
 // walk_bvh2_form with the box test each ray needs.
-template <int KIND, bool ANY, bool COUNT, int STACK>
+template <int KIND, bool ANY, bool COUNT, int STACK, bool UNIT = false>
 __device__ __forceinline__ bool walk_bvh2(const Bvh2View& bvh, const Ray& ray, Closest& c, uint32_t& visits,
                                           uint32_t& tests, uint32_t* err) {
   const SlabRay sr = slab_ray(ray.o, ray.d);
-  return zero_dir(sr) ? walk_bvh2_form<KIND, ANY, COUNT, STACK, true>(bvh, ray, sr, c, visits, tests, err)
-                      : walk_bvh2_form<KIND, ANY, COUNT, STACK, false>(bvh, ray, sr, c, visits, tests, err);
+  return zero_dir(sr) ? walk_bvh2_form<KIND, ANY, COUNT, STACK, true, UNIT>(bvh, ray, sr, c, visits, tests, err)
+                      : walk_bvh2_form<KIND, ANY, COUNT, STACK, false, UNIT>(bvh, ray, sr, c, visits, tests, err);
 }
 
 // Sum the per-thread visit / test counts of a warp into counters[0..1].
