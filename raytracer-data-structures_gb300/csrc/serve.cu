@@ -127,6 +127,7 @@ struct Pending {
   std::vector<uint8_t> pixels;
   uint32_t next_row = 0;     // rows handed to steps (worker)
   uint32_t rows_landed = 0;  // rows whose step has landed or failed (worker)
+  int in_flight = 0;         // steps in flight with rows of this request (worker)
 };
 
 // A step's share of one request: image rows [y0, y0 + rows).
@@ -508,7 +509,10 @@ bool rq_server::launch(Slot& sl, std::vector<Item>& items) {
     for (size_t k = 0; k < n; ++k) land(items[k], sl.status[k], nullptr);
     return false;
   }
-  for (size_t j = 0; j < sl.which.size(); ++j) ++sl.mesh[sl.which[j]]->in_flight;
+  for (size_t j = 0; j < sl.which.size(); ++j) {
+    ++sl.mesh[sl.which[j]]->in_flight;
+    ++sl.items[sl.which[j]].p->in_flight;
+  }
   for (size_t k = 0; k < n; ++k)  // items that could not go ahead land now
     if (sl.status[k] != RQ_SUCCESS) land(items[k], sl.status[k], nullptr);
   sl.npix = npix;
@@ -540,6 +544,7 @@ void rq_server::retire(Slot& sl) {
   for (size_t j = 0; j < sl.which.size(); ++j) {
     const size_t k = sl.which[j];
     --sl.mesh[k]->in_flight;
+    --sl.items[k].p->in_flight;
     const rq_status_t stt =
         derr ? ((derr & kErrStackOverflow) ? RQ_ERROR_STACK_OVERFLOW : RQ_ERROR_INVALID_ARGUMENT) : RQ_SUCCESS;
     land(sl.items[k], stt, sl.host + 3 * (size_t)sl.poff[j]);
@@ -577,13 +582,18 @@ void rq_server::run() {
           // arrive behind a large one start at the next step; steps stay
           // few requests wide (their meshes stay in L2) and large (a step's
           // fixed cost is small beside it).
+          // A request with rows in flight waits for them (the other slot
+          // stays free for requests that arrive meanwhile); the two slots'
+          // wavefronts use at most half of the HBM budget.
           std::vector<Pending*> cand;
           for (Pending* p : queue) {
+            if (p->in_flight) continue;
             cand.push_back(p);
             if (cand.size() >= cfg.max_batch_requests) break;
           }
-          const uint64_t budget = cfg.step_rays;
-          const uint64_t cap = queue.size() > 1 ? std::max<uint64_t>(1, budget / 2) : budget;
+          const uint64_t budget =
+              std::max<uint64_t>(1, std::min<uint64_t>(cfg.step_rays, cfg.hbm_budget / (4 * kSampleBytes)));
+          const uint64_t cap = cand.size() > 1 ? std::max<uint64_t>(1, budget / 2) : budget;
           std::vector<uint32_t> take(cand.size(), 0);
           uint64_t used = 0;
           for (size_t k = 0; k < cand.size() && used < budget; ++k) {
@@ -614,7 +624,10 @@ void rq_server::run() {
           Slot* o = oldest_busy();
           if (o && o->landed.load()) return true;
           if (stop) return o == nullptr;
-          return free_slot() != nullptr && !queue.empty();
+          if (free_slot() == nullptr) return false;
+          for (const Pending* p : queue)
+            if (!p->in_flight) return true;
+          return false;
         });
         continue;
       }
