@@ -218,7 +218,7 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   const bool top = fast && cfg.scheduling == RQ_SCHEDULING_SHARED_TOP && !wide && !q.small_stack;
   QueryTarget qx = q;
   if (bvh2 && cfg.traversal == RQ_TRAVERSAL_FAST && a.node_width == 2 && !q.small_stack) {
-    RQ_B(sc.exact.ensure(((size_t)q.n + 1) * 4), "exact-ray list");
+    RQ_B(sc.exact.ensure(((size_t)q.n + 2) * 4), "exact-ray list");  // count, work counter, rays
     qx.exact = sc.exact.as<uint32_t>();
   }
   if (!sorted && !refill && !spec && !packet && !top) {

@@ -149,7 +149,7 @@ struct QueryTarget {
   float4* hits = nullptr;
   uint32_t* occ = nullptr;
   bool small_stack = false;  // test hook: FAST BVH2 walk with a traversal stack of kDebugStack entries
-  uint32_t* exact = nullptr;  // n + 1 words: rays set aside for the exact box test (launch_trace_bvh2)
+  uint32_t* exact = nullptr;  // n + 2 words: exact-ray count, work counter, rays set aside (launch_trace_bvh2)
 };
 // Batches of at least this many rays are reordered when settings.ray_sort asks.
 constexpr uint32_t kRaySortMin = 65536;

@@ -149,9 +149,10 @@ struct Bvh2View {
 // small_stack (a test hook): the FAST walk's stack holds kDebugStack entries,
 // so moderately deep trees overflow it.
 constexpr int kDebugStack = 8;
-// exact (optional): n + 1 words of scratch; FAST queries then walk the rays
-// that need the exact box test in a second, small launch, keeping the main
-// kernel to the fused walk.
+// exact (optional): n + 2 words of scratch; FAST queries then run as
+// persistent warps (word 1 their work counter) and walk the rays that need
+// the exact box test in a second, small launch, keeping the main kernel to
+// the fused walk.
 void launch_trace_bvh2(int kind, int traversal, bool any, const Bvh2View& v, const float4* rays,
                        uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s,
                        const uint32_t* perm = nullptr, bool small_stack = false, uint32_t* exact = nullptr);

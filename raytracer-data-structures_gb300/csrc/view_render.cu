@@ -156,7 +156,7 @@ cudaError_t render_view(int type, const SceneView& s, const AccelBuffers& a, con
     if ((e = rs.list_b.ensure(nray * 4)) != cudaSuccess) return e;
     if ((e = rs.list_s.ensure(nray * 4)) != cudaSuccess) return e;
     if ((e = rs.list_n.ensure(64)) != cudaSuccess) return e;
-    if ((e = sc.exact.ensure((nray + 1) * 4)) != cudaSuccess) return e;
+    if ((e = sc.exact.ensure((nray + 2) * 4)) != cudaSuccess) return e;  // count, work counter, rays
     uint32_t* exact = sc.exact.as<uint32_t>();
     uint32_t* live = nullptr;  // null: every sample (depth 0)
     uint32_t* next = rs.list_a.as<uint32_t>();
