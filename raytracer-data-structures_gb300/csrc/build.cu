@@ -193,7 +193,7 @@ void launch_query(int type, const SceneView& s, const AccelBuffers& a, int trave
   } else if (type == RQ_KDTREE) {
     KdView v{a.kd_nodes.as<const int4>(), a.kd_idx.as<const int32_t>(), a.prims.as<const float4>(),
              a.root.as<const float>(), a.n_nodes};
-    launch_trace_kd(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st);
+    launch_trace_kd(s.kind, traversal, any, v, q.rays, q.n, q.hits, q.occ, err, st, q.work);
   } else if (a.node_width == 4 && traversal == RQ_TRAVERSAL_FAST) {
     launch_trace_bvh4(s.kind, any, bvh4_view(a), q.rays, q.n, q.hits, q.occ, err, st);
   } else if (a.node_width == 8 && traversal == RQ_TRAVERSAL_FAST) {
@@ -217,6 +217,10 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   const bool packet = fast && cfg.scheduling == RQ_SCHEDULING_WARP_PACKET && !wide;
   const bool top = fast && cfg.scheduling == RQ_SCHEDULING_SHARED_TOP && !wide && !q.small_stack;
   QueryTarget qx = q;
+  if (type == RQ_KDTREE) {
+    RQ_B(sc.work.ensure(256), "traversal work counter");
+    qx.work = sc.work.as<uint32_t>();
+  }
   if (bvh2 && cfg.traversal == RQ_TRAVERSAL_FAST && a.node_width == 2 && !q.small_stack) {
     RQ_B(sc.exact.ensure(((size_t)q.n + 2) * 4), "exact-ray list");  // count, work counter, rays
     qx.exact = sc.exact.as<uint32_t>();

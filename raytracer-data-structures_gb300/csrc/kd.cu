@@ -625,13 +625,13 @@ struct Todo {
   float tMin, tMax;
 };
 
+// The walk of ray r; returns whether an any-hit query found a hit (closest-hit
+// queries store their hit).
 template <int KIND, bool ANY, bool REF>
-__global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, const float4* __restrict__ rays,
-                                                  uint32_t n, float4* __restrict__ hits,
-                                                  uint32_t* __restrict__ occ, uint32_t* err) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ bool kd_walk_ray(const KdView& kd, uint32_t n_nodes, const float4* __restrict__ rays,
+                                            uint32_t r, float4* __restrict__ hits, uint32_t* err) {
   bool occluded = false;
-  if (r < n) {
+  {
     float4 ra = __ldg(rays + 2 * (size_t)r), rb = __ldg(rays + 2 * (size_t)r + 1);
     F3 o = {ra.x, ra.y, ra.z}, d = {rb.x, rb.y, rb.z};
     const float rtmin = ra.w, rtmax = rb.w;
@@ -729,6 +729,15 @@ __global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, c
     }
     if (!ANY) hits[r] = make_float4(best, __uint_as_float(bprim), bu, bv);
   }
+  return occluded;
+}
+
+template <int KIND, bool ANY, bool REF>
+__global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, const float4* __restrict__ rays,
+                                                  uint32_t n, float4* __restrict__ hits,
+                                                  uint32_t* __restrict__ occ, uint32_t* err) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool occluded = r < n && kd_walk_ray<KIND, ANY, REF>(kd, n_nodes, rays, r, hits, err);
   if (ANY) {
     uint32_t bits = __ballot_sync(0xffffffffu, occluded);
     uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
@@ -736,14 +745,50 @@ __global__ void __launch_bounds__(128) k_trace_kd(KdView kd, uint32_t n_nodes, c
   }
 }
 
+// The same walk as persistent warps: a grid the GPU holds at once, each warp
+// taking the next 32 rays from a counter (work, zeroed) until none are left.
+template <int KIND, bool ANY, bool REF>
+__global__ void __launch_bounds__(128) k_trace_kd_warps(KdView kd, uint32_t n_nodes, const float4* __restrict__ rays,
+                                                        uint32_t n, float4* __restrict__ hits,
+                                                        uint32_t* __restrict__ occ, uint32_t* err, uint32_t* work) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const uint32_t r = base + lane;
+    const bool occluded = r < n && kd_walk_ray<KIND, ANY, REF>(kd, n_nodes, rays, r, hits, err);
+    if (ANY) {
+      const uint32_t bits = __ballot_sync(0xffffffffu, occluded);
+      if (lane == 0) occ[base >> 5] = bits;
+    }
+  }
+}
+
+template <typename K>
+uint32_t kd_resident_blocks(K k) {
+  int per_sm = 0, dev = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms < 1)
+    sms = 1;
+  return (uint32_t)(per_sm * sms);
+}
+
 template <int KIND, bool ANY>
 void dispatch_kd(int traversal, const KdView& v, uint32_t n_nodes, const float4* rays, uint32_t n, float4* hits,
-                 uint32_t* occ, uint32_t* err, cudaStream_t s) {
+                 uint32_t* occ, uint32_t* err, uint32_t* work, cudaStream_t s) {
   const unsigned g = (n + 127) / 128;
-  if (traversal == RQ_TRAVERSAL_REFERENCE)
+  if (work) {
+    cudaMemsetAsync(work, 0, 4, s);
+    const auto k = traversal == RQ_TRAVERSAL_REFERENCE ? k_trace_kd_warps<KIND, ANY, true> : k_trace_kd_warps<KIND, ANY, false>;
+    k<<<std::min(g, kd_resident_blocks(k)), 128, 0, s>>>(v, n_nodes, rays, n, hits, occ, err, work);
+  } else if (traversal == RQ_TRAVERSAL_REFERENCE) {
     k_trace_kd<KIND, ANY, true><<<g, 128, 0, s>>>(v, n_nodes, rays, n, hits, occ, err);
-  else
+  } else {
     k_trace_kd<KIND, ANY, false><<<g, 128, 0, s>>>(v, n_nodes, rays, n, hits, occ, err);
+  }
 }
 
 __global__ void k_box_union(const float* __restrict__ aabb, uint32_t n, int32_t* lohi) {
@@ -862,16 +907,16 @@ int bitlen(uint32_t v) {
 }  // namespace
 
 void launch_trace_kd(int kind, int traversal, bool any, const KdView& v, const float4* rays, uint32_t n,
-                     float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s) {
+                     float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s, uint32_t* work) {
   if (n == 0) return;
   count_launch();
   const uint32_t nn = v.n_nodes;
   if (kind == kTriangles) {
-    if (any) dispatch_kd<kTriangles, true>(traversal, v, nn, rays, n, hits, occ, err, s);
-    else dispatch_kd<kTriangles, false>(traversal, v, nn, rays, n, hits, occ, err, s);
+    if (any) dispatch_kd<kTriangles, true>(traversal, v, nn, rays, n, hits, occ, err, work, s);
+    else dispatch_kd<kTriangles, false>(traversal, v, nn, rays, n, hits, occ, err, work, s);
   } else {
-    if (any) dispatch_kd<kSpheres, true>(traversal, v, nn, rays, n, hits, occ, err, s);
-    else dispatch_kd<kSpheres, false>(traversal, v, nn, rays, n, hits, occ, err, s);
+    if (any) dispatch_kd<kSpheres, true>(traversal, v, nn, rays, n, hits, occ, err, work, s);
+    else dispatch_kd<kSpheres, false>(traversal, v, nn, rays, n, hits, occ, err, work, s);
   }
 }
 

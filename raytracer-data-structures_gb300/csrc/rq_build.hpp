@@ -150,6 +150,7 @@ struct QueryTarget {
   uint32_t* occ = nullptr;
   bool small_stack = false;  // test hook: FAST BVH2 walk with a traversal stack of kDebugStack entries
   uint32_t* exact = nullptr;  // n + 2 words: exact-ray count, work counter, rays set aside (launch_trace_bvh2)
+  uint32_t* work = nullptr;   // one word: the work counter of the persistent-warp KD walk (launch_trace_kd)
 };
 // Batches of at least this many rays are reordered when settings.ray_sort asks.
 constexpr uint32_t kRaySortMin = 65536;

@@ -253,8 +253,9 @@ struct KdView {
   const float* root;      // 6 floats
   uint32_t n_nodes;
 };
+// work (optional): one word of scratch; the walk then runs as persistent warps.
 void launch_trace_kd(int kind, int traversal, bool any, const KdView& v, const float4* rays,
-                     uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s);
+                     uint32_t n, float4* hits, uint32_t* occ, uint32_t* err, cudaStream_t s, uint32_t* work = nullptr);
 
 // --------------------------------------------------------- median BVH
 struct MedianScratch;
