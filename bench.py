@@ -861,8 +861,11 @@ def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_
     rays = len(primary) + len(secondary) + len(shadow)
     h2d = hv.nbytes + hi.nbytes + hp.nbytes + hs.nbytes + hsh.nbytes
     d2h = out_p.nbytes + out_s.nbytes + out_b.nbytes
+    # value from the mean step (every step counts); median and fastest step beside
+    # it show a disturbed run (a shared host's memory traffic slows the copies)
     return {"value": round(rays / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3)}
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3),
+            "ms_median": round(float(np.median(times)) * 1e3, 3), "ms_min": round(float(np.min(times)) * 1e3, 3)}
 
 
 # -------------------------------------------------------------- CPU baseline
