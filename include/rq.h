@@ -86,7 +86,7 @@ typedef struct rq_settings_t {
 /* How FAST queries on binary BVH structures map rays to GPU threads.  Speed
  * only: every ray walks the same nodes in the same order either way. */
 typedef enum rq_scheduling_t {
-  RQ_SCHEDULING_THREAD_PER_RAY = 0, /* one thread per ray */
+  RQ_SCHEDULING_THREAD_PER_RAY = 0, /* each thread walks one ray at a time; warps take 32 rays at a time from a counter */
   RQ_SCHEDULING_LANE_REFILL = 1,    /* persistent warps refill finished lanes with new rays */
   RQ_SCHEDULING_SPECULATIVE = 2,    /* while-while walk that postpones leaves until the warp has one each */
   RQ_SCHEDULING_WARP_PACKET = 3,    /* the warp walks one shared stack (lane masks per entry): coherent rays */
