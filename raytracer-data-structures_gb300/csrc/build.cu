@@ -154,41 +154,6 @@ static BuildResult build_none(const SceneView& s, AccelBuffers& a, cudaStream_t 
   return {};
 }
 
-namespace {
-// Sets *flag when a leaf child of a binary node holds other than one
-// primitive (links: the node's fourth float4, (left, right, left count,
-// right count), a leaf child's link negative).
-__global__ void k_unit_leaves(const float4* __restrict__ nodes, uint32_t n_internal, uint32_t* __restrict__ flag) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_internal; i += gridDim.x * blockDim.x) {
-    const int4 l = __ldg(reinterpret_cast<const int4*>(nodes + 4 * (size_t)i + 3));
-    if ((l.x < 0 && l.z != 1) || (l.y < 0 && l.w != 1)) atomicOr(flag, 1u);
-  }
-}
-}  // namespace
-
-// Whether every leaf of a median BVH holds one primitive (the median split
-// leaves a range whole only when its centroids cannot be split): then its
-// queries use the one-primitive-leaf walk (4-byte stack entries).
-static BuildResult median_unit_leaves(AccelBuffers& a, BuildScratch& sc, cudaStream_t st) {
-  a.unit_leaves = false;
-  if (a.n_nodes == 0) {
-    a.unit_leaves = a.n_slots == 1;
-    return {};
-  }
-  RQ_B(sc.work.ensure(256), "leaf check");
-  uint32_t* flag = sc.work.as<uint32_t>();
-  RQ_B(cudaMemsetAsync(flag, 0, 4, st), "leaf check");
-  count_launch();
-  k_unit_leaves<<<std::min<uint32_t>((a.n_nodes + 255) / 256, 1024u), 256, 0, st>>>(a.nodes.as<const float4>(),
-                                                                                     a.n_nodes, flag);
-  RQ_B(cudaGetLastError(), "leaf check");
-  uint32_t h = 1;
-  RQ_B(cudaMemcpyAsync(&h, flag, 4, cudaMemcpyDeviceToHost, st), "leaf check");
-  RQ_B(cudaStreamSynchronize(st), "leaf check");
-  a.unit_leaves = h == 0;
-  return {};
-}
-
 BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, AccelBuffers& a,
                         BuildScratch& sc, uint32_t* err, cudaStream_t st) {
   if (s.n == 0) return BuildResult::error(RQ_ERROR_EMPTY_SCENE, "empty scene");
@@ -199,7 +164,6 @@ BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, 
         cfg.node_width != RQ_NODE_WIDTH_8)
       return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "node_width must be 2, 4 or 8");
     BuildResult r = type == RQ_LBVH ? build_lbvh(s, cfg, a, sc, err, st) : build_median_bvh(s, a, sc, err, st);
-    if (r.ok() && type == RQ_BVH) r = median_unit_leaves(a, sc, st);
     if (r.ok() && cfg.node_width == RQ_NODE_WIDTH_4) r = collapse_bvh4(a, sc, err, st);
     if (r.ok() && cfg.node_width == RQ_NODE_WIDTH_8) r = collapse_bvh8(a, sc, err, st);
     return r;
