@@ -244,14 +244,16 @@ def run_ours(args):
                    rq.SCHEDULING_SPECULATIVE: "speculative", rq.SCHEDULING_WARP_PACKET: "warp_packet",
                    rq.SCHEDULING_SHARED_TOP: "shared_top"}
     morton_names = {rq.MORTON_SCENE_BOUNDS: "scene_bounds", rq.MORTON_SCENE_CUBE: "scene_cube"}
+    quality_names = {rq.LBVH_KARRAS: "karras", rq.LBVH_TREELETS: "treelets"}
     tuning = {}
     best = None
-    candidates = [(w, m) for w in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4, rq.NODE_WIDTH_8) for m in morton_names]
+    candidates = [(w, m, q) for w in (rq.NODE_WIDTH_2, rq.NODE_WIDTH_4, rq.NODE_WIDTH_8) for m in morton_names
+                  for q in quality_names]
     if args.no_tune:  # the live tuner's choice on a GB300, for profiling the same kernel mix
-        candidates = [(rq.NODE_WIDTH_2, rq.MORTON_SCENE_CUBE)]
-    for width, morton in candidates:
+        candidates = [(rq.NODE_WIDTH_2, rq.MORTON_SCENE_CUBE, rq.LBVH_TREELETS)]
+    for width, morton, quality in candidates:
         if True:
-            eng.configure(node_width=width, morton=morton, ray_sort=rq.RAY_SORT_NONE,
+            eng.configure(node_width=width, morton=morton, lbvh_quality=quality, ray_sort=rq.RAY_SORT_NONE,
                           scheduling=rq.SCHEDULING_THREAD_PER_RAY)
             cand = eng.build(scene, rq.LBVH)
             choice, total = {}, timed(cand.rebuild)
@@ -267,24 +269,25 @@ def run_ours(args):
                     eng.configure(ray_sort=srt, scheduling=sch)
                     opts[(srt, sch)] = timed(class_call(cand, name))
                 choice[name] = min(opts, key=opts.get)
-                log(f"[bench] tune width {width} {morton_names[morton]} {name}: " +
+                log(f"[bench] tune width {width} {morton_names[morton]} {quality_names[quality]} {name}: " +
                     ", ".join(f"{sort_names[a]}/{sched_names[b]} {t:.3f}" for (a, b), t in sorted(opts.items(), key=lambda kv: kv[1])))
                 total += opts[choice[name]]
-            tuning[f"width{max(width, 2)}_{morton_names[morton]}"] = {
+            tuning[f"width{max(width, 2)}_{morton_names[morton]}_{quality_names[quality]}"] = {
                 "est_step_ms": round(total, 4),
                 "choice": {k: [sort_names[v[0]], sched_names[v[1]]] for k, v in choice.items()}}
             if best is None or total < best[0]:
                 if best is not None:
                     best[1].close()
-                best = (total, cand, (width, morton), choice)
+                best = (total, cand, (width, morton, quality), choice)
             else:
                 cand.close()
     acc.close()
-    _, acc, (node_width, morton_mode), sort_choice = best
-    eng.configure(node_width=node_width, morton=morton_mode, ray_sort=rq.RAY_SORT_NONE,
+    _, acc, (node_width, morton_mode, lbvh_quality), sort_choice = best
+    eng.configure(node_width=node_width, morton=morton_mode, lbvh_quality=lbvh_quality, ray_sort=rq.RAY_SORT_NONE,
                   scheduling=rq.SCHEDULING_THREAD_PER_RAY)
     node_bytes = 128 if node_width in (rq.NODE_WIDTH_4, rq.NODE_WIDTH_8) else NODE_BYTES
-    log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}, morton {morton_names[morton_mode]}")
+    log(f"[bench] tuning: {tuning} -> width {max(node_width, 2)}, morton {morton_names[morton_mode]}, "
+        f"lbvh {quality_names[lbvh_quality]}")
 
     # Traversal work of each query on these exact rays (the byte model's inputs).
     counts = {}
@@ -342,7 +345,7 @@ def run_ours(args):
         v, t = counts[name]
         return n * RAY_BYTES + (n * HIT_BYTES if closest else ((n + 31) // 32) * 4) + v * node_bytes + t * TRI_BYTES
 
-    build_bytes = build_bytes_per_tri() * n_tri
+    build_bytes = build_bytes_per_tri(lbvh_quality == rq.LBVH_TREELETS) * n_tri
     alg = {"build": build_bytes, "trace_primary": trace_bytes("primary", n_p),
            "trace_secondary": trace_bytes("secondary", n_s), "trace_shadow": trace_bytes("shadow", n_sh, False)}
     achieved = alg[dom] / (kern[dom] * 1e-3) / 1e9
@@ -433,6 +436,7 @@ def run_ours(args):
                                           "step rebuilds the LBVH and traces all three sets"),
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "node_width": max(node_width, 2), "morton": morton_names[morton_mode],
+                       "lbvh_quality": quality_names[lbvh_quality],
                        "ray_sort": {k: sort_names[v[0]] for k, v in sort_choice.items()},
                        "scheduling": {k: sched_names[v[1]] for k, v in sort_choice.items()}, "tuning": tuning},
             "lbvh_build_mtri_s": round(n_tri / (build_ms * 1e-3) / 1e6, 2),
@@ -445,7 +449,7 @@ def run_ours(args):
                                for k, v in counts.items()},
             "roofline": roofline,
             "build_roofline": {"achieved": round(build_bytes / (build_ms * 1e-3) / 1e9, 1), "peak": peak,
-                               "unit": "GB/s", "bytes_per_tri": build_bytes_per_tri(),
+                               "unit": "GB/s", "bytes_per_tri": build_bytes_per_tri(lbvh_quality == rq.LBVH_TREELETS),
                                "frac": round(build_bytes / (build_ms * 1e-3) / 1e9 / peak, 4)},
             "structures": structures,
             "render": render,
@@ -808,14 +812,15 @@ def run_serve_leg(args):
     return out
 
 
-def build_bytes_per_tri():
+def build_bytes_per_tri(treelets=False):
     """Compulsory bytes per triangle of the LBVH build kernels:
     bounds 6 (12 B per vertex, 0.5 vertex per triangle) + Morton 26 (12 B indices,
     6 B vertices, 8 B code/index write) + 4 sort passes x 16 + Karras 28 (code
     read 4, links 16, parents 8) + refit 150 (order 4, indices 12, vertices 6,
     48 B payload write, 24 B child box write, 48 B sibling reread per internal
-    node, 4 B parent link, 4 B flag)."""
-    return 6 + 26 + 64 + 28 + 150
+    node, 4 B parent link, 4 B flag); with the treelet pass + 140 per internal
+    node (64 B node read and write, 4 B cost write, 8 B parent links)."""
+    return 6 + 26 + 64 + 28 + 150 + (140 if treelets else 0)
 
 
 def run_e2e(eng, scene, acc, verts, idx, primary, secondary, shadow, args, sort_choice):
@@ -1031,7 +1036,7 @@ def run_case(args):
     torch.cuda.set_stream(stream)
     eng = rq.Engine(0)
     eng.set_stream(stream.cuda_stream)
-    eng.configure(morton=rq.MORTON_SCENE_CUBE)  # the tuner's build choice (see --no-tune)
+    eng.configure(morton=rq.MORTON_SCENE_CUBE, lbvh_quality=args.lbvh_quality)  # the tuner's build choice (--no-tune)
     if args.case in ("batched", "build-batched"):
         meshes, ray_n, offs = c4_workload(32 if args.small else 256)
         sc = [eng.scene_triangles(v, f) for v, f in meshes]
@@ -1140,9 +1145,12 @@ def main():
     ap.add_argument("--ray-sort", type=int, default=0, help="ray reordering for --case")
     ap.add_argument("--node-width", type=int, default=2, choices=[2, 4, 8], help="--case: settings.node_width")
     ap.add_argument("--scheduling", type=int, default=0, help="--case: settings.scheduling (0-3)")
+    ap.add_argument("--lbvh-quality", type=int, default=0, choices=[0, 1],
+                    help="--case: settings.lbvh_quality (1: treelet restructuring)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner and use its GB300 choice (binary nodes, cube Morton codes, "
-                         "octant ray order for secondary rays): profiling the measured kernel mix")
+                         "treelet restructuring, octant ray order for secondary rays): profiling the measured "
+                         "kernel mix")
     args = ap.parse_args()
     if args.case:
         run_case(args)

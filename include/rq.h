@@ -80,7 +80,8 @@ typedef struct rq_settings_t {
   int32_t ray_sort;           /* rq_ray_sort_t: reorder large FAST batches for coherence */
   int32_t node_width;         /* rq_node_width_t: BVH node fan-out for FAST queries (RQ_BVH, RQ_LBVH) */
   int32_t scheduling;         /* rq_scheduling_t: how FAST binary-BVH queries map rays to threads */
-  int32_t reserved[2];
+  int32_t lbvh_quality;       /* rq_lbvh_quality_t: RQ_LBVH tree after the Karras build, RQ_LBVH_KARRAS */
+  int32_t reserved[1];
 } rq_settings_t;
 
 /* How FAST queries on binary BVH structures map rays to GPU threads.  Speed
@@ -108,6 +109,20 @@ typedef enum rq_node_width_t {
   RQ_NODE_WIDTH_4 = 4,
   RQ_NODE_WIDTH_8 = 8
 } rq_node_width_t;
+
+/* The RQ_LBVH tree.  RQ_LBVH_KARRAS keeps the Karras radix-tree topology
+ * over the sorted Morton codes.  RQ_LBVH_TREELETS then runs one bottom-up
+ * pass of treelet restructuring (Karras and Aila 2013): at every internal node
+ * the treelet of up to four leaves grown from it (largest-area internal leaf
+ * expanded first) is rebuilt with the topology of least surface-area cost,
+ * the tree's own nodes reused.  On the 998,000-triangle terrain the walks
+ * visit about 10% fewer nodes.  Hits and occlusion bits do not change; the
+ * exported topology does.  Single-structure builds only (rq_build_batched
+ * keeps the Karras tree). */
+typedef enum rq_lbvh_quality_t {
+  RQ_LBVH_KARRAS = 0,
+  RQ_LBVH_TREELETS = 1
+} rq_lbvh_quality_t;
 
 /* Ray reordering before FAST BVH2 traversal of batches of at least 65,536
  * rays.  Results are written in the caller's order either way and do not

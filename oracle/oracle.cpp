@@ -926,6 +926,147 @@ int orc_build_lbvh(const uint32_t* codes, const float* aabb6, uint32_t n, float*
   return 0;
 }
 
+namespace treelet {
+constexpr int kTreeletLeaves = 4;  // the engine's kOptLeaves
+struct TB { float lo[3], hi[3]; };
+static void grow(TB& a, const TB& b) {
+  for (int k = 0; k < 3; ++k) { a.lo[k] = std::fmin(a.lo[k], b.lo[k]); a.hi[k] = std::fmax(a.hi[k], b.hi[k]); }
+}
+static float half_area(const TB& b) {
+  const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+struct Tree {
+  float* nd;
+  int32_t link(int id, int side) const { int32_t v; std::memcpy(&v, nd + 16 * (size_t)id + 12 + side, 4); return v; }
+  TB box(int id, int side) const {
+    const float* q = nd + 16 * (size_t)id;
+    TB b;
+    b.lo[0] = q[4 * side + 0]; b.hi[0] = q[4 * side + 1]; b.lo[1] = q[4 * side + 2]; b.hi[1] = q[4 * side + 3];
+    b.lo[2] = q[8 + 2 * side]; b.hi[2] = q[9 + 2 * side];
+    return b;
+  }
+  void set(int id, int32_t l, const TB& bl, int32_t r, const TB& br) {
+    float* q = nd + 16 * (size_t)id;
+    q[0] = bl.lo[0]; q[1] = bl.hi[0]; q[2] = bl.lo[1]; q[3] = bl.hi[1];
+    q[4] = br.lo[0]; q[5] = br.hi[0]; q[6] = br.lo[1]; q[7] = br.hi[1];
+    q[8] = bl.lo[2]; q[9] = bl.hi[2]; q[10] = br.lo[2]; q[11] = br.hi[2];
+    const int32_t w[4] = {l, r, l < 0 ? 1 : 0, r < 0 ? 1 : 0};
+    std::memcpy(q + 12, w, 16);
+  }
+};
+static int low_index(int s) { int k = 0; while (!((s >> k) & 1)) ++k; return k; }
+// Least sum of internal half areas over the topologies of the N treelet
+// leaves (a leaf costs 0): subsets S in increasing order, parts P of S holding
+// S's lowest leaf in decreasing order, first least best[P] + best[S ^ P]; the
+// chosen subsets take the pool's nodes in decreasing subset order.
+static void rebuild(Tree& t, int N, const int32_t* code, const TB* box, const int* pool) {
+  const int F = (1 << N) - 1;
+  float best[32];
+  int split[32];
+  for (int k = 0; k < N; ++k) best[1 << k] = 0.f;
+  for (int S = 1; S <= F; ++S) {
+    if ((S & (S - 1)) == 0) continue;
+    const int low = S & -S;
+    float acc = INFINITY;
+    int accp = 0;
+    for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
+      if (!(P & low)) continue;
+      const float c = best[P] + best[S ^ P];
+      if (c < acc) { acc = c; accp = P; }
+    }
+    TB u = box[low_index(S)];
+    for (int b = 0; b < N; ++b)
+      if ((S >> b) & 1) grow(u, box[b]);
+    best[S] = half_area(u) + acc;
+    split[S] = accp;
+  }
+  uint32_t used = 1u << F;
+  for (int S = F; S >= 3; --S)
+    if ((S & (S - 1)) && ((used >> S) & 1u)) used |= (1u << split[S]) | (1u << (S ^ split[S]));
+  int id_of[32];
+  int next = 0;
+  for (int S = F; S >= 3; --S)
+    if ((S & (S - 1)) && ((used >> S) & 1u)) id_of[S] = pool[next++];
+  for (int S = F; S >= 3; --S) {
+    if (!(S & (S - 1)) || !((used >> S) & 1u)) continue;
+    const int P = split[S], Q = S ^ P;
+    int32_t cl = 0, cr = 0;
+    TB bl = box[0], br = box[0];
+    bool fl = false, fr = false;
+    for (int b = 0; b < N; ++b) {
+      if (P == (1 << b)) cl = code[b];
+      if (Q == (1 << b)) cr = code[b];
+      if ((P >> b) & 1) { if (fl) grow(bl, box[b]); else bl = box[b]; fl = true; }
+      if ((Q >> b) & 1) { if (fr) grow(br, box[b]); else br = box[b]; fr = true; }
+    }
+    if (P & (P - 1)) cl = id_of[P];
+    if (Q & (Q - 1)) cr = id_of[Q];
+    t.set(id_of[S], cl, bl, cr, br);
+  }
+}
+static void restructure(Tree& t, int x) {
+  int32_t code[kTreeletLeaves];
+  TB box[kTreeletLeaves];
+  int pool[kTreeletLeaves - 1];
+  code[0] = t.link(x, 0); code[1] = t.link(x, 1);
+  box[0] = t.box(x, 0); box[1] = t.box(x, 1);
+  pool[0] = x;
+  int n = 2;
+  for (int step = 0; step < kTreeletLeaves - 2; ++step) {
+    int pick = -1;
+    float pa = -1.f;
+    for (int k = 0; k < n; ++k)
+      if (code[k] >= 0) {
+        const float a = half_area(box[k]);
+        if (a > pa) { pa = a; pick = k; }
+      }
+    if (pick < 0) break;
+    const int c = code[pick];
+    pool[step + 1] = c;
+    const int32_t l = t.link(c, 0), r = t.link(c, 1);
+    const TB b0 = t.box(c, 0), b1 = t.box(c, 1);
+    code[pick] = l; box[pick] = b0;
+    code[n] = r; box[n] = b1;
+    ++n;
+  }
+  if (n >= 3) rebuild(t, n, code, box, pool);
+}
+}  // namespace treelet
+
+void orc_treelet_opt(float* nodes16, uint32_t n_internal) {
+  if (n_internal < 2) return;
+  treelet::Tree t{nodes16};
+  // leaf counts (post-order) and the top-node rule
+  std::vector<uint32_t> leaves(n_internal, 0), order;
+  order.reserve(n_internal);
+  std::vector<std::pair<int, int>> st{{0, 0}};
+  while (!st.empty()) {  // iterative post-order: (node, children pushed)
+    auto [v, done] = st.back();
+    st.pop_back();
+    if (done) { order.push_back(v); continue; }
+    st.push_back({v, 1});
+    for (int side = 1; side >= 0; --side) {
+      const int32_t c = t.link(v, side);
+      if (c >= 0) st.push_back({c, 0});
+    }
+  }
+  uint32_t n_top = 0;
+  for (int v : order) {
+    uint32_t s = 0;
+    for (int side = 0; side < 2; ++side) { const int32_t c = t.link(v, side); s += c < 0 ? 1u : leaves[c]; }
+    leaves[v] = s;
+    if (s > 2048) ++n_top;
+  }
+  const bool skip_top = n_top > 2048;
+  std::vector<uint8_t> top(n_internal, 0);
+  for (int v : order) top[v] = leaves[v] > 2048;
+  for (int v : order) {
+    if (skip_top && top[v]) continue;
+    treelet::restructure(t, v);
+  }
+}
+
 // Flattened median BVH: internal nodes numbered breadth-first (left before
 // right), leaf slots assigned left to right, each leaf's primitives ordered by
 // (centroid.x, id).

@@ -66,6 +66,17 @@ void orc_refit(uint32_t n, const int32_t* left, const int32_t* right, const floa
                float* nodes16, float* root_bounds6);
 int orc_build_lbvh(const uint32_t* codes, const float* aabb6, uint32_t n, float* nodes16,
                    uint32_t* order, uint32_t* sorted_codes, float* root_bounds6);
+/* The engine's RQ_LBVH_TREELETS pass (csrc/treelet.cu), in place on the 16-word
+ * nodes of an LBVH with one primitive per leaf: post-order over the tree, at
+ * each internal node the treelet of up to four leaves grown from it (largest
+ * half area first, first of equals) is rebuilt with the topology of least sum
+ * of internal half areas (dynamic program over leaf subsets, first minimum in
+ * the engine's enumeration order), reusing the treelet's nodes (the root
+ * first, then in expansion order, assigned to the chosen subsets in
+ * decreasing subset order).  Nodes of more than 2048 leaves are left as they
+ * are when there are more than 2048 of them (the engine's top-node block
+ * capacity).  No reference counterpart. */
+void orc_treelet_opt(float* nodes16, uint32_t n_internal);
 
 /* ---- median BVH (constructBVHNew, accelerators.h:246-337) ---- */
 /* compat = 0: the engine's deterministic rule; 1: replay of the reference's

@@ -166,6 +166,13 @@ def build_lbvh(codes, aabb):
     return Bvh2(nodes, max(n - 1, 0), rb, order, sk)
 
 
+def treelet_opt(bvh):
+    """The engine's RQ_LBVH_TREELETS pass on a copy of an LBVH (one primitive per leaf)."""
+    nodes = np.ascontiguousarray(bvh.nodes, np.float32).copy()
+    lib().orc_treelet_opt(_p(nodes), C.c_uint32(bvh.n_internal))
+    return Bvh2(nodes, bvh.n_internal, bvh.root_bounds, bvh.order, bvh.sorted_codes)
+
+
 def build_median(aabb, cen, compat=False):
     """compat=False: the engine's deterministic median rule; True: replay of
     the reference's std::partition / std::nth_element sequence."""

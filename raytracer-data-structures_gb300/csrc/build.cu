@@ -133,9 +133,15 @@ static BuildResult build_lbvh(const SceneView& s, const rq_settings_t& cfg, Acce
   uint32_t* mk = sc.mark.as<uint32_t>();
   const RefitTop top{mk, mk + n, mk + refit_treelet_offset(n), flags + (n > 1 ? n - 1 : 0)};
   launch_karras(codes, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(), top, st);
+  const bool treelets = cfg.lbvh_quality == RQ_LBVH_TREELETS && n > 2;
+  if (treelets) RQ_B(sc.heights.ensure(n), "treelet scratch");
   RQ_B(launch_refit(s.kind, s.verts4, s.idx4, s.sph, order, n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(),
-                    top, flags, a.prims.as<float4>(), a.root.as<float>(), err, st),
+                    top, flags, a.prims.as<float4>(), a.root.as<float>(), err, st,
+                    treelets ? sc.heights.as<uint8_t>() : nullptr),
        "LBVH refit launch");
+  if (treelets)
+    RQ_B(launch_treelet_opt(n, a.nodes.as<float4>(), sc.parent.as<uint32_t>(), top, sc.heights.as<uint8_t>(), err, st),
+         "LBVH treelet launch");
   RQ_B(cudaGetLastError(), "LBVH launch");
   a.n_nodes = n > 1 ? n - 1 : 0;
   a.n_slots = n;
@@ -159,6 +165,8 @@ BuildResult build_accel(int type, const SceneView& s, const rq_settings_t& cfg, 
   if (s.n == 0) return BuildResult::error(RQ_ERROR_EMPTY_SCENE, "empty scene");
   a.node_width = 2;
   a.unit_leaves = false;
+  if (cfg.lbvh_quality != RQ_LBVH_KARRAS && cfg.lbvh_quality != RQ_LBVH_TREELETS)
+    return BuildResult::error(RQ_ERROR_INVALID_ARGUMENT, "lbvh_quality must be RQ_LBVH_KARRAS or RQ_LBVH_TREELETS");
   if (type == RQ_LBVH || type == RQ_BVH) {
     if (cfg.node_width != RQ_NODE_WIDTH_2 && cfg.node_width != 2 && cfg.node_width != RQ_NODE_WIDTH_4 &&
         cfg.node_width != RQ_NODE_WIDTH_8)

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_karras(const uint32_t* __restrict_
 struct RefitShared {
   float box[kTreeletSpan][2][6];  // child boxes of the treelet's internal nodes, by index - first slot
   uint32_t up[kTreeletSpan];      // their parent words
-  uint32_t arrived[kTreeletSpan]; // children finished (2: the node is finished)
+  uint32_t arrived[kTreeletSpan]; // children finished (2: the node is finished), + their heights << 8
   uint32_t next;                  // the block's next treelet
 };
 
@@ -151,7 +151,10 @@ __device__ __forceinline__ void climb_top(uint32_t pw, Box6 b, bool top_mode, fl
 // lo, every internal node has its index in [lo, lo + c) and both children in
 // the treelet: one block gathers the leaves' primitives, climbs with
 // shared-memory boxes and arrival bits (block-scope ordering only) and at
-// the end stores the finished nodes' boxes, coalesced.
+// the end stores the finished nodes' boxes, coalesced.  heights (optional):
+// each internal node's height (longest path to a leaf, leaves 0), from the
+// children's heights added into the arrival words.
+template <bool HEIGHTS>
 __global__ void __launch_bounds__(kTreeletThreads, kTreeletBlocksPerSM) k_refit(int kind, const float4* __restrict__ verts,
                                                           const uint4* __restrict__ idx,
                                                           const float4* __restrict__ sph,
@@ -160,7 +163,8 @@ __global__ void __launch_bounds__(kTreeletThreads, kTreeletBlocksPerSM) k_refit(
                                                           const uint32_t* __restrict__ treelets,
                                                           uint32_t* count,  // [0] top nodes, [1] treelets, [2] treelet queue
                                                           uint32_t* flags, float4* __restrict__ prims,
-                                                          float* __restrict__ root_out, uint32_t* err) {
+                                                          float* __restrict__ root_out, uint32_t* err,
+                                                          uint8_t* __restrict__ heights) {
   extern __shared__ __align__(16) unsigned char refit_smem[];
   RefitShared& sh = *reinterpret_cast<RefitShared*>(refit_smem);
   if (n == 1) {
@@ -209,6 +213,7 @@ __global__ void __launch_bounds__(kTreeletThreads, kTreeletBlocksPerSM) k_refit(
       if (!live) continue;
       uint32_t pw = __ldg(parent + (n - 1) + j);
       bool at_root = cnt == 1;  // b is the treelet root's box
+      uint32_t h = 0;           // height of the subtree whose box is b
       for (uint32_t step = 0; !at_root; ++step) {
         const uint32_t node = pw >> 1, side = pw & 1u;
         const uint32_t x = node - lo;
@@ -216,12 +221,17 @@ __global__ void __launch_bounds__(kTreeletThreads, kTreeletBlocksPerSM) k_refit(
         float* mine = sh.box[x][side];
         for (int k = 0; k < 3; ++k) { mine[k] = b.lo[k]; mine[3 + k] = b.hi[k]; }
         __threadfence_block();
-        if (atomicAdd(&sh.arrived[x], 1u) == 1u) {  // second: finish the node
+        const uint32_t old = atomicAdd(&sh.arrived[x], HEIGHTS ? 1u + (h << 8) : 1u);
+        if ((old & 0xFFu) == 1u) {  // second: finish the node
           __threadfence_block();
           const float* L = sh.box[x][0];
           const float* R = sh.box[x][1];
           for (int k = 0; k < 3; ++k) { b.lo[k] = fminf(L[k], R[k]); b.hi[k] = fmaxf(L[3 + k], R[3 + k]); }
           pw = sh.up[x];
+          if constexpr (HEIGHTS) {
+            h = 1u + max(h, old >> 8);
+            sh.up[x] = h;  // nothing reads x's parent word after this climb: it keeps x's height
+          }
           at_root = node == root;
         } else {
           break;
@@ -240,7 +250,8 @@ __global__ void __launch_bounds__(kTreeletThreads, kTreeletBlocksPerSM) k_refit(
     // consecutive threads on consecutive float4s.
     for (uint32_t f = threadIdx.x; f < 3 * cnt; f += blockDim.x) {
       const uint32_t w = f / 3, c = f - 3 * w;
-      if (sh.arrived[w] != 2u) continue;  // not an internal node of this treelet
+      if ((sh.arrived[w] & 0xFFu) != 2u) continue;  // not an internal node of this treelet
+      if (HEIGHTS && c == 0) heights[lo + w] = (uint8_t)min(sh.up[w], 255u);
       const float* L = sh.box[w][0];
       const float* R = sh.box[w][1];
       nodes[4 * (size_t)(lo + w) + c] = c == 0 ? make_float4(L[0], L[3], L[1], L[4])
@@ -356,7 +367,7 @@ void launch_karras(const uint32_t* sorted_codes, uint32_t n, float4* nodes, uint
 cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const float4* sph,
                          const uint32_t* order, uint32_t n, float4* nodes, const uint32_t* parent,
                          const RefitTop& t, uint32_t* flags, float4* prims, float* root_out, uint32_t* err,
-                         cudaStream_t s) {
+                         cudaStream_t s, uint8_t* heights) {
   if (n == 0) return cudaSuccess;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -364,7 +375,9 @@ cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const 
   static std::atomic<uint64_t> attr_set{0};  // devices whose kernels allow their shared memory
   const uint64_t bit = 1ull << (dev & 63);
   if (!(attr_set.load() & bit)) {
-    e = cudaFuncSetAttribute(k_refit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RefitShared));
+    e = cudaFuncSetAttribute(k_refit<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RefitShared));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_refit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RefitShared));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_refit_top, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TopShared));
     if (e != cudaSuccess) return e;
@@ -373,8 +386,9 @@ cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const 
   // Persistent: kTreeletBlocksPerSM treelet blocks per SM take treelets from a queue.
   const uint32_t blocks = n == 1 ? 1u : kTreeletBlocksPerSM * (uint32_t)device_sm_count();
   count_launch();
-  k_refit<<<blocks, kTreeletThreads, sizeof(RefitShared), s>>>(kind, verts, idx, sph, order, n, nodes, parent,
-                                                               t.treelets, t.count, flags, prims, root_out, err);
+  const auto k = heights ? k_refit<true> : k_refit<false>;
+  k<<<blocks, kTreeletThreads, sizeof(RefitShared), s>>>(kind, verts, idx, sph, order, n, nodes, parent, t.treelets,
+                                                         t.count, flags, prims, root_out, err, heights);
   if (n < 2) return cudaGetLastError();
   count_launch();
   k_refit_top<<<1, kRefitTopThreads, sizeof(TopShared), s>>>(nodes, parent, t.mark, t.top, t.count, root_out, err);

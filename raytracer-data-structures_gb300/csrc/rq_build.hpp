@@ -59,11 +59,13 @@ struct BuildScratch {
   DevBuf work;                // work counter of lane-refill traversal
   DevBuf top;                 // top-level node copy of RQ_SCHEDULING_SHARED_TOP queries
   DevBuf exact;               // rays that need the exact box test, set aside by FAST queries
+  DevBuf heights;             // LBVH treelet restructuring: internal node heights (bytes)
   const uint32_t* stall = nullptr;  // sort test hook (SortScratch::stall); null in normal use
   void release() {
     work.release();
     top.release();
     exact.release();
+    heights.release();
     keys_alt.release(); vals_alt.release(); zero.release(); parent.release(); mark.release(); lohi.release();
     keys.release(); vals.release();
     m0.release(); m1.release(); m2.release(); m3.release(); m4.release(); m5.release(); m6.release(); m7.release();

@@ -111,11 +111,17 @@ void launch_karras(const uint32_t* sorted_codes, uint32_t n, float4* nodes, uint
 // Gathers each slot's primitive into the slot-ordered payload and computes
 // every node box: treelets in shared memory, one block each, then the top
 // nodes in one block (or by device-scope climbing when they exceed its
-// capacity); root_out gets 6 floats.
+// capacity); root_out gets 6 floats.  heights (optional, n - 1 bytes): the
+// height of every internal node below the top nodes.
 cudaError_t launch_refit(int kind, const float4* verts, const uint4* idx, const float4* sph,
                          const uint32_t* order, uint32_t n, float4* nodes, const uint32_t* parent,
                          const RefitTop& top, uint32_t* flags, float4* prims, float* root_out, uint32_t* err,
-                         cudaStream_t s);
+                         cudaStream_t s, uint8_t* heights = nullptr);
+// One bottom-up pass of four-leaf treelet restructuring over a refitted LBVH
+// of n one-primitive leaves (the refit decomposition of launch_karras; its
+// treelet queue word top.count[3] must be zero; heights from launch_refit).
+cudaError_t launch_treelet_opt(uint32_t n, float4* nodes, const uint32_t* parent, const RefitTop& top,
+                               const uint8_t* heights, uint32_t* err, cudaStream_t s);
 // Payload in primitive-id order (KD and brute force) plus per-primitive boxes.
 void launch_prims_by_id(int kind, const float* verts, const uint32_t* idx, const float4* sph,
                         uint32_t n, float4* prims, float* aabb6, cudaStream_t s);

@@ -24,6 +24,7 @@ NODE_WIDTH_2, NODE_WIDTH_4, NODE_WIDTH_8 = 0, 4, 8
 SCHEDULING_THREAD_PER_RAY, SCHEDULING_LANE_REFILL, SCHEDULING_SPECULATIVE, SCHEDULING_WARP_PACKET = 0, 1, 2, 3
 SCHEDULING_SHARED_TOP = 4
 MORTON_SCENE_BOUNDS, MORTON_REFERENCE, MORTON_SCENE_CUBE = 0, 1, 2
+LBVH_KARRAS, LBVH_TREELETS = 0, 1
 # SceneModel (settings.h:4)
 IGEA, ARMADILLO, BUNNY_MODEL, BUNNIES, TEST, GRASS, BUDDHA, CITY = range(8)
 DEVICE_POINTERS = 0x1
@@ -43,7 +44,8 @@ class Settings(C.Structure):
                 ("backgroundColor", C.c_float * 3), ("bias", C.c_float), ("aa_samples", C.c_uint32),
                 ("dataStructure", C.c_int32), ("sceneModel", C.c_int32), ("traversal", C.c_int32),
                 ("morton", C.c_int32), ("kd_max_depth", C.c_int32), ("ray_sort", C.c_int32),
-                ("node_width", C.c_int32), ("scheduling", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("node_width", C.c_int32), ("scheduling", C.c_int32), ("lbvh_quality", C.c_int32),
+                ("reserved", C.c_int32 * 1)]
 
 
 class AccelInfo(C.Structure):
