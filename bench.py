@@ -527,7 +527,11 @@ def run_render_legs(eng, stream, dev, args):
         res = {"triangles": int(len(idx)), "image": f"{width}x{height}x{spp}", "bounces": view_kw["bounces"]}
         cam = scenes.pinhole_rays(width, height, spp, eye=view_kw["eye"], target=view_kw["target"],
                                   up=view_kw["up"], fov_deg=view_kw["fov_deg"], seed=SEED + 7) if count_work else None
-        for name in structures:
+        runs = [(name, q) for name in structures
+                for q in ((rq.LBVH_KARRAS, rq.LBVH_TREELETS) if name == "LBVH" else (None,))]
+        for name, quality in runs:
+            if quality is not None:
+                eng.configure(lbvh_quality=quality)
             acc = eng.build(scene, name)
             _, _, cnt = eng.render(acc, view)  # synchronous: the ray counts
             rays = int(cnt.sum())
@@ -553,11 +557,23 @@ def run_render_legs(eng, stream, dev, args):
                 rtimes.append(m[1].elapsed_time(m[2]))
             eng.synchronize()
             t, tr = float(np.mean(times)), float(np.mean(rtimes))
-            res[name] = {"frame_ms": round(t, 3), "render_ms": round(tr, 3), "build_ms": round(t - tr, 3),
-                         "rays": rays, "ray_counts": [int(c) for c in cnt],
-                         "grays_s": round(rays / (t * 1e-3) / 1e9, 4)}
+            entry = {"frame_ms": round(t, 3), "render_ms": round(tr, 3), "build_ms": round(t - tr, 3),
+                     "rays": rays, "ray_counts": [int(c) for c in cnt],
+                     "grays_s": round(rays / (t * 1e-3) / 1e9, 4)}
             if work:
-                res[name]["traversal_work"] = work
+                entry["traversal_work"] = work
+            if quality is not None:  # the LBVH with either build setting: the faster frame is the entry
+                qn = "treelets" if quality == rq.LBVH_TREELETS else "karras"
+                entry["lbvh_quality"] = qn
+                prev = res.get(name)
+                if prev is not None:
+                    if prev["frame_ms"] <= entry["frame_ms"]:
+                        prev["other_lbvh_quality_frame_ms"] = {qn: entry["frame_ms"]}
+                        entry = None
+                    else:
+                        entry["other_lbvh_quality_frame_ms"] = {prev["lbvh_quality"]: prev["frame_ms"]}
+            if entry is not None:
+                res[name] = entry
             acc.close()
         scene.close()
         return res
