@@ -648,7 +648,8 @@ def run_batch_leg(eng, stream, dev, args):
     meshes, ray_n, offs = c4_workload(n_sc)
     n_tri = int(sum(len(f) for _, f in meshes))
     saved = eng.settings
-    eng.configure(ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY)
+    # the Karras trees the batched rebuild makes, for the one-scene-per-launch path too
+    eng.configure(ray_sort=rq.RAY_SORT_NONE, scheduling=rq.SCHEDULING_THREAD_PER_RAY, lbvh_quality=rq.LBVH_KARRAS)
     sc = [eng.scene_triangles(v, f) for v, f in meshes]
     n_rays = int(offs[-1])
     d_rays = batch_rays(torch, dev, meshes, ray_n.tolist(), SEED + 41)
