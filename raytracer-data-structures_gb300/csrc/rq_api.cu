@@ -424,7 +424,10 @@ rq_status_t rq_accel_import_bvh2(rq_ctx_t ctx, rq_scene_t scene, const float* no
     if (order[k] >= scene->n) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "order entry is not a primitive id");
   // Every link must stay inside the arrays, so a walk never reads outside
   // them; what is left unchecked (cycles, boxes that do not bound their
-  // primitives) is caught or tolerated by the walks' own bounds.
+  // primitives) is caught or tolerated by the walks' own bounds.  A tree whose
+  // leaves all hold one primitive (an exported LBVH, for one) is walked with
+  // 4-byte stack entries, as the engine's own LBVH.
+  bool unit = n_nodes > 0;
   for (uint32_t i = 0; i < n_nodes; ++i) {
     const float* nd = nodes + 16 * (size_t)i;
     if (!finite3(nd, 12)) return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "node box not finite");
@@ -435,6 +438,7 @@ rq_status_t rq_accel_import_bvh2(rq_ctx_t ctx, rq_scene_t scene, const float* no
       if (link >= 0 ? (uint32_t)link >= n_nodes
                     : (count < 1 || (uint64_t)(uint32_t)(~link) + (uint64_t)count > n_slots))
         return fail(ctx, RQ_ERROR_INVALID_ARGUMENT, "node link outside the node or slot arrays");
+      if (link < 0 && count != 1) unit = false;
     }
   }
   rq_accel* a = new (std::nothrow) rq_accel();
@@ -468,6 +472,7 @@ rq_status_t rq_accel_import_bvh2(rq_ctx_t ctx, rq_scene_t scene, const float* no
   b.n_nodes = n_nodes;
   b.n_slots = n_slots;
   b.node_width = 2;
+  b.unit_leaves = unit;
   *out = a;
   return RQ_SUCCESS;
 }

@@ -150,7 +150,8 @@ def test_imported_export_traces_like_the_original(engine, oracle, rqm):
     lo, hi = oracle.bounds3(v)
     rays = scenes.incoherent_rays(lo, hi, 8192, seed=30)
     s = engine.scene_triangles(v, f)
-    for kind in (rqm.LBVH, rqm.BVH):
+    for kind, quality in ((rqm.LBVH, rqm.LBVH_KARRAS), (rqm.LBVH, rqm.LBVH_TREELETS), (rqm.BVH, rqm.LBVH_KARRAS)):
+        engine.configure(lbvh_quality=quality)  # one-primitive leaves (LBVH, either tree) or several (BVH)
         acc = engine.build(s, kind)
         nodes, order, _, root, _ = engine.export_bvh2(acc)
         imp = engine.import_bvh2(s, nodes, order, root)
