@@ -242,17 +242,24 @@ BuildResult launch_query_sorted(int type, const SceneView& s, const AccelBuffers
   if (sorted) {
     // Coherence order: sort (octant | origin Morton, index) pairs, then trace
     // through the permutation; results keep the caller's order.
-    RQ_B(sc.keys.ensure((size_t)q.n * 4), "ray sort scratch");
     RQ_B(sc.vals.ensure((size_t)q.n * 4), "ray sort scratch");
-    uint32_t* keys = sc.keys.as<uint32_t>();
     uint32_t* p = sc.vals.as<uint32_t>();
-    const int passes = cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON12 ? 2
-                       : (cfg.ray_sort == RQ_RAY_SORT_OCTANT || cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON3) ? 1 : 4;
-    RQ_B(sc.zero.ensure(zero_words(q.n, passes) * 4), "sort scratch");
-    RQ_B(cudaMemsetAsync(sc.zero.p, 0, (1024 + 16 + sort_status_words(q.n, passes)) * 4, st), "memset");
-    launch_ray_keys(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, keys, p, st, sc.zero.as<uint32_t>(), passes);
-    BuildResult r = sort_perm(keys, p, q.n, passes, sc, err, st, &perm);
-    if (!r.ok()) return r;
+    if (cfg.ray_sort == RQ_RAY_SORT_OCTANT || cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON3) {
+      // keys of 3 or 6 bits: a stable counting sort, same order
+      RQ_B(sc.keys.ensure(ray_order_small_bytes(q.n, cfg.ray_sort)), "ray sort scratch");
+      launch_ray_order_small(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, sc.keys.p, p, st);
+      RQ_B(cudaGetLastError(), "ray order launch");
+      perm = p;
+    } else {
+      RQ_B(sc.keys.ensure((size_t)q.n * 4), "ray sort scratch");
+      uint32_t* keys = sc.keys.as<uint32_t>();
+      const int passes = cfg.ray_sort == RQ_RAY_SORT_OCTANT_MORTON12 ? 2 : 4;
+      RQ_B(sc.zero.ensure(zero_words(q.n, passes) * 4), "sort scratch");
+      RQ_B(cudaMemsetAsync(sc.zero.p, 0, (1024 + 16 + sort_status_words(q.n, passes)) * 4, st), "memset");
+      launch_ray_keys(q.rays, q.n, a.root.as<const float>(), cfg.ray_sort, keys, p, st, sc.zero.as<uint32_t>(), passes);
+      BuildResult r = sort_perm(keys, p, q.n, passes, sc, err, st, &perm);
+      if (!r.ok()) return r;
+    }
   }
   Bvh2View v{a.nodes.as<const float4>(), a.prims.as<const float4>(), a.order.as<const uint32_t>(),
              a.root.as<const float>(), a.n_nodes, a.n_slots, a.unit_leaves ? 1u : 0u};

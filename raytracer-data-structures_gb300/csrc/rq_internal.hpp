@@ -186,6 +186,12 @@ void launch_trace_bvh2_spec(int kind, bool any, const Bvh2View& v, const float4*
 // Coherence sort keys (mode: rq_ray_sort_t other than NONE, 30 bits); vals = identity.
 // With hist (zeroed, 256 words per pass) it also counts the sort's `passes`
 // digits, as launch_histogram would.
+// Ray orders of at most 6 key bits (RQ_RAY_SORT_OCTANT, RQ_RAY_SORT_OCTANT_MORTON3)
+// as a stable counting sort: perm gets the order the stable radix sort of the
+// same keys gives; scratch: ray_order_small_bytes(n, mode) bytes.
+size_t ray_order_small_bytes(uint32_t n, int mode);
+void launch_ray_order_small(const float4* rays, uint32_t n, const float* root, int mode, void* scratch,
+                            uint32_t* perm, cudaStream_t s);
 void launch_ray_keys(const float4* rays, uint32_t n, const float* root, int mode, uint32_t* keys, uint32_t* vals,
                      cudaStream_t s, uint32_t* hist = nullptr, int passes = 0);
 // FAST traversal that also sums internal-node visits and primitive tests

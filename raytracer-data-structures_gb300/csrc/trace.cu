@@ -1051,6 +1051,47 @@ __device__ __forceinline__ uint32_t spread_bits(uint32_t v) {  // 10 bits -> eve
   return v;
 }
 
+// The sort key of ray i under `mode` (the table above).
+__device__ __forceinline__ uint32_t ray_sort_key(const float4* __restrict__ rays, uint32_t i,
+                                                 const float* __restrict__ root, int mode) {
+  uint32_t key = 0;
+  const float4 b = __ldg(rays + 2 * (size_t)i + 1);
+  const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
+  if (mode == RQ_RAY_SORT_OCTANT) {
+    key = oct;
+  } else {
+    const float4 a = __ldg(rays + 2 * (size_t)i);
+    const float o[3] = {a.x, a.y, a.z};
+    const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4
+                      : mode == RQ_RAY_SORT_OCTANT_MORTON3 ? 1 : 5;
+    const float cells = (float)(1u << obits);
+    uint32_t q[3];
+    for (int k = 0; k < 3; ++k) {
+      float lo = root[k], ext = root[3 + k] - root[k];
+      float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
+      u = fminf(fmaxf(u * cells, 0.f), cells - 1.f);
+      q[k] = (uint32_t)u;
+    }
+    const uint32_t morton = (spread_bits(q[0]) << 2) | (spread_bits(q[1]) << 1) | spread_bits(q[2]);
+    if (mode == RQ_RAY_SORT_OCTANT_MORTON) {
+      key = (oct << 27) | morton;
+    } else if (mode == RQ_RAY_SORT_OCTANT_MORTON12) {
+      key = (oct << 12) | morton;
+    } else if (mode == RQ_RAY_SORT_OCTANT_MORTON3) {
+      key = (oct << 3) | morton;
+    } else {
+      const float len = sqrtf(b.x * b.x + b.y * b.y + b.z * b.z);
+      const float inv = len > 0.f ? 1.0f / len : 0.f;
+      const uint32_t dx = (uint32_t)fminf(fabsf(b.x) * inv * 64.f, 63.f);
+      const uint32_t dy = (uint32_t)fminf(fabsf(b.y) * inv * 64.f, 63.f);
+      const uint32_t dir = (dx << 6) | dy;
+      key = mode == RQ_RAY_SORT_ORIGIN_DIRECTION ? (oct << 27) | (morton << 12) | dir
+                                                 : (oct << 27) | (dir << 15) | morton;
+    }
+  }
+  return key;
+}
+
 // Sort keys of the optional ray order, and (when hist is given) the digit
 // histogram of the sort's `passes` 8-bit digits in the same read: a block
 // of 256 threads strides over the rays, counts in shared memory with one
@@ -1072,40 +1113,7 @@ __global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ ray
     const bool live = i < n;
     uint32_t key = 0;
     if (live) {
-      const float4 b = __ldg(rays + 2 * (size_t)i + 1);
-      const uint32_t oct = (b.x < 0.f ? 4u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 1u : 0u);
-      if (mode == RQ_RAY_SORT_OCTANT) {
-        key = oct;
-      } else {
-        const float4 a = __ldg(rays + 2 * (size_t)i);
-        const float o[3] = {a.x, a.y, a.z};
-        const int obits = mode == RQ_RAY_SORT_OCTANT_MORTON ? 9 : mode == RQ_RAY_SORT_OCTANT_MORTON12 ? 4
-                          : mode == RQ_RAY_SORT_OCTANT_MORTON3 ? 1 : 5;
-        const float cells = (float)(1u << obits);
-        uint32_t q[3];
-        for (int k = 0; k < 3; ++k) {
-          float lo = root[k], ext = root[3 + k] - root[k];
-          float u = ext > 0.f ? (o[k] - lo) / ext : 0.f;
-          u = fminf(fmaxf(u * cells, 0.f), cells - 1.f);
-          q[k] = (uint32_t)u;
-        }
-        const uint32_t morton = (spread_bits(q[0]) << 2) | (spread_bits(q[1]) << 1) | spread_bits(q[2]);
-        if (mode == RQ_RAY_SORT_OCTANT_MORTON) {
-          key = (oct << 27) | morton;
-        } else if (mode == RQ_RAY_SORT_OCTANT_MORTON12) {
-          key = (oct << 12) | morton;
-        } else if (mode == RQ_RAY_SORT_OCTANT_MORTON3) {
-          key = (oct << 3) | morton;
-        } else {
-          const float len = sqrtf(b.x * b.x + b.y * b.y + b.z * b.z);
-          const float inv = len > 0.f ? 1.0f / len : 0.f;
-          const uint32_t dx = (uint32_t)fminf(fabsf(b.x) * inv * 64.f, 63.f);
-          const uint32_t dy = (uint32_t)fminf(fabsf(b.y) * inv * 64.f, 63.f);
-          const uint32_t dir = (dx << 6) | dy;
-          key = mode == RQ_RAY_SORT_ORIGIN_DIRECTION ? (oct << 27) | (morton << 12) | dir
-                                                     : (oct << 27) | (dir << 15) | morton;
-        }
-      }
+      key = ray_sort_key(rays, i, root, mode);
       keys[i] = key;
       vals[i] = i;
     }
@@ -1127,6 +1135,131 @@ __global__ void __launch_bounds__(256) k_ray_keys(const float4* __restrict__ ray
       if (v) atomicAdd(hist + k, v);
     }
   }
+}
+
+// Ray orders of at most 6 key bits (RQ_RAY_SORT_OCTANT, RQ_RAY_SORT_OCTANT_MORTON3)
+// by a stable counting sort instead of a radix pass (whose decoupled look-back
+// runs across thousands of tiles): per block of kOrderSpan rays the key bytes
+// and the keys' counts (one shared atomic per distinct key in a warp), an
+// exclusive scan of the counts in bucket-major order (one block), then each
+// block places its rays -- a ray's position is its bucket's offset for the
+// block plus the same-key rays before it in the block (earlier rounds, earlier
+// warps of its round, earlier lanes of its warp).  The permutation is the
+// stable sort's.
+constexpr uint32_t kOrderThreads = 256, kOrderRounds = 16, kOrderSpan = kOrderThreads * kOrderRounds;
+constexpr uint32_t kOrderWarps = kOrderThreads / 32, kOrderMaxBuckets = 64, kOrderNone = 64;
+
+__global__ void __launch_bounds__(kOrderThreads) k_order_count(const float4* __restrict__ rays, uint32_t n,
+                                                               const float* __restrict__ root, int mode,
+                                                               uint32_t buckets, uint8_t* __restrict__ key8,
+                                                               uint32_t* __restrict__ counts) {
+  __shared__ uint32_t sh[kOrderMaxBuckets];
+  const uint32_t lane = threadIdx.x & 31u;
+  if (threadIdx.x < kOrderMaxBuckets) sh[threadIdx.x] = 0u;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * kOrderSpan;
+  for (uint32_t r = 0; r < kOrderRounds; ++r) {
+    const uint32_t i = base + r * kOrderThreads + threadIdx.x;
+    uint32_t k = kOrderNone;
+    if (i < n) {
+      k = ray_sort_key(rays, i, root, mode);
+      key8[i] = (uint8_t)k;
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, k);
+    if (k < kOrderNone && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&sh[k], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < buckets; k += blockDim.x) counts[(size_t)k * gridDim.x + blockIdx.x] = sh[k];
+}
+
+// Exclusive scan of m words in place, one block of 1024 threads (each a
+// contiguous run of the words, read with its loads in flight together).
+__global__ void __launch_bounds__(1024) k_order_scan(uint32_t* __restrict__ counts, uint32_t m) {
+  __shared__ uint32_t part[1024];
+  const uint32_t per = (m + blockDim.x - 1) / blockDim.x;
+  const uint32_t b = min(threadIdx.x * per, m), e = min(b + per, m);
+  uint32_t sum = 0;
+#pragma unroll 16
+  for (uint32_t k = b; k < e; ++k) sum += __ldcg(counts + k);
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+    const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - sum;
+#pragma unroll 16
+  for (uint32_t k = b; k < e; ++k) {
+    const uint32_t c = __ldcg(counts + k);
+    counts[k] = run;
+    run += c;
+  }
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_order_scatter(const uint8_t* __restrict__ key8, uint32_t n,
+                                                                 uint32_t buckets,
+                                                                 const uint32_t* __restrict__ offsets,
+                                                                 uint32_t* __restrict__ perm) {
+  __shared__ uint32_t run[kOrderMaxBuckets];
+  __shared__ uint32_t wcnt[kOrderRounds][kOrderWarps][kOrderMaxBuckets];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t k = threadIdx.x; k < buckets; k += blockDim.x) run[k] = offsets[(size_t)k * gridDim.x + blockIdx.x];
+  for (uint32_t k = threadIdx.x; k < kOrderRounds * kOrderWarps * kOrderMaxBuckets; k += blockDim.x)
+    (&wcnt[0][0][0])[k] = 0u;
+  const uint32_t base = blockIdx.x * kOrderSpan;
+  uint32_t key[kOrderRounds], peers[kOrderRounds];
+#pragma unroll
+  for (uint32_t r = 0; r < kOrderRounds; ++r) {
+    const uint32_t i = base + r * kOrderThreads + threadIdx.x;
+    key[r] = i < n ? (uint32_t)key8[i] : kOrderNone;
+  }
+  __syncthreads();
+  // every round's per-warp counts at once, then one pass of placements
+#pragma unroll
+  for (uint32_t r = 0; r < kOrderRounds; ++r) {
+    peers[r] = __match_any_sync(0xffffffffu, key[r]);
+    if (key[r] < kOrderNone && lane == (uint32_t)(__ffs(peers[r]) - 1)) wcnt[r][warp][key[r]] = __popc(peers[r]);
+  }
+  __syncthreads();
+  // prefix over (round, warp) per bucket, in place: wcnt[r][w][b] becomes the
+  // count of bucket b in earlier rounds and earlier warps of round r
+  for (uint32_t b = threadIdx.x; b < buckets; b += blockDim.x) {
+    uint32_t acc = run[b];
+    for (uint32_t r = 0; r < kOrderRounds; ++r)
+      for (uint32_t w = 0; w < kOrderWarps; ++w) {
+        const uint32_t c = wcnt[r][w][b];
+        wcnt[r][w][b] = acc;
+        acc += c;
+      }
+  }
+  __syncthreads();
+#pragma unroll
+  for (uint32_t r = 0; r < kOrderRounds; ++r) {
+    const uint32_t k = key[r];
+    if (k < kOrderNone)
+      perm[wcnt[r][warp][k] + (uint32_t)__popc(peers[r] & ((1u << lane) - 1u))] = base + r * kOrderThreads + threadIdx.x;
+  }
+}
+
+size_t ray_order_small_bytes(uint32_t n, int mode) {
+  const size_t buckets = mode == RQ_RAY_SORT_OCTANT ? 8 : 64;
+  const size_t blocks = (n + kOrderSpan - 1) / kOrderSpan;
+  return (((size_t)n + 15) & ~(size_t)15) + 4 * buckets * blocks;
+}
+
+void launch_ray_order_small(const float4* rays, uint32_t n, const float* root, int mode, void* scratch,
+                            uint32_t* perm, cudaStream_t s) {
+  if (n == 0) return;
+  const uint32_t buckets = mode == RQ_RAY_SORT_OCTANT ? 8u : 64u;
+  const uint32_t blocks = (n + kOrderSpan - 1) / kOrderSpan;
+  uint8_t* key8 = static_cast<uint8_t*>(scratch);
+  uint32_t* counts = reinterpret_cast<uint32_t*>(key8 + (((size_t)n + 15) & ~(size_t)15));
+  count_launch(3);
+  k_order_count<<<blocks, kOrderThreads, 0, s>>>(rays, n, root, mode, buckets, key8, counts);
+  k_order_scan<<<1, 1024, 0, s>>>(counts, buckets * blocks);
+  k_order_scatter<<<blocks, kOrderThreads, 0, s>>>(key8, n, buckets, counts, perm);
 }
 
 void launch_ray_keys(const float4* rays, uint32_t n, const float* root, int mode, uint32_t* keys, uint32_t* vals,

@@ -43,7 +43,8 @@ def test_warp_walks_at_odd_ray_counts(engine, oracle, rqm, mesh, acc_name, n_ray
         tree = bvh2_from_export(oracle, nodes, order, root, codes)
         want = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.CLOSEST, tree, prims, rays)
         occ = oracle.trace_bvh2(oracle.TRIANGLES, oracle.FAST, oracle.ANY, tree, prims, rays)
-    for sort in (rqm.RAY_SORT_NONE, rqm.RAY_SORT_OCTANT):
+    # none; octant and octant + 3-bit origin (counting sort); octant + origin Morton (radix sort)
+    for sort in (rqm.RAY_SORT_NONE, rqm.RAY_SORT_OCTANT, rqm.RAY_SORT_OCTANT_MORTON3, rqm.RAY_SORT_OCTANT_MORTON):
         engine.configure(ray_sort=sort)  # orders only binary-BVH queries of 65,536 rays or more
         assert np.array_equal(_u32(engine.trace_closest(acc, rays)), _u32(want)), (acc_name, n_rays, sort)
         assert np.array_equal(rqm.unpack_bits(engine.trace_any(acc, rays), n_rays), occ), (acc_name, n_rays, sort)
