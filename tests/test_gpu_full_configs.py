@@ -42,11 +42,13 @@ def _sample(n, frac, seed):
     return np.sort(rng.choice(n, size=max(1, int(n * frac)), replace=False))
 
 
-def test_c2_full_workload_one_percent_sample_matches_oracle(engine, oracle, rqm):
+@pytest.mark.parametrize("quality", ["LBVH_KARRAS", "LBVH_TREELETS"])
+def test_c2_full_workload_one_percent_sample_matches_oracle(engine, oracle, rqm, quality):
     import bench
     verts, idx, primary = bench.make_inputs()
     assert len(idx) == 998_000 and len(primary) == 1920 * 1080 * 4
-    engine.configure(morton=rqm.MORTON_SCENE_CUBE)  # the benchmark's tuned build
+    # the benchmark's tuned build (cube Morton codes, treelet restructuring) and the Karras tree
+    engine.configure(morton=rqm.MORTON_SCENE_CUBE, lbvh_quality=getattr(rqm, quality))
     s = engine.scene_triangles(verts, idx)
     acc = engine.build(s, rqm.LBVH)
     hits_p = engine.trace_closest(acc, primary)
